@@ -1,0 +1,59 @@
+"""Record parsing and output formatting for the end-to-end searcher fixtures.
+
+Mirrors what ish's parallel runners do with a file before and after matching:
+line records split on '\\n' with '\\r' stripped (ishlib/vendor/kseq.mojo:270-330),
+FASTA records as header + concatenated sequence lines
+(ishlib/vendor/kseq.mojo:370-461), and matched records printed decoded
+(ishlib/parallel_line_search_runner.mojo:113-155,
+ishlib/parallel_fastx_search_runner.mojo:136-177).
+"""
+import json
+import os
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+
+
+def cases():
+    return json.load(open(os.path.join(HERE, "golden", "searcher_cases.json")))["cases"]
+
+
+def line_records(text: str):
+    data = text.encode()
+    parts = data.split(b"\n")
+    if parts and parts[-1] == b"":
+        parts = parts[:-1]
+    return [(None, p.rstrip(b"\r")) for p in parts]
+
+
+def fasta_records(text: str):
+    recs = []
+    header, seq = None, []
+    for raw in text.encode().split(b"\n"):
+        line = raw.rstrip(b"\r")
+        if line.startswith(b">"):
+            if header is not None:
+                recs.append((header, b"".join(seq)))
+            header, seq = line[1:], []
+        elif header is not None:
+            seq.append(line)
+    if header is not None:
+        recs.append((header, b"".join(seq)))
+    return recs
+
+
+def records(case):
+    return line_records(case["in_data"]) if case["record_type"] == "line" else fasta_records(case["in_data"])
+
+
+def render(case, recs, hits, code_to_ascii, encoded):
+    """Output text of the runner: matched records, decoded, in input order."""
+    out = []
+    for (header, _), enc, hit in zip(recs, encoded, hits):
+        if not hit:
+            continue
+        body = bytes(code_to_ascii[enc]) if len(enc) else b""
+        if header is not None:
+            out.append(b">" + header + b"\n" + body + b"\n")
+        else:
+            out.append(body + b"\n")
+    return b"".join(out).decode("utf-8", errors="surrogateescape")
