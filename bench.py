@@ -1,0 +1,343 @@
+"""Benchmark of the GB300 alignment-scoring engine.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+Workload (one step): a 300-residue protein query (blosum62, gap 10/1) against
+1,000,000 synthetic protein records (log-normal lengths, median 350, 0.1%
+planted homologs), scored once with striped-semi-global (ends FFTT) and once
+with striped-local, threshold 0.8 -- the single-query protein configuration of
+ish's benchmarks.  Metric: GCUPS = sum over passes of Q x total record length /
+seconds / 1e9 (ish's own definition, benchmarking/ish_bench_aligner.mojo:740-750).
+
+  value     device time of the scoring + hit-compaction kernels, records
+            resident in HBM (CUDA events on the engine stream); the record
+            stream (~419 MB) is larger than L2, so every pass reads HBM.
+  e2e       the same step through the C ABI from pinned host buffers: upload
+            records, score both passes, copy scores/ends/hits back.
+  roofline  integer cell-update roofline: measured DPX add-max throughput x 2
+            cells per instruction / 5 instructions per cell pair.
+  cpu_baseline / --impl reference: the CPU oracle (a restatement of ish's
+            striped CPU matchers) on all host cores, on a bounded sample.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+INSTR_PER_CELL_PAIR = 5  # max, add-max, sub, add-max (E), add-max (F): wave.cuh
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--records", type=int, default=1_000_000, help="records in the batch (default: full size)")
+    ap.add_argument("--cpu-seconds", type=float, default=12.0, help="target CPU time of the baseline sample")
+    ap.add_argument("--no-plain", action="store_true", help="skip the plain-kernel comparison")
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline")
+    return ap.parse_args()
+
+
+class Clocks:
+    """nvidia-smi samples during the timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index = index
+        self.lines = []
+        self.p = None
+
+    def start(self):
+        try:
+            self.p = subprocess.Popen(["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.Q}",
+                                       "--format=csv,noheader,nounits", "-lms", "200"],
+                                      stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            threading.Thread(target=self._read, daemon=True).start()
+        except Exception:
+            self.p = None
+
+    def _read(self):
+        for line in self.p.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if self.p:
+            self.p.terminate()
+            try:
+                self.p.wait(timeout=5)
+            except Exception:
+                self.p.kill()
+        sm, mx, reasons = [], 0.0, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in self.lines:
+            f = [x.strip() for x in line.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx = max(mx, float(f[2]))
+            except ValueError:
+                continue
+            for name, v in zip(names, f[5:9]):
+                if v.lower() == "active":
+                    reasons.add(name)
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": mx or None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def dist_setup(n_gpus):
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        import torch
+        import torch.distributed as dist
+
+        backend = "nccl" if torch.cuda.is_available() else "gloo"
+        if backend == "nccl":
+            torch.cuda.set_device(local)
+        dist.init_process_group(backend)
+        return rank, world, local, dist
+    return rank, world, local, None
+
+
+def reduce_max(dist, v):
+    if dist is None:
+        return v
+    import torch
+
+    t = torch.tensor([v], dtype=torch.float64, device="cuda" if dist.get_backend() == "nccl" else "cpu")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def barrier(dist):
+    if dist is not None:
+        dist.barrier()
+
+
+def cpu_sample(wl, seconds):
+    """(records, offsets, cells per pass, seconds per step) of a sample sized to ~`seconds`."""
+    import oracle as O
+
+    rng = np.random.default_rng(123)
+    q = wl.queries[0]
+    mx = int(__import__("ish_gb300").ScoringMatrix(wl.kind).values[q, q].sum())
+    threads = os.cpu_count() or 1
+    def timed(idx):
+        sub = wl.subset(idx)
+        t = time.perf_counter()
+        for algo, ends in ((O.SEMI_GLOBAL, O.TS | O.TE), (O.LOCAL, 0)):
+            m = O.Matcher(algo, wl.kind, q, mx, 0.8, gap_open=10, gap_extend=1, ends=ends)
+            m.batch(sub.records, sub.offsets, threads=threads, forward=False, matches=True)
+        return sub, time.perf_counter() - t
+    probe = np.sort(rng.choice(wl.n, min(wl.n, 400), replace=False))
+    sub, dt = timed(probe)
+    k = int(min(wl.n, max(len(probe), len(probe) * seconds / max(dt, 1e-3))))
+    idx = np.sort(rng.choice(wl.n, k, replace=False))
+    return idx, threads
+
+
+def run_reference(args):
+    """CPU oracle (restatement of ish's striped CPU matchers) on all host cores."""
+    import oracle as O
+    from ish_gb300 import workloads
+
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    wl = workloads.protein(n=args.records)
+    idx, threads = cpu_sample(wl, args.cpu_seconds / max(1, args.steps + args.warmup) * 4)
+    sub = wl.subset(idx)
+    q = wl.queries[0]
+    mx = int(__import__("ish_gb300").ScoringMatrix(wl.kind).values[q, q].sum())
+    cells = 2 * len(q) * int(sub.offsets[-1])
+    times = []
+    for s in range(args.warmup + args.steps):
+        t = time.perf_counter()
+        for algo, ends in ((O.SEMI_GLOBAL, O.TS | O.TE), (O.LOCAL, 0)):
+            m = O.Matcher(algo, wl.kind, q, mx, 0.8, gap_open=10, gap_extend=1, ends=ends)
+            m.batch(sub.records, sub.offsets, threads=threads, forward=False, matches=True)
+        if s >= args.warmup:
+            times.append(time.perf_counter() - t)
+    ms = 1e3 * float(np.mean(times))
+    gcups = cells / (ms * 1e-3) / 1e9
+    sample = f"{len(idx)} of {wl.n} records ({int(sub.offsets[-1])} residues), semi-global + local per step"
+    print(json.dumps({
+        "impl": "reference", "metric": "GCUPS", "value": round(gcups, 4), "unit": "GCUPS",
+        "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms, 3),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "int16",
+        "data": "synthetic", "config": workload_config(args.records),
+        "cpu_baseline": {"value": round(gcups, 4), "unit": "GCUPS", "cores": threads, "kind": "port",
+                         "sample": sample},
+        "e2e": {"value": round(gcups, 4), "unit": "GCUPS", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }))
+
+
+def workload_config(n):
+    return {"workload": f"protein single-query search: 300-aa query vs {n} records, blosum62, gap 10/1, "
+                        "striped-semi-global FFTT + striped-local per step, threshold 0.8",
+            "query_len": 300, "records": n, "record_lengths": "lognormal(median 350, sigma 0.6) clipped 30-5000",
+            "l2": "record stream larger than L2 (129 MB): every pass reads HBM", "parallelism": "records"}
+
+
+def run_ours(args):
+    rank, world, local, dist = dist_setup(args.gpus)
+    from ish_gb300 import native, workloads
+    from ish_gb300.scoring import ScoringMatrix
+
+    native.load(build_if_missing=True)
+    wl = workloads.protein(seed=1 + rank, n=args.records)
+    q = wl.queries[0]
+    m = ScoringMatrix(wl.kind)
+    mx = int(m.values[q, q].sum())
+    cells_per_pass = len(q) * int(wl.offsets[-1])
+    cells = 2 * cells_per_pass
+    ctx = native.Context(local)
+    q_sg = ctx.set_query(q, wl.kind, m.values, native.ALGO_SEMI_GLOBAL, 10, 1,
+                         native.FREE_TARGET_START | native.FREE_TARGET_END, mx, 0.8)
+    q_sw = ctx.set_query(q, wl.kind, m.values, native.ALGO_LOCAL, 10, 1, 0, mx, 0.8)
+    sid = ctx.records_load(wl.records, wl.offsets)
+
+    def step():
+        r1 = ctx.score_set(q_sg, sid, want=("score", "qend", "tend", "hit_idx"))
+        t1 = ctx.last_kernel_ms()
+        r2 = ctx.score_set(q_sw, sid, want=("score", "qend", "tend", "hit_idx"))
+        t2 = ctx.last_kernel_ms()
+        return t1 + t2, (r1, r2)
+
+    for _ in range(args.warmup):
+        step()
+    clocks = Clocks(local)
+    clocks.start()
+    barrier(dist)
+    dev_ms = []
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        ms, res = step()
+        dev_ms.append(ms)
+    wall_ms = 1e3 * (time.perf_counter() - t0) / args.steps
+    barrier(dist)
+    clk = clocks.stop()
+    step_ms = reduce_max(dist, float(np.mean(dev_ms)))
+    value = world * cells / (step_ms * 1e-3) / 1e9
+    hits = (len(res[0]["hit_idx"]), len(res[1]["hit_idx"]))
+
+    # ---- end to end through the C ABI from pinned host memory ----
+    try:
+        import torch
+
+        pin = torch.empty(len(wl.records), dtype=torch.uint8, pin_memory=True).numpy()
+        pin_off = torch.empty(len(wl.offsets), dtype=torch.int64, pin_memory=True).numpy().view(np.uint64)
+    except Exception:
+        pin = np.empty(len(wl.records), np.uint8)
+        pin_off = np.empty(len(wl.offsets), np.uint64)
+    pin[:] = wl.records
+    pin_off[:] = wl.offsets
+    e2e_ms = []
+    for s in range(args.warmup + args.steps):
+        barrier(dist)
+        t = time.perf_counter()
+        sid2 = ctx.records_load(pin, pin_off)
+        ctx.score_set(q_sg, sid2, want=("score", "qend", "tend", "hit_idx"))
+        ctx.score_set(q_sw, sid2, want=("score", "qend", "tend", "hit_idx"))
+        ctx.records_free(sid2)
+        if s >= args.warmup:
+            e2e_ms.append(1e3 * (time.perf_counter() - t))
+    e2e_step = reduce_max(dist, float(np.mean(e2e_ms)))
+    e2e_value = world * cells / (e2e_step * 1e-3) / 1e9
+    n = wl.n
+    h2d = int(len(wl.records) + 8 * len(wl.offsets))
+    d2h = int(2 * (12 * n + 4 * 8 + 4 * sum(hits)))
+
+    # ---- plain one-thread-per-record kernel (the in-GPU comparison) ----
+    plain = None
+    if not args.no_plain:
+        ctx.set_option(native.OPT_KERNEL, native.KERNEL_PLAIN)
+        step()
+        pm = [step()[0] for _ in range(2)]
+        ctx.set_option(native.OPT_KERNEL, native.KERNEL_AUTO)
+        plain = cells / (float(np.mean(pm)) * 1e-3) / 1e9
+
+    # ---- integer roofline ----
+    dpx = ctx.calibrate()
+    peak_gcups = dpx * 2 / INSTR_PER_CELL_PAIR / 1e9
+    per_gpu = cells / (step_ms * 1e-3) / 1e9
+    traffic = None
+    prof = os.path.join(ROOT, "profiles", "wave_protein_traffic.json")
+    if os.path.exists(prof):
+        try:
+            traffic = json.load(open(prof)).get("dram_bytes_per_launch")
+        except Exception:
+            traffic = None
+
+    cpu = None
+    if rank == 0 and not args.no_cpu:
+        import oracle as O
+
+        idx, threads = cpu_sample(wl, args.cpu_seconds)
+        sub = wl.subset(idx)
+        t = time.perf_counter()
+        for algo, ends in ((O.SEMI_GLOBAL, O.TS | O.TE), (O.LOCAL, 0)):
+            om = O.Matcher(algo, wl.kind, q, mx, 0.8, gap_open=10, gap_extend=1, ends=ends)
+            om.batch(sub.records, sub.offsets, threads=threads, forward=False, matches=True)
+        dt = time.perf_counter() - t
+        cpu = {"value": round(2 * len(q) * int(sub.offsets[-1]) / dt / 1e9, 4), "unit": "GCUPS", "cores": threads,
+               "kind": "port",
+               "sample": f"{len(idx)} of {n} records, semi-global + local, {dt:.1f} s on {threads} threads"}
+
+    if rank == 0:
+        lat = np.array(e2e_ms)
+        out = {
+            "metric": "GCUPS", "value": round(value, 2), "unit": "GCUPS", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(step_ms, 3),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "s16x2",
+            "data": "synthetic", "config": workload_config(n),
+            "roofline": {"bound": "int", "achieved": round(per_gpu, 2), "peak": round(peak_gcups, 2),
+                         "unit": "GCUPS", "frac": round(per_gpu / peak_gcups, 4), "traffic": traffic,
+                         "peak_source": f"measured now: {dpx / 1e12:.2f} T DPX add-max instr/s x 2 cells / "
+                                        f"{INSTR_PER_CELL_PAIR} instr per cell pair",
+                         "hbm": {"achieved_gbs": round(2 * int(wl.offsets[-1]) / (step_ms * 1e-3) / 1e9, 2),
+                                 "peak_gbs": 6790.0, "peak_source": "MEASURED_PEAKS.json hbm_gbs"}},
+            "cpu_baseline": cpu,
+            "e2e": {"value": round(e2e_value, 2), "unit": "GCUPS", "h2d_bytes_per_step": h2d,
+                    "d2h_bytes_per_step": d2h,
+                    "latency_ms": {"p50": round(float(np.percentile(lat, 50)), 3),
+                                   "p99": round(float(np.percentile(lat, 99)), 3)}},
+            "gpu_launches": 8 * args.steps,
+            "clocks": clk,
+            "plain_kernel_gcups": round(plain, 2) if plain else None,
+            "wall_ms_per_step": round(wall_ms, 3),
+            "hits": {"semi_global": hits[0], "local": hits[1]},
+        }
+        print(json.dumps(out))
+    ctx.close()
+    if dist is not None:
+        dist.destroy_process_group()
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,799 @@
+// ish_gpu.cu -- host side of libish_gpu.so: the C ABI declared in
+// include/ish_gpu.h.  It owns device memory, pinned staging and the engine
+// stream, packs record sets in HBM, builds query profiles and picks and
+// launches the scoring kernels.
+#include <algorithm>
+#include <cerrno>
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <map>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "../../include/ish_gpu.h"
+#include "kernels.cuh"
+
+using namespace ish;
+
+namespace {
+
+thread_local std::string g_open_error;
+
+struct DevBuf {
+  void *p = nullptr;
+  size_t cap = 0;
+  cudaError_t ensure(size_t bytes) {
+    if (bytes <= cap && p) return cudaSuccess;
+    if (p) cudaFree(p);
+    p = nullptr;
+    cap = 0;
+    size_t want = bytes < 256 ? 256 : bytes;
+    cudaError_t e = cudaMalloc(&p, want);
+    if (e == cudaSuccess) cap = want;
+    return e;
+  }
+  void release() {
+    if (p) cudaFree(p);
+    p = nullptr;
+    cap = 0;
+  }
+  template <class T>
+  T *as() const { return reinterpret_cast<T *>(p); }
+};
+
+struct WaveLayout {
+  int G = 0, K = 0, d = 0, kp = 0, pair = 0;
+  uint32_t prof_bytes = 0;
+  DevBuf prof, hinit;
+};
+
+struct Query {
+  int algo = 0, kind = 0, alphabet = 0, Q = 0, open = 0, ext = 0, ends = 0;
+  int32_t max_score = 0;
+  float thr = 0.f;
+  std::vector<int8_t> M;
+  std::vector<uint8_t> q;
+  int mmin = 0, mmax = 0;
+  int neg_limit = 0;
+  DevBuf plain_prof, plain_hinit;
+  bool plain_ready = false;
+  std::map<long, WaveLayout> layouts;
+};
+
+struct RecordSet {
+  uint32_t n = 0;
+  uint64_t total = 0;
+  uint32_t max_len = 0;
+  DevBuf codes, off_s, len_s, orig_s;
+  std::vector<uint32_t> hist;  // length-bucket histogram (host copy)
+  uint32_t n_empty = 0;
+};
+
+}  // namespace
+
+struct ish_ctx {
+  int device = 0;
+  int num_sms = 0;
+  cudaStream_t stream = nullptr;
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+  std::string err;
+  int kernel = ISH_KERNEL_AUTO;
+  int sg_lanes = 8, sw_u8_lanes = 16, sw_u16_lanes = 8;
+  int force_G = 0, force_K = 0;
+  std::map<int32_t, Query> queries;
+  int32_t next_query = 1;
+  std::map<int32_t, RecordSet> sets;
+  int32_t next_set = 1;
+  // scratch
+  DevBuf raw, off_in, len_tmp, slot_tmp, poff_tmp, hist, scan_tmp;
+  DevBuf counter, error, out_score, out_qend, out_tend, out_hit, hit_idx, block_counts, nhits;
+  DevBuf plain_scratch;
+  float last_ms = 0.f;
+};
+
+namespace {
+
+int fail(ish_ctx *c, int code, const char *fmt, ...) {
+  char buf[512];
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(buf, sizeof buf, fmt, ap);
+  va_end(ap);
+  if (c) c->err = buf;
+  else g_open_error = buf;
+  return code;
+}
+
+#define CU(call)                                                                                   \
+  do {                                                                                             \
+    cudaError_t _e = (call);                                                                       \
+    if (_e != cudaSuccess)                                                                         \
+      return fail(ctx, _e == cudaErrorMemoryAllocation ? ISH_ENOMEM : ISH_EDEVICE, "%s: %s (%s:%d)", \
+                  #call, cudaGetErrorString(_e), __FILE__, __LINE__);                              \
+  } while (0)
+
+inline uint32_t ceil_div(uint64_t a, uint64_t b) { return (uint32_t)((a + b - 1) / b); }
+
+int matrix_alphabet_ok(uint32_t alphabet) { return alphabet >= 1 && alphabet <= 256; }
+
+// Safe-regime checks (see engine.cuh): the fast kernels evaluate plain Gotoh
+// in 16-bit lanes; the result equals the reference's striped int16 pass when
+// gap_open > gap_extend and no lane value of the reference can saturate or
+// wrap.  Bounds are conservative.
+struct Regime {
+  bool fast = false;
+  uint64_t max_safe_len = 0;  // records longer than this need the exact path
+};
+
+Regime regime(const Query &q, int qpad) {
+  Regime r;
+  if (q.Q == 0) return r;
+  if (!(q.open > q.ext) || q.ext < 0) return r;
+  const long top = (long)(q.Q + 1) * std::max(q.mmax, 1);
+  if (top > 30000) return r;
+  if (q.algo == ISH_ALGO_LOCAL) {
+    r.fast = true;
+    r.max_safe_len = ~0ull;
+    return r;
+  }
+  if (q.open + q.ext > 10000) return r;
+  const long base = 2L * q.open + (long)q.ext * (qpad + 2) + std::abs(q.mmin) + 64;
+  if (base > 30000) return r;
+  r.fast = true;
+  if (q.ends & ISH_FREE_TARGET_START) {
+    r.max_safe_len = ~0ull;
+  } else {
+    const long room = 30000 - base - q.open;
+    r.max_safe_len = q.ext > 0 ? (uint64_t)(room / q.ext) : ~0ull;
+  }
+  return r;
+}
+
+int neg_limit_of(int open, int mmin) {
+  // v_neg_limit (ishlib/matcher/alignment/semi_global_aln/striped.mojo:329-334)
+  const int16_t o = (int16_t)open;
+  if ((int16_t)(-o) < (int16_t)mmin) return (int16_t)(-32768 + o + 1);
+  return (int16_t)(-32768 - mmin + 1);
+}
+
+// Columns per thread (K) and threads per group (G) for a query length: the
+// smallest modelled cost G*K*(1 + 12/K) with G*K >= Q + 1, K even, K <= 48.
+void choose_shape(int Q, int force_G, int force_K, int *G, int *K) {
+  double bestc = 1e30;
+  int bg = 32, bk = WAVE_KMAX;
+  for (int g = 1; g <= 32; g <<= 1) {
+    if (force_G && g != force_G) continue;
+    int k = (Q + 1 + g - 1) / g;
+    k = (k + 1) & ~1;
+    if (k < 2) k = 2;
+    if (force_K) {
+      if (g * force_K < Q + 1) continue;
+      k = force_K;
+    }
+    if (k > (force_K ? WAVE_KMAX : 48)) continue;
+    const double c = (double)g * k * (1.0 + 12.0 / k);
+    if (c < bestc) {
+      bestc = c;
+      bg = g;
+      bk = k;
+    }
+  }
+  if (bestc > 1e29) {  // nothing under 48 columns: use the widest shape
+    bg = force_G ? force_G : 32;
+    bk = ((Q + 1 + bg - 1) / bg + 1) & ~1;
+  }
+  *G = bg;
+  *K = bk;
+}
+
+int build_wave_layout(ish_ctx *ctx, Query &q, int G, int K, WaveLayout **out) {
+  const int pair_ok = q.alphabet * q.alphabet * G * ((K + 3) & ~3) * 4 <= 64 * 1024;
+  const long key = ((long)G << 20) | ((long)K << 8) | pair_ok;
+  auto it = q.layouts.find(key);
+  if (it != q.layouts.end()) {
+    *out = &it->second;
+    return ISH_OK;
+  }
+  WaveLayout L;
+  L.G = G;
+  L.K = K;
+  L.d = G * K - q.Q;
+  L.pair = pair_ok;
+  const int A = q.alphabet;
+  const bool sg = q.algo == ISH_ALGO_SEMI_GLOBAL;
+  const int ppad = (sg && !(q.ends & ISH_FREE_TARGET_START)) ? -(q.open + q.ext) : 0;
+  auto P = [&](int c, int col) -> int {
+    if (col < 0) return ppad;
+    return q.M[(size_t)c * A + q.q[col]];
+  };
+  std::vector<uint8_t> host;
+  if (L.pair) {
+    L.kp = (K + 3) & ~3;
+    std::vector<uint32_t> w((size_t)A * A * G * L.kp, 0u);
+    for (int a = 0; a < A; ++a)
+      for (int b = 0; b < A; ++b)
+        for (int t = 0; t < G; ++t)
+          for (int j = 0; j < K; ++j) {
+            const int col = t * K + j - L.d;
+            w[((size_t)(a * A + b) * G + t) * L.kp + j] =
+                ((uint32_t)P(a, col) & 0xffffu) | ((uint32_t)(P(b, col) & 0xffff) << 16);
+          }
+    host.resize(w.size() * 4);
+    memcpy(host.data(), w.data(), host.size());
+  } else {
+    L.kp = (K + 7) & ~7;
+    std::vector<int16_t> w((size_t)A * G * L.kp, 0);
+    for (int a = 0; a < A; ++a)
+      for (int t = 0; t < G; ++t)
+        for (int j = 0; j < K; ++j) w[((size_t)a * G + t) * L.kp + j] = (int16_t)P(a, t * K + j - L.d);
+    host.resize(w.size() * 2);
+    memcpy(host.data(), w.data(), host.size());
+  }
+  L.prof_bytes = (uint32_t)((host.size() + 15) & ~(size_t)15);
+  host.resize(L.prof_bytes, 0);
+  std::vector<int16_t> hin((size_t)G * K, 0);
+  for (int c = 0; c < G * K; ++c) {
+    const int col = c - L.d;
+    int v = 0;
+    if (sg && col >= 0 && !(q.ends & ISH_FREE_QUERY_START)) v = -q.open - q.ext * col;
+    hin[c] = (int16_t)v;
+  }
+  CU(L.prof.ensure(L.prof_bytes));
+  CU(L.hinit.ensure(hin.size() * 2));
+  CU(cudaMemcpy(L.prof.p, host.data(), L.prof_bytes, cudaMemcpyHostToDevice));
+  CU(cudaMemcpy(L.hinit.p, hin.data(), hin.size() * 2, cudaMemcpyHostToDevice));
+  auto res = q.layouts.emplace(key, std::move(L));
+  *out = &res.first->second;
+  return ISH_OK;
+}
+
+int build_plain(ish_ctx *ctx, Query &q) {
+  if (q.plain_ready) return ISH_OK;
+  const int A = q.alphabet;
+  std::vector<int16_t> prof((size_t)A * q.Q + 8, 0);
+  for (int c = 0; c < A; ++c)
+    for (int col = 0; col < q.Q; ++col) prof[(size_t)c * q.Q + col] = q.M[(size_t)c * A + q.q[col]];
+  std::vector<int16_t> hin(q.Q + 1, 0);
+  if (q.algo == ISH_ALGO_SEMI_GLOBAL && !(q.ends & ISH_FREE_QUERY_START))
+    for (int col = 0; col < q.Q; ++col) hin[col] = (int16_t)(-q.open - q.ext * col);
+  CU(q.plain_prof.ensure(prof.size() * 2));
+  CU(q.plain_hinit.ensure(hin.size() * 2));
+  CU(cudaMemcpy(q.plain_prof.p, prof.data(), prof.size() * 2, cudaMemcpyHostToDevice));
+  CU(cudaMemcpy(q.plain_hinit.p, hin.data(), hin.size() * 2, cudaMemcpyHostToDevice));
+  q.plain_ready = true;
+  return ISH_OK;
+}
+
+// Upload and pack a record set (see k_lengths .. k_pack in kernels.cu).
+int load_records(ish_ctx *ctx, const uint8_t *records, const uint64_t *offsets, uint32_t n, RecordSet &rs) {
+  if (n == 0) {
+    rs.n = 0;
+    rs.total = 0;
+    return ISH_OK;
+  }
+  if (!offsets) return fail(ctx, ISH_EINVAL, "offsets is NULL");
+  const uint64_t base = offsets[0], end = offsets[n];
+  if (end < base) return fail(ctx, ISH_EINVAL, "offsets are not monotone");
+  const uint64_t bytes = end - base;
+  if (bytes && !records) return fail(ctx, ISH_EINVAL, "records is NULL");
+  rs.n = n;
+  rs.total = bytes;
+  cudaStream_t s = ctx->stream;
+  // raw bytes (+16 slack for the realigning pack loads)
+  CU(ctx->raw.ensure(bytes + 32));
+  if (bytes) CU(cudaMemcpyAsync(ctx->raw.p, records + base, bytes, cudaMemcpyHostToDevice, s));
+  CU(ctx->off_in.ensure((size_t)(n + 1) * 8));
+  if (base == 0) {
+    CU(cudaMemcpyAsync(ctx->off_in.p, offsets, (size_t)(n + 1) * 8, cudaMemcpyHostToDevice, s));
+  } else {
+    std::vector<uint64_t> rebased(offsets, offsets + n + 1);
+    for (auto &v : rebased) v -= base;
+    CU(cudaMemcpyAsync(ctx->off_in.p, rebased.data(), (size_t)(n + 1) * 8, cudaMemcpyHostToDevice, s));
+    CU(cudaStreamSynchronize(s));
+  }
+  CU(ctx->len_tmp.ensure((size_t)n * 4));
+  CU(ctx->slot_tmp.ensure((size_t)n * 8));
+  CU(ctx->poff_tmp.ensure((size_t)n * 8));
+  CU(ctx->hist.ensure((size_t)NBUCKETS * 4 * 2));
+  CU(cudaMemsetAsync(ctx->hist.p, 0, (size_t)NBUCKETS * 4, s));
+  const uint32_t nb = std::min<uint32_t>(ceil_div(n, 256), (uint32_t)ctx->num_sms * 16);
+  k_lengths<<<nb, 256, 0, s>>>(ctx->off_in.as<uint64_t>(), n, ctx->len_tmp.as<uint32_t>(), ctx->slot_tmp.as<uint64_t>(),
+                                ctx->hist.as<uint32_t>());
+  // exclusive scan of slot sizes -> packed offsets
+  const uint32_t tiles = ceil_div(n, SCAN_TILE);
+  CU(ctx->scan_tmp.ensure((size_t)(tiles + 1) * 8 * 2));
+  uint64_t *bsum = ctx->scan_tmp.as<uint64_t>();
+  uint64_t *boff = bsum + tiles + 1;
+  k_scan64_block<<<tiles, 1024, 0, s>>>(ctx->slot_tmp.as<uint64_t>(), ctx->poff_tmp.as<uint64_t>(), n, bsum);
+  if (tiles > 1) {
+    if (tiles > SCAN_TILE) return fail(ctx, ISH_EINVAL, "too many records in one set (%u)", n);
+    k_scan64_block<<<1, 1024, 0, s>>>(bsum, boff, tiles, nullptr);
+    k_scan64_add<<<tiles, 1024, 0, s>>>(ctx->poff_tmp.as<uint64_t>(), n, boff);
+  }
+  // host copy of the histogram, then turn it into descending bucket cursors
+  rs.hist.assign(NBUCKETS, 0);
+  CU(cudaMemcpyAsync(rs.hist.data(), ctx->hist.p, (size_t)NBUCKETS * 4, cudaMemcpyDeviceToHost, s));
+  k_bucket_scan<<<1, 1024, 0, s>>>(ctx->hist.as<uint32_t>());
+  CU(rs.len_s.ensure((size_t)n * 4));
+  CU(rs.off_s.ensure((size_t)n * 8));
+  CU(rs.orig_s.ensure((size_t)n * 4));
+  k_scatter<<<nb, 256, 0, s>>>(ctx->len_tmp.as<uint32_t>(), ctx->poff_tmp.as<uint64_t>(), n, ctx->hist.as<uint32_t>(),
+                               rs.len_s.as<uint32_t>(), rs.off_s.as<uint64_t>(), rs.orig_s.as<uint32_t>());
+  const uint64_t packed = bytes + 16ull * n + 16;
+  CU(rs.codes.ensure(packed));
+  const uint32_t pb = std::min<uint32_t>(ceil_div((uint64_t)n * 32, 256), (uint32_t)ctx->num_sms * 32);
+  k_pack<<<pb, 256, 0, s>>>(ctx->raw.as<uint8_t>(), bytes, ctx->off_in.as<uint64_t>(), ctx->poff_tmp.as<uint64_t>(), n,
+                            rs.codes.as<uint8_t>());
+  CU(cudaGetLastError());
+  CU(cudaStreamSynchronize(s));
+  rs.n_empty = rs.hist[0];
+  rs.max_len = 0;
+  for (int b = NBUCKETS - 1; b >= 0; --b)
+    if (rs.hist[b]) {
+      rs.max_len = b < 32768 ? (uint32_t)b : (uint32_t)(32768 + ((uint64_t)(b - 32768) << 5) + 31);
+      break;
+    }
+  return ISH_OK;
+}
+
+// Number of records (a prefix of the descending order) whose length bucket
+// may exceed `len`.
+uint32_t count_longer(const RecordSet &rs, uint64_t len) {
+  uint64_t cnt = 0;
+  for (uint32_t b = NBUCKETS - 1; b > 0; --b) {
+    const uint64_t lo = b < 32768 ? b : 32768 + ((uint64_t)(b - 32768) << 5);
+    const uint64_t hi = b < 32768 ? b : lo + 31;
+    if (hi <= len) break;
+    (void)lo;
+    cnt += rs.hist[b];
+  }
+  return (uint32_t)cnt;
+}
+
+int ensure_outputs(ish_ctx *ctx, uint32_t n) {
+  CU(ctx->out_score.ensure((size_t)n * 4 + 4));
+  CU(ctx->out_qend.ensure((size_t)n * 4 + 4));
+  CU(ctx->out_tend.ensure((size_t)n * 4 + 4));
+  CU(ctx->out_hit.ensure((size_t)n + 16));
+  CU(ctx->counter.ensure(64));
+  CU(ctx->error.ensure(64));
+  return ISH_OK;
+}
+
+int launch_wave(ish_ctx *ctx, Query &q, RecordSet &rs, uint32_t first, uint32_t count, OutDev out) {
+  if (count == 0) return ISH_OK;
+  int G, K;
+  choose_shape(q.Q, ctx->force_G, ctx->force_K, &G, &K);
+  if (G * K < q.Q + 1) return fail(ctx, ISH_EOVERFLOW, "query of %d residues exceeds the wavefront engine", q.Q);
+  WaveLayout *L = nullptr;
+  int rc = build_wave_layout(ctx, q, G, K, &L);
+  if (rc) return rc;
+  const int mode = q.algo == ISH_ALGO_LOCAL ? SW : SG;
+  WaveFn fn = wave_fn(K, mode, L->pair);
+  if (!fn) return fail(ctx, ISH_EOVERFLOW, "no wavefront kernel for K=%d", K);
+  const int groups = WAVE_THREADS / G;
+  const size_t smem = ((L->prof_bytes + 15) & ~15u) + (size_t)groups * 32 * 4;
+  CU(cudaFuncSetAttribute((const void *)fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  int per_sm = 0;
+  CU(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, (const void *)fn, WAVE_THREADS, smem));
+  if (per_sm < 1) return fail(ctx, ISH_EOVERFLOW, "wavefront kernel K=%d does not fit (smem %zu)", K, smem);
+  const uint32_t pairs = (count + 1) / 2;
+  const uint32_t want = ceil_div(pairs, groups);
+  const uint32_t grid = std::max<uint32_t>(1, std::min<uint32_t>(want, (uint32_t)(per_sm * ctx->num_sms)));
+  WaveParams p{};
+  p.prof = L->prof.as<const uint4>();
+  p.prof_bytes = L->prof_bytes;
+  p.Q = q.Q;
+  p.G = G;
+  p.K = K;
+  p.d = L->d;
+  p.kp = L->kp;
+  p.alphabet = q.alphabet;
+  p.pair_prof = L->pair;
+  p.open = q.open;
+  p.ext = q.ext;
+  p.ends = q.ends;
+  p.neg_limit = q.neg_limit;
+  const bool sg = mode == SG;
+  p.hleft = (sg && !(q.ends & ISH_FREE_TARGET_START)) ? NEG_BIG : 0;
+  p.fin = sg ? NEG_BIG : 0;
+  p.hinit = L->hinit.as<const int16_t>();
+  p.first = first;
+  p.count = count;
+  p.counter = ctx->counter.as<uint32_t>();
+  p.max_steps = rs.total + 2ull * count + 1024;
+  p.error = ctx->error.as<int>();
+  p.rec = RecordsDev{rs.codes.as<const uint8_t>(), rs.off_s.as<const uint64_t>(), rs.len_s.as<const uint32_t>(),
+                     rs.orig_s.as<const uint32_t>(), rs.n};
+  p.out = out;
+  p.dec = Decision{q.max_score, q.thr};
+  CU(cudaMemsetAsync(ctx->counter.p, 0, 4, ctx->stream));
+  fn<<<grid, WAVE_THREADS, smem, ctx->stream>>>(p);
+  CU(cudaGetLastError());
+  return ISH_OK;
+}
+
+int launch_plain(ish_ctx *ctx, Query &q, RecordSet &rs, uint32_t first, uint32_t count, OutDev out) {
+  if (count == 0) return ISH_OK;
+  int rc = build_plain(ctx, q);
+  if (rc) return rc;
+  const int threads = 128;
+  const uint32_t blocks = std::max<uint32_t>(1, std::min<uint32_t>(ceil_div(count, threads), (uint32_t)ctx->num_sms * 4));
+  const uint32_t nth = blocks * threads;
+  CU(ctx->plain_scratch.ensure((size_t)2 * q.Q * nth * 4 + 16));
+  PlainParams p{};
+  p.prof = q.plain_prof.as<const int16_t>();
+  p.prof_bytes = (uint32_t)(((size_t)q.alphabet * q.Q * 2 + 15) & ~(size_t)15);
+  p.use_smem = p.prof_bytes <= 96 * 1024;
+  p.Q = q.Q;
+  p.alphabet = q.alphabet;
+  p.open = q.open;
+  p.ext = q.ext;
+  p.ends = q.ends;
+  p.neg_limit = q.neg_limit;
+  p.hinit = q.plain_hinit.as<const int16_t>();
+  p.scratch = ctx->plain_scratch.as<int32_t>();
+  p.nthreads = nth;
+  p.first = first;
+  p.count = count;
+  p.error = ctx->error.as<int>();
+  p.rec = RecordsDev{rs.codes.as<const uint8_t>(), rs.off_s.as<const uint64_t>(), rs.len_s.as<const uint32_t>(),
+                     rs.orig_s.as<const uint32_t>(), rs.n};
+  p.out = out;
+  p.dec = Decision{q.max_score, q.thr};
+  const size_t smem = p.use_smem ? p.prof_bytes : 0;
+  PlainFn fn = plain_fn(q.algo == ISH_ALGO_LOCAL ? SW : SG);
+  CU(cudaFuncSetAttribute((const void *)fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)std::max<size_t>(smem, 1)));
+  fn<<<blocks, threads, smem, ctx->stream>>>(p);
+  CU(cudaGetLastError());
+  return ISH_OK;
+}
+
+// Score query q against set rs into the context's device output buffers.
+int run_scoring(ish_ctx *ctx, Query &q, RecordSet &rs) {
+  const uint32_t n = rs.n;
+  int rc = ensure_outputs(ctx, n);
+  if (rc) return rc;
+  cudaStream_t s = ctx->stream;
+  CU(cudaMemsetAsync(ctx->error.p, 0, 4, s));
+  OutDev out{ctx->out_score.as<int32_t>(), ctx->out_qend.as<int32_t>(), ctx->out_tend.as<int32_t>(),
+             ctx->out_hit.as<uint8_t>()};
+  const int mode = q.algo == ISH_ALGO_LOCAL ? SW : SG;
+  const uint32_t n_empty = (q.Q == 0) ? n : rs.n_empty;
+  const uint32_t nonempty = n - n_empty;
+  CU(cudaEventRecord(ctx->ev0, s));
+  if (n_empty) {
+    k_trivial<<<std::max<uint32_t>(1, std::min<uint32_t>(ceil_div(n_empty, 256), 1024)), 256, 0, s>>>(
+        RecordsDev{rs.codes.as<const uint8_t>(), rs.off_s.as<const uint64_t>(), rs.len_s.as<const uint32_t>(),
+                   rs.orig_s.as<const uint32_t>(), rs.n},
+        nonempty, n_empty, mode, q.Q, out, Decision{q.max_score, q.thr});
+    CU(cudaGetLastError());
+  }
+  if (nonempty) {
+    int G, K;
+    choose_shape(q.Q, ctx->force_G, ctx->force_K, &G, &K);
+    Regime r = regime(q, G * K);
+    if (!r.fast)
+      return fail(ctx, ISH_EINVAL,
+                  "parameters outside the exact-integer fast regime (gap_open must exceed gap_extend and scores "
+                  "must stay within int16)");
+    const uint32_t n_long = r.max_safe_len == ~0ull ? 0 : std::min(count_longer(rs, r.max_safe_len), nonempty);
+    if (n_long)
+      return fail(ctx, ISH_EINVAL, "%u records are longer than %llu residues with a non-free target start", n_long,
+                  (unsigned long long)r.max_safe_len);
+    if (ctx->kernel == ISH_KERNEL_PLAIN)
+      rc = launch_plain(ctx, q, rs, 0, nonempty, out);
+    else
+      rc = launch_wave(ctx, q, rs, 0, nonempty, out);
+    if (rc) return rc;
+  }
+  return ISH_OK;
+}
+
+int fetch_outputs(ish_ctx *ctx, uint32_t n, int32_t *score, int32_t *qend, int32_t *tend, uint8_t *hit,
+                  uint32_t *hit_idx, uint32_t *n_hits) {
+  cudaStream_t s = ctx->stream;
+  const bool compact = (hit_idx || n_hits) && n;
+  if (compact) {
+    const uint32_t nb = ceil_div(n, HIT_TILE);
+    CU(ctx->block_counts.ensure((size_t)nb * 4 + 8));
+    CU(ctx->hit_idx.ensure((size_t)n * 4 + 4));
+    CU(ctx->nhits.ensure(16));
+    k_count_hits<<<nb, 1024, 0, s>>>(ctx->out_hit.as<uint8_t>(), n, ctx->block_counts.as<uint32_t>());
+    k_scan_counts<<<1, 1024, 0, s>>>(ctx->block_counts.as<uint32_t>(), nb, ctx->nhits.as<uint32_t>());
+    k_write_hits<<<nb, 1024, 0, s>>>(ctx->out_hit.as<uint8_t>(), n, ctx->block_counts.as<uint32_t>(),
+                                     ctx->hit_idx.as<uint32_t>());
+    CU(cudaGetLastError());
+  }
+  CU(cudaEventRecord(ctx->ev1, s));
+  if (n && score) CU(cudaMemcpyAsync(score, ctx->out_score.p, (size_t)n * 4, cudaMemcpyDeviceToHost, s));
+  if (n && qend) CU(cudaMemcpyAsync(qend, ctx->out_qend.p, (size_t)n * 4, cudaMemcpyDeviceToHost, s));
+  if (n && tend) CU(cudaMemcpyAsync(tend, ctx->out_tend.p, (size_t)n * 4, cudaMemcpyDeviceToHost, s));
+  if (n && hit) CU(cudaMemcpyAsync(hit, ctx->out_hit.p, (size_t)n, cudaMemcpyDeviceToHost, s));
+  int herr = 0;
+  uint32_t total = 0;
+  CU(cudaMemcpyAsync(&herr, ctx->error.p, 4, cudaMemcpyDeviceToHost, s));
+  if (compact) CU(cudaMemcpyAsync(&total, ctx->nhits.p, 4, cudaMemcpyDeviceToHost, s));
+  CU(cudaStreamSynchronize(s));
+  if (hit_idx && total) {
+    CU(cudaMemcpyAsync(hit_idx, ctx->hit_idx.p, (size_t)total * 4, cudaMemcpyDeviceToHost, s));
+    CU(cudaStreamSynchronize(s));
+  }
+  if (n_hits) *n_hits = total;
+  float ms = 0.f;
+  if (cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1) == cudaSuccess) ctx->last_ms = ms;
+  if (herr & 2) return fail(ctx, ISH_ETIMEDOUT, "wavefront kernel exceeded its step budget (internal error)");
+  if (herr) return fail(ctx, ISH_EINVAL, "a record contains a code >= the alphabet size of the query");
+  return ISH_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int ish_gpu_abi_version(void) { return ISH_GPU_ABI_VERSION; }
+
+int ish_gpu_open(int device, ish_ctx **out) {
+  if (!out) return fail(nullptr, ISH_EINVAL, "out is NULL");
+  *out = nullptr;
+  int ndev = 0;
+  cudaError_t e = cudaGetDeviceCount(&ndev);
+  if (e != cudaSuccess || ndev == 0)
+    return fail(nullptr, ISH_ENODEV, "no CUDA device: %s", e == cudaSuccess ? "count is 0" : cudaGetErrorString(e));
+  if (device < 0 || device >= ndev) return fail(nullptr, ISH_EINVAL, "device %d out of range (%d devices)", device, ndev);
+  ish_ctx *ctx = new ish_ctx();
+  ctx->device = device;
+  auto bail = [&](cudaError_t err, const char *what) {
+    g_open_error = std::string(what) + ": " + cudaGetErrorString(err);
+    delete ctx;
+    return ISH_EDEVICE;
+  };
+  if ((e = cudaSetDevice(device)) != cudaSuccess) return bail(e, "cudaSetDevice");
+  if ((e = cudaDeviceGetAttribute(&ctx->num_sms, cudaDevAttrMultiProcessorCount, device)) != cudaSuccess)
+    return bail(e, "cudaDeviceGetAttribute");
+  if ((e = cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking)) != cudaSuccess)
+    return bail(e, "cudaStreamCreate");
+  if ((e = cudaEventCreate(&ctx->ev0)) != cudaSuccess) return bail(e, "cudaEventCreate");
+  if ((e = cudaEventCreate(&ctx->ev1)) != cudaSuccess) return bail(e, "cudaEventCreate");
+  *out = ctx;
+  return ISH_OK;
+}
+
+void ish_gpu_close(ish_ctx *ctx) {
+  if (!ctx) return;
+  cudaSetDevice(ctx->device);
+  cudaStreamSynchronize(ctx->stream);
+  for (auto &kv : ctx->queries) {
+    kv.second.plain_prof.release();
+    kv.second.plain_hinit.release();
+    for (auto &l : kv.second.layouts) {
+      l.second.prof.release();
+      l.second.hinit.release();
+    }
+  }
+  for (auto &kv : ctx->sets) {
+    kv.second.codes.release();
+    kv.second.off_s.release();
+    kv.second.len_s.release();
+    kv.second.orig_s.release();
+  }
+  DevBuf *bufs[] = {&ctx->raw, &ctx->off_in, &ctx->len_tmp, &ctx->slot_tmp, &ctx->poff_tmp, &ctx->hist,
+                    &ctx->scan_tmp, &ctx->counter, &ctx->error, &ctx->out_score, &ctx->out_qend, &ctx->out_tend,
+                    &ctx->out_hit, &ctx->hit_idx, &ctx->block_counts, &ctx->nhits, &ctx->plain_scratch};
+  for (DevBuf *b : bufs) b->release();
+  cudaEventDestroy(ctx->ev0);
+  cudaEventDestroy(ctx->ev1);
+  cudaStreamDestroy(ctx->stream);
+  delete ctx;
+}
+
+const char *ish_gpu_last_error(const ish_ctx *ctx) { return ctx ? ctx->err.c_str() : g_open_error.c_str(); }
+
+int ish_gpu_set_option(ish_ctx *ctx, int option, int64_t value) {
+  if (!ctx) return ISH_EINVAL;
+  switch (option) {
+  case ISH_OPT_KERNEL:
+    if (value < ISH_KERNEL_AUTO || value > ISH_KERNEL_EXACT) return fail(ctx, ISH_EINVAL, "bad kernel %lld", (long long)value);
+    ctx->kernel = (int)value;
+    return ISH_OK;
+  case ISH_OPT_SG_LANES:
+  case ISH_OPT_SW_U8_LANES:
+  case ISH_OPT_SW_U16_LANES:
+    if (value < 1 || value > 64) return fail(ctx, ISH_EINVAL, "lane count must be in 1..64");
+    (option == ISH_OPT_SG_LANES ? ctx->sg_lanes : option == ISH_OPT_SW_U8_LANES ? ctx->sw_u8_lanes : ctx->sw_u16_lanes) =
+        (int)value;
+    return ISH_OK;
+  case ISH_OPT_WAVE_GROUP:
+    if (value != 0 && (value < 1 || value > 32 || (value & (value - 1))))
+      return fail(ctx, ISH_EINVAL, "group size must be 0 or a power of two <= 32");
+    ctx->force_G = (int)value;
+    return ISH_OK;
+  case ISH_OPT_WAVE_K:
+    if (value != 0 && (value < 2 || value > WAVE_KMAX || (value & 1)))
+      return fail(ctx, ISH_EINVAL, "K must be 0 or even in 2..%d", WAVE_KMAX);
+    ctx->force_K = (int)value;
+    return ISH_OK;
+  default:
+    return fail(ctx, ISH_EINVAL, "unknown option %d", option);
+  }
+}
+
+int ish_gpu_set_query(ish_ctx *ctx, const uint8_t *enc_query, uint32_t qlen, int matrix_kind, const int8_t *matrix,
+                      uint32_t alphabet, int algo, uint32_t gap_open, uint32_t gap_ext, uint32_t ends_free,
+                      int32_t max_score, float threshold, int32_t *query_id) {
+  if (!ctx || !query_id) return ctx ? fail(ctx, ISH_EINVAL, "query_id is NULL") : ISH_EINVAL;
+  if (algo != ISH_ALGO_SEMI_GLOBAL && algo != ISH_ALGO_LOCAL) return fail(ctx, ISH_EINVAL, "unknown algorithm %d", algo);
+  if (matrix_kind < ISH_MATRIX_ASCII || matrix_kind > ISH_MATRIX_BLOSUM62)
+    return fail(ctx, ISH_EINVAL, "unknown matrix kind %d", matrix_kind);
+  if (!matrix || !matrix_alphabet_ok(alphabet)) return fail(ctx, ISH_EINVAL, "matrix must be alphabet^2 int8, alphabet 1..256");
+  if (qlen && !enc_query) return fail(ctx, ISH_EINVAL, "enc_query is NULL");
+  if (qlen > 32767) return fail(ctx, ISH_EOVERFLOW, "query of %u residues is longer than 32767", qlen);
+  if (ends_free > 15) return fail(ctx, ISH_EINVAL, "ends_free has bits above ISH_FREE_TARGET_END");
+  Query q;
+  q.algo = algo;
+  q.kind = matrix_kind;
+  q.alphabet = (int)alphabet;
+  q.Q = (int)qlen;
+  // The matchers hand UInt penalties to lanes of the pass type: int16 for the
+  // semi-global pass (striped_semi_global_matcher.mojo:232-245), uint8 for
+  // ssw_align (local_aln/striped.mojo:151-152).
+  if (algo == ISH_ALGO_SEMI_GLOBAL) {
+    q.open = (int16_t)gap_open;
+    q.ext = (int16_t)gap_ext;
+  } else {
+    q.open = (uint8_t)gap_open;
+    q.ext = (uint8_t)gap_ext;
+  }
+  q.ends = algo == ISH_ALGO_SEMI_GLOBAL ? (int)ends_free : 0;
+  q.max_score = max_score;
+  q.thr = threshold;
+  q.M.assign(matrix, matrix + (size_t)alphabet * alphabet);
+  q.q.assign(enc_query, enc_query + qlen);
+  for (uint32_t i = 0; i < qlen; ++i)
+    if (q.q[i] >= alphabet) return fail(ctx, ISH_EINVAL, "query code %u at %u >= alphabet %u", q.q[i], i, alphabet);
+  q.mmin = 0;
+  q.mmax = 0;
+  for (int8_t v : q.M) {
+    q.mmin = std::min<int>(q.mmin, v);
+    q.mmax = std::max<int>(q.mmax, v);
+  }
+  q.neg_limit = neg_limit_of(q.open, q.mmin);
+  cudaSetDevice(ctx->device);
+  const int32_t id = ctx->next_query++;
+  ctx->queries.emplace(id, std::move(q));
+  *query_id = id;
+  return ISH_OK;
+}
+
+int ish_gpu_free_query(ish_ctx *ctx, int32_t query_id) {
+  if (!ctx) return ISH_EINVAL;
+  auto it = ctx->queries.find(query_id);
+  if (it == ctx->queries.end()) return fail(ctx, ISH_EINVAL, "unknown query %d", query_id);
+  cudaStreamSynchronize(ctx->stream);
+  it->second.plain_prof.release();
+  it->second.plain_hinit.release();
+  for (auto &l : it->second.layouts) {
+    l.second.prof.release();
+    l.second.hinit.release();
+  }
+  ctx->queries.erase(it);
+  return ISH_OK;
+}
+
+int ish_gpu_records_load(ish_ctx *ctx, const uint8_t *records, const uint64_t *offsets, uint32_t n, int32_t *set_id) {
+  if (!ctx || !set_id) return ctx ? fail(ctx, ISH_EINVAL, "set_id is NULL") : ISH_EINVAL;
+  cudaSetDevice(ctx->device);
+  RecordSet rs;
+  int rc = load_records(ctx, records, offsets, n, rs);
+  if (rc) {
+    rs.codes.release();
+    rs.off_s.release();
+    rs.len_s.release();
+    rs.orig_s.release();
+    return rc;
+  }
+  const int32_t id = ctx->next_set++;
+  ctx->sets.emplace(id, std::move(rs));
+  *set_id = id;
+  return ISH_OK;
+}
+
+int ish_gpu_records_free(ish_ctx *ctx, int32_t set_id) {
+  if (!ctx) return ISH_EINVAL;
+  auto it = ctx->sets.find(set_id);
+  if (it == ctx->sets.end()) return fail(ctx, ISH_EINVAL, "unknown record set %d", set_id);
+  cudaStreamSynchronize(ctx->stream);
+  it->second.codes.release();
+  it->second.off_s.release();
+  it->second.len_s.release();
+  it->second.orig_s.release();
+  ctx->sets.erase(it);
+  return ISH_OK;
+}
+
+int ish_gpu_records_info(ish_ctx *ctx, int32_t set_id, uint32_t *n, uint64_t *total_bytes) {
+  if (!ctx) return ISH_EINVAL;
+  auto it = ctx->sets.find(set_id);
+  if (it == ctx->sets.end()) return fail(ctx, ISH_EINVAL, "unknown record set %d", set_id);
+  if (n) *n = it->second.n;
+  if (total_bytes) *total_bytes = it->second.total;
+  return ISH_OK;
+}
+
+int ish_gpu_score_set(ish_ctx *ctx, int32_t query_id, int32_t set_id, int32_t *score, int32_t *query_end,
+                      int32_t *target_end, uint8_t *hit, uint32_t *hit_idx, uint32_t *n_hits) {
+  if (!ctx) return ISH_EINVAL;
+  auto qi = ctx->queries.find(query_id);
+  if (qi == ctx->queries.end()) return fail(ctx, ISH_EINVAL, "unknown query %d", query_id);
+  auto si = ctx->sets.find(set_id);
+  if (si == ctx->sets.end()) return fail(ctx, ISH_EINVAL, "unknown record set %d", set_id);
+  cudaSetDevice(ctx->device);
+  int rc = run_scoring(ctx, qi->second, si->second);
+  if (rc) {
+    cudaStreamSynchronize(ctx->stream);
+    return rc;
+  }
+  return fetch_outputs(ctx, si->second.n, score, query_end, target_end, hit, hit_idx, n_hits);
+}
+
+int ish_gpu_score(ish_ctx *ctx, int32_t query_id, const uint8_t *records, const uint64_t *offsets, uint32_t n,
+                  int32_t *score, int32_t *query_end, int32_t *target_end, uint8_t *hit, uint32_t *hit_idx,
+                  uint32_t *n_hits) {
+  if (!ctx) return ISH_EINVAL;
+  auto qi = ctx->queries.find(query_id);
+  if (qi == ctx->queries.end()) return fail(ctx, ISH_EINVAL, "unknown query %d", query_id);
+  cudaSetDevice(ctx->device);
+  RecordSet rs;
+  int rc = load_records(ctx, records, offsets, n, rs);
+  if (!rc) rc = run_scoring(ctx, qi->second, rs);
+  if (!rc) rc = fetch_outputs(ctx, n, score, query_end, target_end, hit, hit_idx, n_hits);
+  cudaStreamSynchronize(ctx->stream);
+  rs.codes.release();
+  rs.off_s.release();
+  rs.len_s.release();
+  rs.orig_s.release();
+  return rc;
+}
+
+int ish_gpu_calibrate(ish_ctx *ctx, double *dpx_ops_per_s) {
+  if (!ctx || !dpx_ops_per_s) return ISH_EINVAL;
+  cudaSetDevice(ctx->device);
+  CU(ctx->counter.ensure(64));
+  const int blocks = ctx->num_sms * 8, threads = 256, iters = 8192;
+  cudaStream_t s = ctx->stream;
+  k_dpx_peak<<<blocks, threads, 0, s>>>(ctx->counter.as<uint32_t>(), 256, 0x00010001u, 0xfffbfffbu);  // warm-up
+  CU(cudaEventRecord(ctx->ev0, s));
+  k_dpx_peak<<<blocks, threads, 0, s>>>(ctx->counter.as<uint32_t>(), iters, 0x00010001u, 0xfffbfffbu);
+  CU(cudaEventRecord(ctx->ev1, s));
+  CU(cudaGetLastError());
+  CU(cudaStreamSynchronize(s));
+  float ms = 0.f;
+  CU(cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1));
+  *dpx_ops_per_s = (double)blocks * threads * iters * 8 / (ms * 1e-3);
+  return ISH_OK;
+}
+
+int ish_gpu_last_kernel_ms(ish_ctx *ctx, double *ms) {
+  if (!ctx || !ms) return ISH_EINVAL;
+  *ms = ctx->last_ms;
+  return ISH_OK;
+}
+
+}  // extern "C"
+
+// Dispatch over the instantiation files.
+namespace ish {
+WaveFn wave_fn_a(int, int, int);
+WaveFn wave_fn_b(int, int, int);
+WaveFn wave_fn_c(int, int, int);
+WaveFn wave_fn_d(int, int, int);
+WaveFn wave_fn(int K, int mode, int pair) {
+  if (K <= 16) return wave_fn_a(K, mode, pair);
+  if (K <= 32) return wave_fn_b(K, mode, pair);
+  if (K <= 48) return wave_fn_c(K, mode, pair);
+  return wave_fn_d(K, mode, pair);
+}
+}  // namespace ish

@@ -1,0 +1,389 @@
+// kernels.cu -- record packing, the plain one-thread-per-record kernel and
+// the epilogue kernels of the GB300 alignment-scoring engine.
+#include "kernels.cuh"
+
+namespace ish {
+
+// ---------------------------------------------------------------------------
+// Record packing.  The caller's records arrive as one concatenated byte array
+// plus n+1 offsets (what ish's runners accumulate per batch,
+// ishlib/parallel_line_search_runner.mojo:84-111).  On the device each record
+// is copied to a 16-byte aligned slot (so the wavefront feeder can stream it
+// with 16-byte loads) and the records are ordered by descending length, so
+// that the two records of a pair have nearly the same length and the longest
+// pairs start first.
+// ---------------------------------------------------------------------------
+
+__device__ __forceinline__ uint32_t len_bucket(uint64_t len) {
+  // exact below 32768, 32-residue resolution above (records up to ~1 Mb)
+  if (len < 32768) return (uint32_t)len;
+  uint64_t b = 32768 + ((len - 32768) >> 5);
+  return b > NBUCKETS - 1 ? NBUCKETS - 1 : (uint32_t)b;
+}
+
+__global__ void k_lengths(const uint64_t *off, uint32_t n, uint32_t *len, uint64_t *slot_bytes,
+                          uint32_t *hist) {
+  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    const uint64_t l = off[i + 1] - off[i];
+    len[i] = (uint32_t)l;
+    slot_bytes[i] = (l + 15) & ~(uint64_t)15;
+    atomicAdd(&hist[len_bucket(l)], 1u);
+  }
+}
+
+// Exclusive scan of the bucket histogram in DESCENDING bucket order (one block).
+__global__ void k_bucket_scan(uint32_t *hist) {
+  __shared__ uint32_t part[1024];
+  const int tid = threadIdx.x;
+  const int per = NBUCKETS / 1024;
+  // thread tid owns descending buckets [tid*per, (tid+1)*per) counted from the top
+  uint32_t s = 0;
+  for (int k = 0; k < per; ++k) s += hist[NBUCKETS - 1 - (tid * per + k)];
+  part[tid] = s;
+  __syncthreads();
+  for (int off = 1; off < 1024; off <<= 1) {
+    uint32_t v = tid >= off ? part[tid - off] : 0;
+    __syncthreads();
+    part[tid] += v;
+    __syncthreads();
+  }
+  uint32_t run = part[tid] - s;
+  for (int k = 0; k < per; ++k) {
+    const int b = NBUCKETS - 1 - (tid * per + k);
+    const uint32_t c = hist[b];
+    hist[b] = run;
+    run += c;
+  }
+}
+
+__global__ void k_scatter(const uint32_t *len, const uint64_t *poff, uint32_t n, uint32_t *cursor,
+                          uint32_t *len_s, uint64_t *off_s, uint32_t *orig_s) {
+  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    const uint32_t l = len[i];
+    const uint32_t pos = atomicAdd(&cursor[len_bucket(l)], 1u);
+    len_s[pos] = l;
+    off_s[pos] = poff[i];
+    orig_s[pos] = i;
+  }
+}
+
+// One warp per record: copy src[off[i] .. off[i+1]) to dst[poff[i] ..) with
+// 16-byte stores, realigning 4-byte words with funnel shifts; the tail of the
+// 16-byte slot is zero-filled.
+__global__ void k_pack(const uint8_t *src, uint64_t src_bytes, const uint64_t *off, const uint64_t *poff,
+                       uint32_t n, uint8_t *dst) {
+  const uint32_t warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const uint32_t lane = threadIdx.x & 31;
+  const uint32_t nwarps = (gridDim.x * blockDim.x) >> 5;
+  const uint32_t *src32 = reinterpret_cast<const uint32_t *>(src);
+  const uint64_t nwords = (src_bytes + 3) >> 2;
+  for (uint32_t r = warp; r < n; r += nwarps) {
+    const uint64_t s0 = off[r], len = off[r + 1] - off[r];
+    uint4 *d = reinterpret_cast<uint4 *>(dst + poff[r]);
+    const uint64_t nchunks = (len + 15) >> 4;
+    for (uint64_t c = lane; c < nchunks; c += 32) {
+      const uint64_t b = s0 + c * 16;  // first source byte of the chunk
+      const uint64_t w0 = b >> 2;
+      const uint32_t sh = (uint32_t)(b & 3) * 8;
+      uint32_t w[5];
+#pragma unroll
+      for (int k = 0; k < 5; ++k) w[k] = (w0 + k < nwords) ? __ldg(src32 + w0 + k) : 0u;
+      uint32_t o[4];
+#pragma unroll
+      for (int k = 0; k < 4; ++k) o[k] = __funnelshift_r(w[k], w[k + 1], sh);
+      // zero bytes past the record end
+      const uint64_t rem = len - c * 16;
+      if (rem < 16) {
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+          const int64_t keep = (int64_t)rem - 4 * k;
+          if (keep <= 0) o[k] = 0;
+          else if (keep < 4) o[k] &= (1u << (8 * keep)) - 1u;
+        }
+      }
+      d[c] = make_uint4(o[0], o[1], o[2], o[3]);
+    }
+  }
+}
+
+// Exclusive scan of uint64 values (n <= 1024 * 1024 * 16 per call level).
+__global__ void k_scan64_block(const uint64_t *in, uint64_t *out, uint32_t n, uint64_t *block_sums) {
+  __shared__ uint64_t warp_sums[32];
+  const uint32_t base = blockIdx.x * SCAN_TILE;
+  const int tid = threadIdx.x;
+  // each thread scans SCAN_TILE / 1024 consecutive values
+  constexpr int PER = SCAN_TILE / 1024;
+  uint64_t v[PER];
+  uint64_t s = 0;
+#pragma unroll
+  for (int k = 0; k < PER; ++k) {
+    const uint32_t i = base + tid * PER + k;
+    v[k] = i < n ? in[i] : 0;
+    s += v[k];
+  }
+  // inclusive warp scan of s
+  uint64_t x = s;
+  const int lane = tid & 31, wid = tid >> 5;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const uint64_t y = __shfl_up_sync(0xffffffffu, x, o);
+    if (lane >= o) x += y;
+  }
+  if (lane == 31) warp_sums[wid] = x;
+  __syncthreads();
+  if (wid == 0) {
+    uint64_t w = warp_sums[lane];
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const uint64_t y = __shfl_up_sync(0xffffffffu, w, o);
+      if (lane >= o) w += y;
+    }
+    warp_sums[lane] = w;
+  }
+  __syncthreads();
+  uint64_t run = x - s + (wid > 0 ? warp_sums[wid - 1] : 0);
+#pragma unroll
+  for (int k = 0; k < PER; ++k) {
+    const uint32_t i = base + tid * PER + k;
+    if (i < n) out[i] = run;
+    run += v[k];
+  }
+  if (tid == 1023 && block_sums) block_sums[blockIdx.x] = run;
+}
+
+__global__ void k_scan64_add(uint64_t *out, uint32_t n, const uint64_t *block_offsets) {
+  const uint32_t b = blockIdx.x;
+  const uint64_t add = block_offsets[b];
+  for (uint32_t i = b * SCAN_TILE + threadIdx.x; i < min(n, (b + 1) * SCAN_TILE); i += blockDim.x) out[i] += add;
+}
+
+// ---------------------------------------------------------------------------
+// Empty records: semi_global_aln returns (0, 0, 0) when the record or the
+// query is empty (semi_global_aln/striped.mojo:275-276); sw on an empty record
+// leaves max 0, end -1 and reports query end 0 (local_aln/striped.mojo:423-428).
+// ---------------------------------------------------------------------------
+__global__ void k_trivial(RecordsDev rec, uint32_t first, uint32_t count, int mode, int qlen, OutDev out,
+                          Decision dec) {
+  for (uint32_t s = blockIdx.x * blockDim.x + threadIdx.x; s < count; s += gridDim.x * blockDim.x) {
+    const uint32_t orig = rec.orig[first + s];
+    int32_t score = 0, qe = 0, te = 0;
+    if (mode == SW) {
+      te = -1;
+      qe = qlen > 0 ? 0 : -1;
+    }
+    if (out.score) out.score[orig] = score;
+    if (out.qend) out.qend[orig] = qe;
+    if (out.tend) out.tend[orig] = te;
+    if (out.hit) out.hit[orig] = decide(mode, score, qe, te, dec);
+  }
+}
+
+// ---------------------------------------------------------------------------
+// The plain kernel: one thread per record, scalar int32 Gotoh with the query
+// on the inner loop -- the design of the reference's GPU kernel
+// (ishlib/gpu/kernels/semi_global.mojo:20-115 with
+// ishlib/matcher/alignment/semi_global_aln/basic.mojo:242-425) made exact:
+// it applies the end rules of the striped CPU matchers.  Its H and E columns
+// live in a global scratch buffer, interleaved by thread for coalescing.
+// It is the one-query-per-launch comparison for the wavefront kernel.
+// ---------------------------------------------------------------------------
+template <int MODE>
+__global__ void __launch_bounds__(128) plain_kernel(const PlainParams p) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int16_t *prof = p.prof;
+  if (p.use_smem) {
+    uint4 *dst = reinterpret_cast<uint4 *>(smem_raw);
+    const uint4 *src = reinterpret_cast<const uint4 *>(p.prof);
+    for (uint32_t i = threadIdx.x; i < p.prof_bytes / 16; i += blockDim.x) dst[i] = src[i];
+    __syncthreads();
+    prof = reinterpret_cast<const int16_t *>(smem_raw);
+  }
+  const uint32_t nth = p.nthreads;
+  const uint32_t gt = blockIdx.x * blockDim.x + threadIdx.x;
+  if (gt >= nth) return;
+  const int Q = p.Q, open = p.open, ext = p.ext;
+  const bool ts = p.ends & 4, te = p.ends & 8, qe = p.ends & 2;
+  int32_t *Hc = p.scratch + gt;
+  int32_t *Ec = p.scratch + (size_t)Q * nth + gt;
+  for (uint32_t s = gt; s < p.count; s += nth) {
+    const uint32_t idx = p.first + s;
+    const int T = (int)p.rec.len[idx];
+    const uint8_t *codes = p.rec.codes + p.rec.off[idx];
+    const uint32_t orig = p.rec.orig[idx];
+    for (int q = 0; q < Q; ++q) {
+      const int h0 = p.hinit[q];
+      Hc[(size_t)q * nth] = h0;
+      Ec[(size_t)q * nth] = MODE == SW ? 0 : h0 - open;
+    }
+    int best = MODE == SW ? 0 : p.neg_limit, er = -1, eq = MODE == SW ? 0 : Q - 1;
+    int hlast = 0;
+    for (int i = 0; i < T; ++i) {
+      uint32_t c = codes[i];
+      if (c >= (uint32_t)p.alphabet) {
+        atomicOr(p.error, 1);
+        c = 0;
+      }
+      const int16_t *prow = prof + (size_t)c * Q;
+      int hdiag, F;
+      if (MODE == SW) {
+        hdiag = 0;
+        F = 0;
+      } else {
+        hdiag = (i == 0 || ts) ? 0 : -open - ext * (i - 1);  // boundary[i]
+        F = (ts ? 0 : -open - ext * i) - open;                // boundary[i+1] - open
+      }
+      int colmax = 0, colq = 0;
+      int h = 0;
+      for (int q = 0; q < Q; ++q) {
+        const int e = Ec[(size_t)q * nth];
+        const int hold = Hc[(size_t)q * nth];
+        h = max(hdiag + prow[q], max(e, F));
+        hdiag = hold;
+        Hc[(size_t)q * nth] = h;
+        int v = h - open;
+        if (MODE == SW) v = max(v, 0);
+        Ec[(size_t)q * nth] = max(e - ext, v);
+        F = max(F - ext, v);
+        if (MODE == SW && h > colmax) {
+          colmax = h;
+          colq = q;
+        }
+      }
+      if (MODE == SW) {
+        if (colmax > best) {
+          best = colmax;
+          er = i;
+          eq = colq;
+        }
+      } else {
+        if (h > best) {
+          best = h;
+          er = i;
+        }
+        hlast = h;
+      }
+    }
+    int score, tend, qend;
+    if (MODE == SW) {
+      score = best;
+      tend = best == 0 ? -1 : er;
+      qend = best == 0 ? 0 : eq;
+    } else if (!te && !qe) {
+      score = hlast;
+      tend = T - 1;
+      qend = Q - 1;
+    } else {
+      score = te ? best : p.neg_limit;
+      tend = er;
+      qend = Q - 1;
+      if (qe) {
+        for (int q = 0; q < Q; ++q) {
+          const int v = Hc[(size_t)q * nth];
+          if (v > score) {
+            score = v;
+            qend = q;
+            tend = T - 1;
+          } else if (v == score && tend == T - 1 && q < qend) {
+            qend = q;
+          }
+        }
+      }
+    }
+    if (p.out.score) p.out.score[orig] = score;
+    if (p.out.qend) p.out.qend[orig] = qend;
+    if (p.out.tend) p.out.tend[orig] = tend;
+    if (p.out.hit) p.out.hit[orig] = decide(MODE, score, qend, tend, p.dec);
+  }
+}
+
+PlainFn plain_fn(int mode) { return mode == SW ? (PlainFn)plain_kernel<SW> : (PlainFn)plain_kernel<SG>; }
+
+// ---------------------------------------------------------------------------
+// Hit compaction: indices of hit[i] != 0 in ascending order.
+// ---------------------------------------------------------------------------
+__global__ void k_count_hits(const uint8_t *hit, uint32_t n, uint32_t *block_counts) {
+  __shared__ uint32_t wsum[32];
+  const uint32_t base = blockIdx.x * HIT_TILE;
+  uint32_t c = 0;
+  for (uint32_t i = base + threadIdx.x; i < min(n, base + HIT_TILE); i += blockDim.x) c += hit[i] != 0;
+  for (int o = 16; o > 0; o >>= 1) c += __shfl_down_sync(0xffffffffu, c, o);
+  if ((threadIdx.x & 31) == 0) wsum[threadIdx.x >> 5] = c;
+  __syncthreads();
+  if (threadIdx.x < 32) {
+    uint32_t v = threadIdx.x < (blockDim.x >> 5) ? wsum[threadIdx.x] : 0;
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+    if (threadIdx.x == 0) block_counts[blockIdx.x] = v;
+  }
+}
+
+__global__ void k_scan_counts(uint32_t *counts, uint32_t nb, uint32_t *total) {
+  // single block, sequential chunks of 1024
+  __shared__ uint32_t part[1024];
+  uint32_t carry = 0;
+  for (uint32_t base = 0; base < nb; base += 1024) {
+    const uint32_t i = base + threadIdx.x;
+    const uint32_t v = i < nb ? counts[i] : 0;
+    part[threadIdx.x] = v;
+    __syncthreads();
+    for (int o = 1; o < 1024; o <<= 1) {
+      const uint32_t y = threadIdx.x >= (unsigned)o ? part[threadIdx.x - o] : 0;
+      __syncthreads();
+      part[threadIdx.x] += y;
+      __syncthreads();
+    }
+    if (i < nb) counts[i] = carry + part[threadIdx.x] - v;
+    const uint32_t tot = part[1023];
+    __syncthreads();
+    carry += tot;
+  }
+  if (threadIdx.x == 0) *total = carry;
+}
+
+__global__ void k_write_hits(const uint8_t *hit, uint32_t n, const uint32_t *block_offsets, uint32_t *idx) {
+  __shared__ uint32_t wsum[32];
+  __shared__ uint32_t run;
+  const uint32_t base = blockIdx.x * HIT_TILE;
+  if (threadIdx.x == 0) run = block_offsets[blockIdx.x];
+  __syncthreads();
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  for (uint32_t b = base; b < min(n, base + HIT_TILE); b += blockDim.x) {
+    const uint32_t i = b + threadIdx.x;
+    const bool h = i < n && i < base + HIT_TILE && hit[i];
+    const uint32_t m = __ballot_sync(0xffffffffu, h);
+    if (lane == 0) wsum[wid] = __popc(m);
+    __syncthreads();
+    uint32_t before = 0, total = 0;
+    for (int w = 0; w < nw; ++w) {
+      if (w < wid) before += wsum[w];
+      total += wsum[w];
+    }
+    if (h) idx[run + before + __popc(m & ((1u << lane) - 1u))] = i;
+    __syncthreads();
+    if (threadIdx.x == 0) run += total;
+    __syncthreads();
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Calibration: throughput of the packed 16-bit DPX add-max instruction the
+// cell recurrence is built from.  Eight independent dependency chains per
+// thread keep the pipe busy; the result is folded so nothing is dead code.
+// ---------------------------------------------------------------------------
+__global__ void k_dpx_peak(uint32_t *out, int iters, uint32_t b, uint32_t c) {
+  uint32_t a[8], cc[8];
+#pragma unroll
+  for (int k = 0; k < 8; ++k) {
+    a[k] = threadIdx.x * 0x00010001u + k;
+    cc[k] = c + k * 0x00030005u;
+  }
+  for (int i = 0; i < iters; ++i) {
+#pragma unroll
+    for (int k = 0; k < 8; ++k) a[k] = __viaddmax_s16x2(a[k], b, cc[k]);
+  }
+  uint32_t x = 0;
+#pragma unroll
+  for (int k = 0; k < 8; ++k) x ^= a[k];
+  if (x == 0x12345678u) out[0] = x;
+}
+
+}  // namespace ish

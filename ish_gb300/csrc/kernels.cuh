@@ -1,0 +1,37 @@
+// kernels.cuh -- declarations shared by the kernel translation units and the
+// host engine.
+#pragma once
+
+#include "engine.cuh"
+
+namespace ish {
+
+constexpr uint32_t NBUCKETS = 65536;     // length buckets of the record sort
+constexpr uint32_t SCAN_TILE = 4096;     // values per block of k_scan64_block (1024 threads)
+constexpr uint32_t HIT_TILE = 8192;      // records per block of the hit compaction
+
+__global__ void k_lengths(const uint64_t *off, uint32_t n, uint32_t *len, uint64_t *slot_bytes, uint32_t *hist);
+__global__ void k_bucket_scan(uint32_t *hist);
+__global__ void k_scatter(const uint32_t *len, const uint64_t *poff, uint32_t n, uint32_t *cursor, uint32_t *len_s,
+                          uint64_t *off_s, uint32_t *orig_s);
+__global__ void k_pack(const uint8_t *src, uint64_t src_bytes, const uint64_t *off, const uint64_t *poff, uint32_t n,
+                       uint8_t *dst);
+__global__ void k_scan64_block(const uint64_t *in, uint64_t *out, uint32_t n, uint64_t *block_sums);
+__global__ void k_scan64_add(uint64_t *out, uint32_t n, const uint64_t *block_offsets);
+__global__ void k_trivial(RecordsDev rec, uint32_t first, uint32_t count, int mode, int qlen, OutDev out, Decision dec);
+typedef void (*PlainFn)(const PlainParams);
+PlainFn plain_fn(int mode);  // plain_kernel<SG> / plain_kernel<SW>
+__global__ void k_count_hits(const uint8_t *hit, uint32_t n, uint32_t *block_counts);
+__global__ void k_scan_counts(uint32_t *counts, uint32_t nb, uint32_t *total);
+__global__ void k_dpx_peak(uint32_t *out, int iters, uint32_t b, uint32_t c);
+__global__ void k_write_hits(const uint8_t *hit, uint32_t n, const uint32_t *block_offsets, uint32_t *idx);
+
+// Wavefront kernels are instantiated for K = 2, 4, ..., WAVE_KMAX columns per
+// thread, both modes and both profile layouts.
+constexpr int WAVE_KMAX = 64;
+constexpr int WAVE_THREADS = 256;
+typedef void (*WaveFn)(const WaveParams);
+// Returns the kernel for (K, mode, pair profile) or nullptr.
+WaveFn wave_fn(int K, int mode, int pair);
+
+}  // namespace ish

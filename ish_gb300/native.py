@@ -1,0 +1,221 @@
+"""ctypes binding of libish_gpu.so (include/ish_gpu.h).
+
+The library is built in-tree by ``ish_gb300.build``; loading fails loudly when
+it is missing -- there is no CPU fallback behind this module.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+from . import build as _build
+
+OK = 0
+EINVAL, ENOMEM, EOVERFLOW, ENODEV, EDEVICE, EAGAIN, ETIMEDOUT = -22, -12, -75, -19, -5, -11, -110
+ALGO_SEMI_GLOBAL, ALGO_LOCAL = 0, 1
+FREE_QUERY_START, FREE_QUERY_END, FREE_TARGET_START, FREE_TARGET_END = 1, 2, 4, 8
+KERNEL_AUTO, KERNEL_PLAIN, KERNEL_EXACT = 0, 1, 2
+OPT_KERNEL, OPT_SG_LANES, OPT_SW_U8_LANES, OPT_SW_U16_LANES, OPT_WAVE_GROUP, OPT_WAVE_K = 1, 2, 3, 4, 5, 6
+
+# Entry points declared in include/ish_gpu.h (checked by the tests).
+EXPORTS = (
+    "ish_gpu_abi_version", "ish_gpu_open", "ish_gpu_close", "ish_gpu_last_error", "ish_gpu_set_option",
+    "ish_gpu_set_query", "ish_gpu_free_query", "ish_gpu_score", "ish_gpu_records_load", "ish_gpu_records_free",
+    "ish_gpu_records_info", "ish_gpu_score_set", "ish_gpu_last_kernel_ms", "ish_gpu_calibrate",
+)
+
+
+class IshGpuError(RuntimeError):
+    def __init__(self, code: int, msg: str):
+        super().__init__(f"ish_gpu error {code}: {msg}")
+        self.code = code
+
+
+_lib = None
+
+u8p = C.POINTER(C.c_uint8)
+i8p = C.POINTER(C.c_int8)
+i32p = C.POINTER(C.c_int32)
+u32p = C.POINTER(C.c_uint32)
+u64p = C.POINTER(C.c_uint64)
+
+
+def lib_path() -> str:
+    return _build.LIB
+
+
+def load(build_if_missing: bool = False):
+    """Load libish_gpu.so; raises if it is not built (or builds it on request)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    path = _build.LIB
+    if not os.path.exists(path):
+        if not build_if_missing:
+            raise OSError(f"{path} is not built; run `python -m ish_gb300.build`")
+        _build.build()
+    L = C.CDLL(path)
+    vp = C.c_void_p
+    L.ish_gpu_abi_version.restype = C.c_int
+    L.ish_gpu_open.argtypes = [C.c_int, C.POINTER(vp)]
+    L.ish_gpu_close.argtypes = [vp]
+    L.ish_gpu_close.restype = None
+    L.ish_gpu_last_error.argtypes = [vp]
+    L.ish_gpu_last_error.restype = C.c_char_p
+    L.ish_gpu_set_option.argtypes = [vp, C.c_int, C.c_int64]
+    L.ish_gpu_set_query.argtypes = [vp, u8p, C.c_uint32, C.c_int, i8p, C.c_uint32, C.c_int, C.c_uint32, C.c_uint32,
+                                    C.c_uint32, C.c_int32, C.c_float, i32p]
+    L.ish_gpu_free_query.argtypes = [vp, C.c_int32]
+    L.ish_gpu_score.argtypes = [vp, C.c_int32, u8p, u64p, C.c_uint32, i32p, i32p, i32p, u8p, u32p, u32p]
+    L.ish_gpu_records_load.argtypes = [vp, u8p, u64p, C.c_uint32, i32p]
+    L.ish_gpu_records_free.argtypes = [vp, C.c_int32]
+    L.ish_gpu_records_info.argtypes = [vp, C.c_int32, u32p, u64p]
+    L.ish_gpu_score_set.argtypes = [vp, C.c_int32, C.c_int32, i32p, i32p, i32p, u8p, u32p, u32p]
+    L.ish_gpu_last_kernel_ms.argtypes = [vp, C.POINTER(C.c_double)]
+    L.ish_gpu_calibrate.argtypes = [vp, C.POINTER(C.c_double)]
+    for name in EXPORTS:
+        if name not in ("ish_gpu_close", "ish_gpu_last_error"):
+            getattr(L, name).restype = C.c_int
+    _lib = L
+    return L
+
+
+def _p(a, ct):
+    return None if a is None else a.ctypes.data_as(C.POINTER(ct))
+
+
+def pack_records(records):
+    """Concatenate a list of byte strings / uint8 arrays: (bytes uint8[], offsets uint64[n+1])."""
+    lens = np.fromiter((len(r) for r in records), dtype=np.uint64, count=len(records))
+    off = np.zeros(len(records) + 1, np.uint64)
+    np.cumsum(lens, out=off[1:])
+    buf = np.empty(int(off[-1]) if len(records) else 0, np.uint8)
+    for i, r in enumerate(records):
+        a, b = int(off[i]), int(off[i + 1])
+        if b > a:
+            buf[a:b] = np.frombuffer(r, np.uint8) if isinstance(r, (bytes, bytearray)) else r
+    return buf, off
+
+
+class Context:
+    """One engine context on one CUDA device (one per host thread)."""
+
+    def __init__(self, device: int = 0):
+        L = load()
+        h = C.c_void_p()
+        rc = L.ish_gpu_open(device, C.byref(h))
+        if rc != OK:
+            raise IshGpuError(rc, L.ish_gpu_last_error(None).decode())
+        self._L = L
+        self._h = h
+
+    def close(self):
+        if getattr(self, "_h", None):
+            self._L.ish_gpu_close(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def _check(self, rc):
+        if rc != OK:
+            raise IshGpuError(rc, self._L.ish_gpu_last_error(self._h).decode())
+        return rc
+
+    def set_option(self, option: int, value: int):
+        self._check(self._L.ish_gpu_set_option(self._h, option, int(value)))
+
+    def set_query(self, enc_query, matrix_kind: int, matrix: np.ndarray, algo: int, gap_open: int, gap_ext: int,
+                  ends_free: int, max_score: int, threshold: float) -> int:
+        q = np.ascontiguousarray(enc_query, np.uint8)
+        m = np.ascontiguousarray(matrix, np.int8).ravel()
+        alphabet = int(round(len(m) ** 0.5))
+        qid = C.c_int32()
+        self._check(self._L.ish_gpu_set_query(self._h, _p(q, C.c_uint8), len(q), matrix_kind, _p(m, C.c_int8), alphabet,
+                                              algo, gap_open, gap_ext, ends_free, int(max_score), float(threshold),
+                                              C.byref(qid)))
+        return qid.value
+
+    def free_query(self, qid: int):
+        self._check(self._L.ish_gpu_free_query(self._h, qid))
+
+    def _outputs(self, n, want):
+        out = {}
+        if "score" in want:
+            out["score"] = np.empty(max(n, 1), np.int32)
+        if "qend" in want:
+            out["qend"] = np.empty(max(n, 1), np.int32)
+        if "tend" in want:
+            out["tend"] = np.empty(max(n, 1), np.int32)
+        if "hit" in want:
+            out["hit"] = np.empty(max(n, 1), np.uint8)
+        if "hit_idx" in want:
+            out["hit_idx"] = np.empty(max(n, 1), np.uint32)
+        return out
+
+    def score(self, qid: int, records: np.ndarray, offsets: np.ndarray,
+              want=("score", "qend", "tend", "hit", "hit_idx")) -> dict:
+        records = np.ascontiguousarray(records, np.uint8)
+        offsets = np.ascontiguousarray(offsets, np.uint64)
+        n = len(offsets) - 1
+        out = self._outputs(n, want)
+        nh = C.c_uint32()
+        self._check(self._L.ish_gpu_score(self._h, qid, _p(records, C.c_uint8), _p(offsets, C.c_uint64), n,
+                                          _p(out.get("score"), C.c_int32), _p(out.get("qend"), C.c_int32),
+                                          _p(out.get("tend"), C.c_int32), _p(out.get("hit"), C.c_uint8),
+                                          _p(out.get("hit_idx"), C.c_uint32), C.byref(nh)))
+        res = {k: v[:n] for k, v in out.items() if k != "hit_idx"}
+        if "hit_idx" in out:
+            res["hit_idx"] = out["hit_idx"][: nh.value]
+        return res
+
+    def records_load(self, records: np.ndarray, offsets: np.ndarray) -> int:
+        records = np.ascontiguousarray(records, np.uint8)
+        offsets = np.ascontiguousarray(offsets, np.uint64)
+        sid = C.c_int32()
+        self._check(self._L.ish_gpu_records_load(self._h, _p(records, C.c_uint8), _p(offsets, C.c_uint64),
+                                                 len(offsets) - 1, C.byref(sid)))
+        return sid.value
+
+    def records_free(self, sid: int):
+        self._check(self._L.ish_gpu_records_free(self._h, sid))
+
+    def records_info(self, sid: int):
+        n, b = C.c_uint32(), C.c_uint64()
+        self._check(self._L.ish_gpu_records_info(self._h, sid, C.byref(n), C.byref(b)))
+        return n.value, b.value
+
+    def score_set(self, qid: int, sid: int, want=("score", "qend", "tend", "hit", "hit_idx")) -> dict:
+        n, _ = self.records_info(sid)
+        out = self._outputs(n, want)
+        nh = C.c_uint32()
+        self._check(self._L.ish_gpu_score_set(self._h, qid, sid, _p(out.get("score"), C.c_int32),
+                                              _p(out.get("qend"), C.c_int32), _p(out.get("tend"), C.c_int32),
+                                              _p(out.get("hit"), C.c_uint8), _p(out.get("hit_idx"), C.c_uint32),
+                                              C.byref(nh)))
+        res = {k: v[:n] for k, v in out.items() if k != "hit_idx"}
+        if "hit_idx" in out:
+            res["hit_idx"] = out["hit_idx"][: nh.value]
+        return res
+
+    def calibrate(self) -> float:
+        """Packed 16-bit DPX add-max instructions per second on this device."""
+        r = C.c_double()
+        self._check(self._L.ish_gpu_calibrate(self._h, C.byref(r)))
+        return r.value
+
+    def last_kernel_ms(self) -> float:
+        ms = C.c_double()
+        self._check(self._L.ish_gpu_last_kernel_ms(self._h, C.byref(ms)))
+        return ms.value

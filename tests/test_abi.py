@@ -1,0 +1,71 @@
+"""CPU-side checks of the C ABI: the library builds, loads, exports every
+entry point include/ish_gpu.h declares, and fails cleanly without a GPU."""
+import ctypes as C
+import os
+import re
+
+import numpy as np
+import pytest
+
+import oracle as O
+from ish_gb300 import native
+from ish_gb300.scoring import ScoringMatrix
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+HEADER = os.path.join(ROOT, "include", "ish_gpu.h")
+
+
+def declared_symbols():
+    src = open(HEADER).read()
+    return sorted(set(re.findall(r"^ISH_API[^(]*?\b(ish_gpu_\w+)\s*\(", src, re.M)))
+
+
+def test_header_declares_the_binding_surface():
+    assert declared_symbols() == sorted(native.EXPORTS)
+
+
+def test_library_exports_every_declared_symbol():
+    lib = native.load(build_if_missing=True)
+    for name in declared_symbols():
+        assert hasattr(lib, name), name
+    assert lib.ish_gpu_abi_version() == 1
+
+
+def test_open_reports_error_without_device(monkeypatch):
+    monkeypatch.setenv("CUDA_VISIBLE_DEVICES", os.environ.get("CUDA_VISIBLE_DEVICES", ""))
+    lib = native.load(build_if_missing=True)
+    h = C.c_void_p()
+    rc = lib.ish_gpu_open(0, C.byref(h))
+    try:
+        import torch
+        has_gpu = torch.cuda.is_available()
+    except Exception:
+        has_gpu = False
+    if has_gpu:
+        assert rc == 0
+        lib.ish_gpu_close(h)
+    else:
+        assert rc in (native.ENODEV, native.EDEVICE)
+        assert h.value is None
+        assert lib.ish_gpu_last_error(None)
+
+
+def test_null_arguments_are_rejected():
+    lib = native.load(build_if_missing=True)
+    assert lib.ish_gpu_open(0, None) == native.EINVAL
+    assert lib.ish_gpu_set_option(None, native.OPT_KERNEL, 0) == native.EINVAL
+    lib.ish_gpu_close(None)  # no-op
+
+
+@pytest.mark.parametrize("kind", [O.ASCII, O.ACTGN, O.ACTGN0, O.BLOSUM62])
+def test_product_matrices_match_oracle(kind):
+    vals, size, a2c, c2a = O.matrix(kind)
+    m = ScoringMatrix(kind)
+    assert m.size == size
+    assert (m.values.ravel() == vals).all()
+    assert (m.ascii_to_code == a2c).all()
+    assert (m.code_to_ascii == c2a).all()
+    text = bytes(range(256))
+    enc, score = m.encode_and_score(text)
+    oenc, oscore = O.encode_and_score(kind, text)
+    assert (enc == oenc).all() and score == oscore
