@@ -75,7 +75,7 @@ __global__ void __launch_bounds__(256) wave_kernel(const WaveParams p) {
   uint64_t steps = 0;
 
   // tracking (see header comment)
-  uint32_t best = 0;           // SG: running max of H(i, Q-1); SW: running max of this thread's cells
+  int bestA = 0, bestB = 0;    // SG: running max of H(i, Q-1); SW: running max of this thread's cells
   int rowA = -1, rowB = -1;    // first row of `best`, per lane
   int mqA = 0, mqB = 0;        // SW: smallest column of `best` in that row
   // last-row reduction messages
@@ -179,7 +179,7 @@ __global__ void __launch_bounds__(256) wave_kernel(const WaveParams p) {
           E[j] = (MODE == SW) ? 0u : dup16(h0 - p.open);
         }
         prevH = (t == 0) ? HLEFT : dup16(p.hinit[t * K - 1]);
-        best = (MODE == SW) ? 0u : dup16(p.neg_limit);
+        bestA = bestB = (MODE == SW) ? 0 : p.neg_limit;
         rowA = rowB = -1;
         mqA = mqB = 0;
         row = 0;
@@ -237,11 +237,10 @@ __global__ void __launch_bounds__(256) wave_kernel(const WaveParams p) {
 
       if (MODE == SG) {
         if (te) {
-          bool phi, plo;
-          const uint32_t nb = __vibmax_s16x2(best, H[qlast_local], &phi, &plo);
-          if (!plo) rowA = row;
-          if (!phi) rowB = row;
-          best = nb;
+          // strict improvement only: the FIRST row of the maximum wins
+          const int ha = lo16(H[qlast_local]), hb = hi16(H[qlast_local]);
+          if (ha > bestA) { bestA = ha; rowA = row; }
+          if (hb > bestB) { bestB = hb; rowB = row; }
         }
         if (lastA || lastB) {
           uint32_t mx = 0;
@@ -283,7 +282,7 @@ __global__ void __launch_bounds__(256) wave_kernel(const WaveParams p) {
               if (!te && !qe) {
                 score = hl; er = T - 1; eq = p.Q - 1;
               } else {
-                int s0 = x == 0 ? lo16(best) : hi16(best);
+                int s0 = x == 0 ? bestA : bestB;
                 int r0 = x == 0 ? rowA : rowB;
                 score = te ? s0 : p.neg_limit;
                 er = te ? r0 : (x == 0 ? rowA : rowB);
@@ -308,10 +307,9 @@ __global__ void __launch_bounds__(256) wave_kernel(const WaveParams p) {
 #pragma unroll
         for (int j = 1; j + 1 < K; j += 2) cm = __vimax3_s16x2(cm, H[j], H[j + 1]);
         if ((K & 1) == 0 && K > 1) cm = __vmaxs2(cm, H[K - 1]);
-        bool phi, plo;
-        const uint32_t nb = __vibmax_s16x2(best, cm, &phi, &plo);
-        if (!plo || !phi) {
-          const int ca = lo16(cm), cb = hi16(cm);
+        const int ca = lo16(cm), cb = hi16(cm);
+        const bool upA = ca > bestA, upB = cb > bestB;
+        if (upA || upB) {
           int qa = 0x7fff, qb = 0x7fff;
 #pragma unroll
           for (int j = K - 1; j >= 0; --j) {
@@ -319,12 +317,11 @@ __global__ void __launch_bounds__(256) wave_kernel(const WaveParams p) {
             if (lo16(H[j]) == ca) qa = q;
             if (hi16(H[j]) == cb) qb = q;
           }
-          if (!plo) { rowA = row; mqA = qa; }
-          if (!phi) { rowB = row; mqB = qb; }
+          if (upA) { bestA = ca; rowA = row; mqA = qa; }
+          if (upB) { bestB = cb; rowB = row; mqB = qb; }
         }
-        best = nb;
         if (lastA || lastB) {
-          int bA = lo16(best), bB = hi16(best), rA = rowA, rB = rowB, qA = mqA, qB = mqB;
+          int bA = bestA, bB = bestB, rA = rowA, rB = rowB, qA = mqA, qB = mqB;
           if (t > 0) {
             const int ia = lo16(iR0), ib = hi16(iR0);
             const int ira = (int)iR2, irb = (int)iR3;
