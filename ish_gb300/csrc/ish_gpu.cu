@@ -160,30 +160,27 @@ int neg_limit_of(int open, int mmin) {
 }
 
 // Columns per thread (K) and threads per group (G) for a query length: the
-// smallest modelled cost G*K*(1 + 12/K) with G*K >= Q + 1, K even, K <= 48.
+// smallest modelled cost G*K*(1 + ROW_OVERHEAD/K) with G*K >= Q + 1.  Kernels
+// exist for every K <= 32 (two blocks per SM) and even K up to 64 (one block
+// per SM, charged double).
+int wave_k_available(int k) { return (k >= 1 && k <= 32) || (k > 32 && k <= WAVE_KMAX && !(k & 1)); }
+
 void choose_shape(int Q, int force_G, int force_K, int *G, int *K) {
+  const double ROW_OVERHEAD = 4.0;  // per-row instructions in units of cell pairs
   double bestc = 1e30;
-  int bg = 32, bk = WAVE_KMAX;
+  int bg = 0, bk = 0;
   for (int g = 1; g <= 32; g <<= 1) {
     if (force_G && g != force_G) continue;
-    int k = (Q + 1 + g - 1) / g;
-    k = (k + 1) & ~1;
-    if (k < 2) k = 2;
-    if (force_K) {
-      if (g * force_K < Q + 1) continue;
-      k = force_K;
-    }
-    if (k > (force_K ? WAVE_KMAX : 48)) continue;
-    const double c = (double)g * k * (1.0 + 12.0 / k);
+    int k = force_K ? force_K : (Q + 1 + g - 1) / g;
+    if (!force_K && k > 32) k = (k + 1) & ~1;
+    if (!wave_k_available(k) || g * k < Q + 1) continue;
+    double c = (double)g * k * (1.0 + ROW_OVERHEAD / k);
+    if (k > 32) c *= 2.0;
     if (c < bestc) {
       bestc = c;
       bg = g;
       bk = k;
     }
-  }
-  if (bestc > 1e29) {  // nothing under 48 columns: use the widest shape
-    bg = force_G ? force_G : 32;
-    bk = ((Q + 1 + bg - 1) / bg + 1) & ~1;
   }
   *G = bg;
   *K = bk;
@@ -367,7 +364,7 @@ int launch_wave(ish_ctx *ctx, Query &q, RecordSet &rs, uint32_t first, uint32_t 
   if (count == 0) return ISH_OK;
   int G, K;
   choose_shape(q.Q, ctx->force_G, ctx->force_K, &G, &K);
-  if (G * K < q.Q + 1) return fail(ctx, ISH_EOVERFLOW, "query of %d residues exceeds the wavefront engine", q.Q);
+  if (!G || G * K < q.Q + 1) return fail(ctx, ISH_EOVERFLOW, "no wavefront shape for a query of %d residues", q.Q);
   WaveLayout *L = nullptr;
   int rc = build_wave_layout(ctx, q, G, K, &L);
   if (rc) return rc;
@@ -475,7 +472,7 @@ int run_scoring(ish_ctx *ctx, Query &q, RecordSet &rs) {
   if (nonempty) {
     int G, K;
     choose_shape(q.Q, ctx->force_G, ctx->force_K, &G, &K);
-    Regime r = regime(q, G * K);
+    Regime r = regime(q, G ? G * K : q.Q + 64);
     if (!r.fast)
       return fail(ctx, ISH_EINVAL,
                   "parameters outside the exact-integer fast regime (gap_open must exceed gap_extend and scores "
@@ -612,8 +609,8 @@ int ish_gpu_set_option(ish_ctx *ctx, int option, int64_t value) {
     ctx->force_G = (int)value;
     return ISH_OK;
   case ISH_OPT_WAVE_K:
-    if (value != 0 && (value < 2 || value > WAVE_KMAX || (value & 1)))
-      return fail(ctx, ISH_EINVAL, "K must be 0 or even in 2..%d", WAVE_KMAX);
+    if (value != 0 && !wave_k_available((int)value))
+      return fail(ctx, ISH_EINVAL, "K must be 0, 1..32 or even up to %d", WAVE_KMAX);
     ctx->force_K = (int)value;
     return ISH_OK;
   default:
@@ -790,10 +787,15 @@ WaveFn wave_fn_a(int, int, int);
 WaveFn wave_fn_b(int, int, int);
 WaveFn wave_fn_c(int, int, int);
 WaveFn wave_fn_d(int, int, int);
+WaveFn wave_fn_e(int, int, int);
+WaveFn wave_fn_f(int, int, int);
 WaveFn wave_fn(int K, int mode, int pair) {
-  if (K <= 16) return wave_fn_a(K, mode, pair);
-  if (K <= 32) return wave_fn_b(K, mode, pair);
-  if (K <= 48) return wave_fn_c(K, mode, pair);
-  return wave_fn_d(K, mode, pair);
+  if (K < 1) return nullptr;
+  if (K <= 8) return wave_fn_a(K, mode, pair);
+  if (K <= 16) return wave_fn_b(K, mode, pair);
+  if (K <= 24) return wave_fn_c(K, mode, pair);
+  if (K <= 32) return wave_fn_d(K, mode, pair);
+  if (K <= 48) return wave_fn_e(K, mode, pair);
+  return wave_fn_f(K, mode, pair);
 }
 }  // namespace ish

@@ -5,18 +5,22 @@
 // record A and record B of the pair.  Thread t of the group owns K consecutive
 // query columns [t*K - d, (t+1)*K - d); the query is padded at the front with
 // d >= 1 columns whose profile and boundary values make them transparent (see
-// build_wave_profile), so the last query column is always the last register of
-// thread G-1.  Records flow through the group as a software pipeline: thread t
-// processes row i of the pair one step after thread t-1 did, receiving from it
-// H(i, first column - 1), F(i, first column) and the control word (record codes
-// of row i) through __shfl_up_sync.  G = 1 is "one thread per record pair with
-// packed 16-bit lanes" for short queries; G = 32 is a warp-wide anti-diagonal
-// wavefront for long queries.
+// build_wave_layout in ish_gpu.cu), so the last query column is always the
+// last register of thread G-1.  Rows flow through the group as a software
+// pipeline: thread t processes row i of the pair one step after thread t-1
+// did, receiving H(i, first column - 1) and F(i, first column) through
+// __shfl_up_sync.  G = 1 is "one thread per record pair with packed 16-bit
+// lanes" for short queries; G = 32 is a warp-wide anti-diagonal wavefront for
+// long queries.
 //
 // Per cell and record pair (two cells) the recurrence costs five DPX/SIMD
 // instructions:
-//   H = max(Hdiag + P, max(E, F));  v = H - open;  E = max(E - ext, v);  F = max(F - ext, v)
-// (local alignment floors v at 0, which keeps E, F and H non-negative).
+//   T = max(Hdiag + P, E);  u = T - open;  E = max(E - ext, u);  H = max(T, F);  F = max(F - ext, u)
+// (local alignment floors u at 0, which keeps E, F and H non-negative).  E
+// opens from T only, never from F: an F-then-E gap pair always has an
+// E-then-F twin of at least the same score, which this recurrence keeps, so H
+// is exactly the Gotoh H -- and the serial dependency along a row is the single
+// F instruction per cell.
 //
 // End coordinates follow the reference exactly:
 //   semi-global, target end free: first row where H(i, Q-1) strictly beats the
@@ -33,7 +37,7 @@
 namespace ish {
 
 template <int K, int MODE, bool PAIR>
-__global__ void __launch_bounds__(256) wave_kernel(const WaveParams p) {
+__global__ void __launch_bounds__(256, (K <= 32 ? 2 : 1)) wave_kernel(const WaveParams p) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const int tid = threadIdx.x;
   {
@@ -45,132 +49,92 @@ __global__ void __launch_bounds__(256) wave_kernel(const WaveParams p) {
   const int G = p.G;
   const int lane = tid & 31;
   const int t = lane & (G - 1);
-  const int group = tid / G;
-  uint32_t *slots = reinterpret_cast<uint32_t *>(smem_raw + ((p.prof_bytes + 15u) & ~15u)) + group * 32;
+  uint32_t *slots = reinterpret_cast<uint32_t *>(smem_raw + ((p.prof_bytes + 15u) & ~15u)) + (tid / G) * 32;
   __syncthreads();
 
   const unsigned FULL = 0xffffffffu;
   const uint32_t NOPEN = dup16(-p.open);
   const uint32_t NEXT = dup16(-p.ext);
   const uint32_t VFLOOR = (MODE == SW) ? 0u : dup16(-32768);
-  const uint32_t HLEFT = dup16(p.hleft);
-  const uint32_t FIN = dup16(p.fin);
   const bool te = (MODE == SG) && (p.ends & 8);
   const bool qe = (MODE == SG) && (p.ends & 2);
-  const int qlast_local = K - 1;  // column Q-1 is register K-1 of thread G-1
   const uint32_t npairs = (p.count + 1) >> 1;
-
-  // profile rows
   const uint16_t *prof16 = reinterpret_cast<const uint16_t *>(smem_raw);
   const uint32_t *prof32 = reinterpret_cast<const uint32_t *>(smem_raw);
+  const int col0 = t * K - p.d;  // query column of register 0
 
   uint32_t H[K], E[K];
 #pragma unroll
-  for (int j = 0; j < K; ++j) { H[j] = 0; E[j] = 0; }
-  uint32_t prevH = HLEFT;
-  uint32_t outH = 0, outF = 0, outC = CTL_IDLE;
-  int row = 0;
-  int lenA = 0, lenB = 0;
-  uint32_t origA = 0, origB = 0;
-  uint64_t steps = 0;
-
-  // tracking (see header comment)
-  int bestA = 0, bestB = 0;    // SG: running max of H(i, Q-1); SW: running max of this thread's cells
-  int rowA = -1, rowB = -1;    // first row of `best`, per lane
-  int mqA = 0, mqB = 0;        // SW: smallest column of `best` in that row
-  // last-row reduction messages
-  uint32_t oR0 = 0, oR1 = 0, oR2 = 0, oR3 = 0, iR0 = 0, iR1 = 0, iR2 = 0, iR3 = 0;
+  for (int j = 0; j < K; ++j) {
+    H[j] = 0;
+    E[j] = 0;
+  }
+  uint32_t prevH = 0, outH = 0, outF = 0, outC = CTL_IDLE;
+  int row = 0, lenA = 0, lenB = 0, lastA_row = -1, lastB_row = -1;
+  uint32_t pr = 0;
+  // this thread's record streams: 4 codes per 32-bit word, one word ahead
+  const uint8_t *pa = nullptr, *pb = nullptr;
+  uint32_t wA = 0, wB = 0, nA = 0, nB = 0;
+  // tracking
+  uint32_t best = 0;         // SG: lane-wise running max of H(i, Q-1); SW: of this thread's cells
+  int rowA = -1, rowB = -1;  // first row of the lane's maximum
+  int mqA = 0, mqB = 0;      // SW: smallest column of that maximum in that row
+  uint32_t oR0 = 0, oR1 = 0, oR2 = 0, oR3 = 0;  // last-row partials for thread t+1
   bool has_out = false;
-
-  // thread-0 feeder state
+  // thread 0 of the group grabs record pairs
   bool f_active = false, f_done = false;
-  int f_row = 0, f_rows = 0, f_lenA = 0, f_lenB = 0;
+  int f_row = 0, f_rows = 0;
   uint32_t f_seq = 31;
-  const uint8_t *f_pa = nullptr, *f_pb = nullptr;
-  uint4 f_curA = make_uint4(0, 0, 0, 0), f_nxtA = f_curA, f_curB = f_curA, f_nxtB = f_curA;
-  uint32_t f_wA = 0, f_wB = 0;
+  uint64_t steps = 0;
 
   while (true) {
     __syncwarp();
-    uint32_t msgH = __shfl_up_sync(FULL, outH, 1, G);
-    uint32_t msgF = __shfl_up_sync(FULL, outF, 1, G);
+    const uint32_t msgH = __shfl_up_sync(FULL, outH, 1, G);
+    const uint32_t msgF = __shfl_up_sync(FULL, outF, 1, G);
     uint32_t msgC = __shfl_up_sync(FULL, outC, 1, G);
-    if (__any_sync(FULL, has_out)) {
-      iR0 = __shfl_up_sync(FULL, oR0, 1, G);
-      iR1 = __shfl_up_sync(FULL, oR1, 1, G);
-      if (MODE == SW) {
-        iR2 = __shfl_up_sync(FULL, oR2, 1, G);
-        iR3 = __shfl_up_sync(FULL, oR3, 1, G);
-      }
-      has_out = false;
-    }
 
     if (t == 0) {
-      // ---- feeder: inject the next row of the current pair ----
       if (!f_active && !f_done) {
-        uint32_t pr = atomicAdd(p.counter, 1u);
-        if (pr < npairs) {
+        const uint32_t np = atomicAdd(p.counter, 1u);
+        if (np < npairs) {
           f_active = true;
           f_seq = (f_seq + 1) & 31;
-          slots[f_seq] = pr;
-          uint32_t sA = p.first + 2 * pr, sB = sA + 1;
-          f_lenA = (int)p.rec.len[sA];
-          f_lenB = (2 * pr + 1 < p.count) ? (int)p.rec.len[sB] : 0;
-          f_pa = p.rec.codes + p.rec.off[sA];
-          f_pb = f_lenB ? p.rec.codes + p.rec.off[sB] : f_pa;
-          f_rows = max(max(f_lenA, f_lenB), 1);
+          slots[f_seq] = np;
+          const uint32_t sA = p.first + 2 * np;
+          const int la = (int)p.rec.len[sA];
+          const int lb = (2 * np + 1 < p.count) ? (int)p.rec.len[sA + 1] : 0;
+          f_rows = max(max(la, lb), 1);
           f_row = 0;
-          f_nxtA = __ldg(reinterpret_cast<const uint4 *>(f_pa));
-          f_nxtB = f_lenB ? __ldg(reinterpret_cast<const uint4 *>(f_pb)) : make_uint4(0, 0, 0, 0);
         } else {
           f_done = true;
         }
       }
       if (f_active) {
-        const int r = f_row;
-        if ((r & 15) == 0) {
-          f_curA = f_nxtA;
-          f_curB = f_nxtB;
-          if (r + 16 < f_lenA) f_nxtA = __ldg(reinterpret_cast<const uint4 *>(f_pa + r + 16));
-          if (r + 16 < f_lenB) f_nxtB = __ldg(reinterpret_cast<const uint4 *>(f_pb + r + 16));
-        }
-        if ((r & 3) == 0) {
-          const int w = (r >> 2) & 3;
-          f_wA = w == 0 ? f_curA.x : w == 1 ? f_curA.y : w == 2 ? f_curA.z : f_curA.w;
-          f_wB = w == 0 ? f_curB.x : w == 1 ? f_curB.y : w == 2 ? f_curB.z : f_curB.w;
-        }
-        uint32_t cA = r < f_lenA ? (f_wA & 0xffu) : 0u;
-        uint32_t cB = r < f_lenB ? (f_wB & 0xffu) : 0u;
-        f_wA >>= 8;
-        f_wB >>= 8;
-        if (cA >= (uint32_t)p.alphabet || cB >= (uint32_t)p.alphabet) {
-          atomicOr(p.error, 1);
-          cA = 0;
-          cB = 0;
-        }
-        msgC = cA | (cB << 8) | (r == 0 ? CTL_NEW : 0u) | (f_seq << CTL_SEQ_SHIFT);
-        f_row = r + 1;
-        if (f_row >= f_rows) f_active = false;
+        msgC = (f_row == 0 ? CTL_NEW : 0u) | (f_seq << CTL_SEQ_SHIFT);
+        if (++f_row >= f_rows) f_active = false;
       } else {
         msgC = CTL_IDLE;
       }
-      msgH = HLEFT;
-      msgF = FIN;
     }
 
     const bool busy = !(msgC & CTL_IDLE);
     if (busy) {
       if (msgC & CTL_NEW) {
-        const uint32_t pr = slots[(msgC >> CTL_SEQ_SHIFT) & 31];
-        const uint32_t sA = p.first + 2 * pr, sB = sA + 1;
+        pr = slots[(msgC >> CTL_SEQ_SHIFT) & 31];
+        const uint32_t sA = p.first + 2 * pr;
         lenA = (int)p.rec.len[sA];
-        origA = p.rec.orig[sA];
+        pa = p.rec.codes + p.rec.off[sA];
         if (2 * pr + 1 < p.count) {
-          lenB = (int)p.rec.len[sB];
-          origB = p.rec.orig[sB];
+          lenB = (int)p.rec.len[sA + 1];
+          pb = p.rec.codes + p.rec.off[sA + 1];
         } else {
           lenB = 0;
+          pb = pa;
         }
+        lastA_row = lenA - 1;
+        lastB_row = lenB > 0 ? lenB - 1 : -2;
+        nA = __ldg(reinterpret_cast<const uint32_t *>(pa));
+        nB = lenB ? __ldg(reinterpret_cast<const uint32_t *>(pb)) : 0u;
         const int16_t *hi = p.hinit + t * K;
 #pragma unroll
         for (int j = 0; j < K; ++j) {
@@ -178,8 +142,8 @@ __global__ void __launch_bounds__(256) wave_kernel(const WaveParams p) {
           H[j] = dup16(h0);
           E[j] = (MODE == SW) ? 0u : dup16(h0 - p.open);
         }
-        prevH = (t == 0) ? HLEFT : dup16(p.hinit[t * K - 1]);
-        bestA = bestB = (MODE == SW) ? 0 : p.neg_limit;
+        prevH = (t == 0) ? dup16(p.hleft) : dup16(p.hinit[t * K - 1]);
+        best = (MODE == SW) ? 0u : dup16(p.neg_limit);
         rowA = rowB = -1;
         mqA = mqB = 0;
         row = 0;
@@ -187,8 +151,24 @@ __global__ void __launch_bounds__(256) wave_kernel(const WaveParams p) {
         ++row;
       }
 
-      // ---- profile of this row ----
-      const uint32_t cA = msgC & 0xffu, cB = (msgC >> 8) & 0xffu;
+      // ---- record codes of this row ----
+      if ((row & 3) == 0) {
+        wA = nA;
+        wB = nB;
+        if (row + 4 < lenA) nA = __ldg(reinterpret_cast<const uint32_t *>(pa + row + 4));
+        if (row + 4 < lenB) nB = __ldg(reinterpret_cast<const uint32_t *>(pb + row + 4));
+      }
+      uint32_t cA = row < lenA ? (wA & 0xffu) : 0u;
+      uint32_t cB = row < lenB ? (wB & 0xffu) : 0u;
+      wA >>= 8;
+      wB >>= 8;
+      if (cA >= (uint32_t)p.alphabet || cB >= (uint32_t)p.alphabet) {
+        atomicOr(p.error, 1);
+        cA = cA >= (uint32_t)p.alphabet ? 0u : cA;
+        cB = cB >= (uint32_t)p.alphabet ? 0u : cB;
+      }
+
+      // ---- profile words of this row ----
       uint32_t P[K];
       if (PAIR) {
         const uint4 *r4 = reinterpret_cast<const uint4 *>(prof32 + ((cA * p.alphabet + cB) * G + t) * p.kp);
@@ -217,50 +197,100 @@ __global__ void __launch_bounds__(256) wave_kernel(const WaveParams p) {
 
       // ---- the row ----
       uint32_t hdiag = prevH;
-      uint32_t F = msgF;
+      uint32_t F = (t == 0) ? dup16(p.fin) : msgF;
 #pragma unroll
       for (int j = 0; j < K; ++j) {
-        const uint32_t ef = __vmaxs2(E[j], F);
-        const uint32_t h = __viaddmax_s16x2(hdiag, P[j], ef);
+        const uint32_t T = __viaddmax_s16x2(hdiag, P[j], E[j]);
+        const uint32_t u = __viaddmax_s16x2(T, NOPEN, VFLOOR);
+        E[j] = __viaddmax_s16x2(E[j], NEXT, u);
         hdiag = H[j];
-        H[j] = h;
-        const uint32_t v = __viaddmax_s16x2(h, NOPEN, VFLOOR);
-        E[j] = __viaddmax_s16x2(E[j], NEXT, v);
-        F = __viaddmax_s16x2(F, NEXT, v);
+        H[j] = __vmaxs2(T, F);
+        F = __viaddmax_s16x2(F, NEXT, u);
       }
-      prevH = msgH;
+      prevH = (t == 0) ? dup16(p.hleft) : msgH;
       outH = H[K - 1];
       outF = F;
       outC = msgC;
 
-      const bool lastA = (row == lenA - 1), lastB = (row == lenB - 1);
-
-      if (MODE == SG) {
-        if (te) {
-          // strict improvement only: the FIRST row of the maximum wins
-          const int ha = lo16(H[qlast_local]), hb = hi16(H[qlast_local]);
-          if (ha > bestA) { bestA = ha; rowA = row; }
-          if (hb > bestB) { bestB = hb; rowB = row; }
+      if (MODE == SG && te) {
+        // running max of column Q-1 (register K-1 of thread G-1); a strict
+        // improvement records the row, so the FIRST row of the maximum wins
+        const uint32_t nb = __vmaxs2(best, H[K - 1]);
+        if (nb != best) {
+          if (lo16(nb) != lo16(best)) rowA = row;
+          if (hi16(nb) != hi16(best)) rowB = row;
+          best = nb;
         }
-        if (lastA || lastB) {
-          uint32_t mx = 0;
-          uint32_t mq = 0;
+      }
+      if (MODE == SW) {
+        uint32_t cm = H[0];
+#pragma unroll
+        for (int j = 1; j + 1 < K; j += 2) cm = __vimax3_s16x2(cm, H[j], H[j + 1]);
+        if ((K & 1) == 0 && K > 1) cm = __vmaxs2(cm, H[K - 1]);
+        const uint32_t nb = __vmaxs2(best, cm);
+        if (nb != best) {
+          const int ca = lo16(cm), cb = hi16(cm);
+          const bool upA = ca > lo16(best), upB = cb > hi16(best);
+          int qa = 0x7fff, qb = 0x7fff;
+#pragma unroll
+          for (int j = K - 1; j >= 0; --j) {
+            if (lo16(H[j]) == ca) qa = col0 + j;
+            if (hi16(H[j]) == cb) qb = col0 + j;
+          }
+          if (upA) {
+            rowA = row;
+            mqA = qa;
+          }
+          if (upB) {
+            rowB = row;
+            mqB = qb;
+          }
+          best = nb;
+        }
+      }
+    } else {
+      outC = CTL_IDLE;
+    }
+
+    // ---- last row of a record: fold partial results left to right ----
+    const bool lastA = busy && row == lastA_row, lastB = busy && row == lastB_row;
+    if (__any_sync(FULL, lastA || lastB || has_out)) {
+      const uint32_t iR0 = __shfl_up_sync(FULL, oR0, 1, G);
+      const uint32_t iR1 = __shfl_up_sync(FULL, oR1, 1, G);
+      uint32_t iR2 = 0, iR3 = 0;
+      if (MODE == SW) {
+        iR2 = __shfl_up_sync(FULL, oR2, 1, G);
+        iR3 = __shfl_up_sync(FULL, oR3, 1, G);
+      }
+      has_out = false;
+      if (lastA || lastB) {
+        if (MODE == SG) {
+          uint32_t mx = 0, mq = 0;
           if (qe) {
-            // smallest column of the row maximum, this thread's columns
             int bA = -32768, bB = -32768, qA = 0x7fff, qB = 0x7fff;
 #pragma unroll
             for (int j = 0; j < K; ++j) {
-              const int q = t * K + j - p.d;
-              if (q >= 0) {
+              if (col0 + j >= 0) {
                 const int a = lo16(H[j]), b = hi16(H[j]);
-                if (a > bA) { bA = a; qA = q; }
-                if (b > bB) { bB = b; qB = q; }
+                if (a > bA) {
+                  bA = a;
+                  qA = col0 + j;
+                }
+                if (b > bB) {
+                  bB = b;
+                  qB = col0 + j;
+                }
               }
             }
-            if (t > 0) {  // fold in columns to the left (thread t-1, previous step)
-              const int ia = lo16(iR0), ib = hi16(iR0);
-              if (!(bA > ia)) { bA = ia; qA = (int)(iR1 & 0xffffu); }
-              if (!(bB > ib)) { bB = ib; qB = (int)(iR1 >> 16); }
+            if (t > 0) {  // columns to the left win ties
+              if (!(bA > lo16(iR0))) {
+                bA = lo16(iR0);
+                qA = (int)(iR1 & 0xffffu);
+              }
+              if (!(bB > hi16(iR0))) {
+                bB = hi16(iR0);
+                qB = (int)(iR1 >> 16);
+              }
             }
             mx = (uint32_t)(bA & 0xffff) | ((uint32_t)bB << 16);
             mq = (uint32_t)qA | ((uint32_t)qB << 16);
@@ -273,25 +303,26 @@ __global__ void __launch_bounds__(256) wave_kernel(const WaveParams p) {
           if (t == G - 1) {
 #pragma unroll
             for (int x = 0; x < 2; ++x) {
-              const bool fin = x == 0 ? lastA : lastB;
-              if (!fin) continue;
-              const uint32_t orig = x == 0 ? origA : origB;
+              if (!(x == 0 ? lastA : lastB)) continue;
+              const uint32_t orig = p.rec.orig[p.first + 2 * pr + x];
               const int T = x == 0 ? lenA : lenB;
-              const int hl = x == 0 ? lo16(H[qlast_local]) : hi16(H[qlast_local]);
-              int score, er, eq;
+              int score, er, eq = p.Q - 1;
               if (!te && !qe) {
-                score = hl; er = T - 1; eq = p.Q - 1;
+                score = x == 0 ? lo16(H[K - 1]) : hi16(H[K - 1]);
+                er = T - 1;
               } else {
-                int s0 = x == 0 ? bestA : bestB;
-                int r0 = x == 0 ? rowA : rowB;
-                score = te ? s0 : p.neg_limit;
-                er = te ? r0 : (x == 0 ? rowA : rowB);
-                eq = p.Q - 1;
+                score = te ? (x == 0 ? lo16(best) : hi16(best)) : p.neg_limit;
+                er = x == 0 ? rowA : rowB;
                 if (qe) {
                   const int s1 = x == 0 ? lo16(mx) : hi16(mx);
                   const int t1 = x == 0 ? (int)(mq & 0xffffu) : (int)(mq >> 16);
-                  if (s1 > score) { score = s1; er = T - 1; eq = t1; }
-                  else if (s1 == score && er == T - 1 && t1 < eq) { eq = t1; }
+                  if (s1 > score) {
+                    score = s1;
+                    er = T - 1;
+                    eq = t1;
+                  } else if (s1 == score && er == T - 1 && t1 < eq) {
+                    eq = t1;
+                  }
                 }
               }
               if (p.out.score) p.out.score[orig] = score;
@@ -300,34 +331,21 @@ __global__ void __launch_bounds__(256) wave_kernel(const WaveParams p) {
               if (p.out.hit) p.out.hit[orig] = decide(SG, score, eq, er, p.dec);
             }
           }
-        }
-      } else {
-        // ---- local: this thread's first strict maximum ----
-        uint32_t cm = H[0];
-#pragma unroll
-        for (int j = 1; j + 1 < K; j += 2) cm = __vimax3_s16x2(cm, H[j], H[j + 1]);
-        if ((K & 1) == 0 && K > 1) cm = __vmaxs2(cm, H[K - 1]);
-        const int ca = lo16(cm), cb = hi16(cm);
-        const bool upA = ca > bestA, upB = cb > bestB;
-        if (upA || upB) {
-          int qa = 0x7fff, qb = 0x7fff;
-#pragma unroll
-          for (int j = K - 1; j >= 0; --j) {
-            const int q = t * K + j - p.d;
-            if (lo16(H[j]) == ca) qa = q;
-            if (hi16(H[j]) == cb) qb = q;
-          }
-          if (upA) { bestA = ca; rowA = row; mqA = qa; }
-          if (upB) { bestB = cb; rowB = row; mqB = qb; }
-        }
-        if (lastA || lastB) {
-          int bA = bestA, bB = bestB, rA = rowA, rB = rowB, qA = mqA, qB = mqB;
+        } else {
+          int bA = lo16(best), bB = hi16(best), rA = rowA, rB = rowB, qA = mqA, qB = mqB;
           if (t > 0) {
-            const int ia = lo16(iR0), ib = hi16(iR0);
-            const int ira = (int)iR2, irb = (int)iR3;
+            const int ia = lo16(iR0), ib = hi16(iR0), ira = (int)iR2, irb = (int)iR3;
             const int iqa = (int)(int16_t)(iR1 & 0xffffu), iqb = (int)(int16_t)(iR1 >> 16);
-            if (ia > bA || (ia == bA && (ira < rA || (ira == rA && iqa < qA)))) { bA = ia; rA = ira; qA = iqa; }
-            if (ib > bB || (ib == bB && (irb < rB || (irb == rB && iqb < qB)))) { bB = ib; rB = irb; qB = iqb; }
+            if (ia > bA || (ia == bA && (ira < rA || (ira == rA && iqa < qA)))) {
+              bA = ia;
+              rA = ira;
+              qA = iqa;
+            }
+            if (ib > bB || (ib == bB && (irb < rB || (irb == rB && iqb < qB)))) {
+              bB = ib;
+              rB = irb;
+              qB = iqb;
+            }
           }
           if (t < G - 1) {
             oR0 = (uint32_t)(bA & 0xffff) | ((uint32_t)bB << 16);
@@ -338,13 +356,13 @@ __global__ void __launch_bounds__(256) wave_kernel(const WaveParams p) {
           } else {
 #pragma unroll
             for (int x = 0; x < 2; ++x) {
-              const bool fin = x == 0 ? lastA : lastB;
-              if (!fin) continue;
-              const uint32_t orig = x == 0 ? origA : origB;
-              int score = x == 0 ? bA : bB;
-              int er = x == 0 ? rA : rB;
-              int eq = x == 0 ? qA : qB;
-              if (score == 0) { er = -1; eq = 0; }
+              if (!(x == 0 ? lastA : lastB)) continue;
+              const uint32_t orig = p.rec.orig[p.first + 2 * pr + x];
+              int score = x == 0 ? bA : bB, er = x == 0 ? rA : rB, eq = x == 0 ? qA : qB;
+              if (score == 0) {
+                er = -1;
+                eq = 0;
+              }
               if (p.out.score) p.out.score[orig] = score;
               if (p.out.qend) p.out.qend[orig] = eq;
               if (p.out.tend) p.out.tend[orig] = er;
@@ -353,12 +371,11 @@ __global__ void __launch_bounds__(256) wave_kernel(const WaveParams p) {
           }
         }
       }
-    } else {
-      outC = CTL_IDLE;
     }
-    // Every row the feeder injects reaches thread G-1 within G-1 steps, so the
-    // group is done once the feeder is and no row is in flight.  The step
-    // budget (all rows of the range plus the pipeline depth) is a hard stop.
+
+    // Every row thread 0 starts reaches thread G-1 within G-1 steps, so the
+    // group is done once thread 0 is and no row is in flight.  The step budget
+    // (all rows of the range plus the pipeline depth) is a hard stop.
     const bool more = busy || (t == 0 && !f_done);
     if (!__any_sync(FULL, more)) break;
     if (++steps > p.max_steps) {

@@ -1,4 +1,4 @@
-// wave_b.cu -- wavefront kernel instantiations for K = 18..32
+// wave_b.cu -- wavefront kernel instantiations for K = 9, 10, 11, 12, 13, 14, 15, 16
 // (split across files so the build compiles them in parallel).
 #include "kernels.cuh"
 #include "wave.cuh"
@@ -7,30 +7,30 @@ namespace ish {
 
 WaveFn wave_fn_b(int K, int mode, int pair) {
   switch (K) {
-    case 18:
-      return mode == SG ? (pair ? (WaveFn)wave_kernel<18, SG, true> : (WaveFn)wave_kernel<18, SG, false>)
-                        : (pair ? (WaveFn)wave_kernel<18, SW, true> : (WaveFn)wave_kernel<18, SW, false>);
-    case 20:
-      return mode == SG ? (pair ? (WaveFn)wave_kernel<20, SG, true> : (WaveFn)wave_kernel<20, SG, false>)
-                        : (pair ? (WaveFn)wave_kernel<20, SW, true> : (WaveFn)wave_kernel<20, SW, false>);
-    case 22:
-      return mode == SG ? (pair ? (WaveFn)wave_kernel<22, SG, true> : (WaveFn)wave_kernel<22, SG, false>)
-                        : (pair ? (WaveFn)wave_kernel<22, SW, true> : (WaveFn)wave_kernel<22, SW, false>);
-    case 24:
-      return mode == SG ? (pair ? (WaveFn)wave_kernel<24, SG, true> : (WaveFn)wave_kernel<24, SG, false>)
-                        : (pair ? (WaveFn)wave_kernel<24, SW, true> : (WaveFn)wave_kernel<24, SW, false>);
-    case 26:
-      return mode == SG ? (pair ? (WaveFn)wave_kernel<26, SG, true> : (WaveFn)wave_kernel<26, SG, false>)
-                        : (pair ? (WaveFn)wave_kernel<26, SW, true> : (WaveFn)wave_kernel<26, SW, false>);
-    case 28:
-      return mode == SG ? (pair ? (WaveFn)wave_kernel<28, SG, true> : (WaveFn)wave_kernel<28, SG, false>)
-                        : (pair ? (WaveFn)wave_kernel<28, SW, true> : (WaveFn)wave_kernel<28, SW, false>);
-    case 30:
-      return mode == SG ? (pair ? (WaveFn)wave_kernel<30, SG, true> : (WaveFn)wave_kernel<30, SG, false>)
-                        : (pair ? (WaveFn)wave_kernel<30, SW, true> : (WaveFn)wave_kernel<30, SW, false>);
-    case 32:
-      return mode == SG ? (pair ? (WaveFn)wave_kernel<32, SG, true> : (WaveFn)wave_kernel<32, SG, false>)
-                        : (pair ? (WaveFn)wave_kernel<32, SW, true> : (WaveFn)wave_kernel<32, SW, false>);
+    case 9:
+      return mode == SG ? (pair ? (WaveFn)wave_kernel<9, SG, true> : (WaveFn)wave_kernel<9, SG, false>)
+                        : (pair ? (WaveFn)wave_kernel<9, SW, true> : (WaveFn)wave_kernel<9, SW, false>);
+    case 10:
+      return mode == SG ? (pair ? (WaveFn)wave_kernel<10, SG, true> : (WaveFn)wave_kernel<10, SG, false>)
+                        : (pair ? (WaveFn)wave_kernel<10, SW, true> : (WaveFn)wave_kernel<10, SW, false>);
+    case 11:
+      return mode == SG ? (pair ? (WaveFn)wave_kernel<11, SG, true> : (WaveFn)wave_kernel<11, SG, false>)
+                        : (pair ? (WaveFn)wave_kernel<11, SW, true> : (WaveFn)wave_kernel<11, SW, false>);
+    case 12:
+      return mode == SG ? (pair ? (WaveFn)wave_kernel<12, SG, true> : (WaveFn)wave_kernel<12, SG, false>)
+                        : (pair ? (WaveFn)wave_kernel<12, SW, true> : (WaveFn)wave_kernel<12, SW, false>);
+    case 13:
+      return mode == SG ? (pair ? (WaveFn)wave_kernel<13, SG, true> : (WaveFn)wave_kernel<13, SG, false>)
+                        : (pair ? (WaveFn)wave_kernel<13, SW, true> : (WaveFn)wave_kernel<13, SW, false>);
+    case 14:
+      return mode == SG ? (pair ? (WaveFn)wave_kernel<14, SG, true> : (WaveFn)wave_kernel<14, SG, false>)
+                        : (pair ? (WaveFn)wave_kernel<14, SW, true> : (WaveFn)wave_kernel<14, SW, false>);
+    case 15:
+      return mode == SG ? (pair ? (WaveFn)wave_kernel<15, SG, true> : (WaveFn)wave_kernel<15, SG, false>)
+                        : (pair ? (WaveFn)wave_kernel<15, SW, true> : (WaveFn)wave_kernel<15, SW, false>);
+    case 16:
+      return mode == SG ? (pair ? (WaveFn)wave_kernel<16, SG, true> : (WaveFn)wave_kernel<16, SG, false>)
+                        : (pair ? (WaveFn)wave_kernel<16, SW, true> : (WaveFn)wave_kernel<16, SW, false>);
     default:
       return nullptr;
   }

@@ -1,4 +1,4 @@
-// wave_c.cu -- wavefront kernel instantiations for K = 34..48
+// wave_c.cu -- wavefront kernel instantiations for K = 17, 18, 19, 20, 21, 22, 23, 24
 // (split across files so the build compiles them in parallel).
 #include "kernels.cuh"
 #include "wave.cuh"
@@ -7,30 +7,30 @@ namespace ish {
 
 WaveFn wave_fn_c(int K, int mode, int pair) {
   switch (K) {
-    case 34:
-      return mode == SG ? (pair ? (WaveFn)wave_kernel<34, SG, true> : (WaveFn)wave_kernel<34, SG, false>)
-                        : (pair ? (WaveFn)wave_kernel<34, SW, true> : (WaveFn)wave_kernel<34, SW, false>);
-    case 36:
-      return mode == SG ? (pair ? (WaveFn)wave_kernel<36, SG, true> : (WaveFn)wave_kernel<36, SG, false>)
-                        : (pair ? (WaveFn)wave_kernel<36, SW, true> : (WaveFn)wave_kernel<36, SW, false>);
-    case 38:
-      return mode == SG ? (pair ? (WaveFn)wave_kernel<38, SG, true> : (WaveFn)wave_kernel<38, SG, false>)
-                        : (pair ? (WaveFn)wave_kernel<38, SW, true> : (WaveFn)wave_kernel<38, SW, false>);
-    case 40:
-      return mode == SG ? (pair ? (WaveFn)wave_kernel<40, SG, true> : (WaveFn)wave_kernel<40, SG, false>)
-                        : (pair ? (WaveFn)wave_kernel<40, SW, true> : (WaveFn)wave_kernel<40, SW, false>);
-    case 42:
-      return mode == SG ? (pair ? (WaveFn)wave_kernel<42, SG, true> : (WaveFn)wave_kernel<42, SG, false>)
-                        : (pair ? (WaveFn)wave_kernel<42, SW, true> : (WaveFn)wave_kernel<42, SW, false>);
-    case 44:
-      return mode == SG ? (pair ? (WaveFn)wave_kernel<44, SG, true> : (WaveFn)wave_kernel<44, SG, false>)
-                        : (pair ? (WaveFn)wave_kernel<44, SW, true> : (WaveFn)wave_kernel<44, SW, false>);
-    case 46:
-      return mode == SG ? (pair ? (WaveFn)wave_kernel<46, SG, true> : (WaveFn)wave_kernel<46, SG, false>)
-                        : (pair ? (WaveFn)wave_kernel<46, SW, true> : (WaveFn)wave_kernel<46, SW, false>);
-    case 48:
-      return mode == SG ? (pair ? (WaveFn)wave_kernel<48, SG, true> : (WaveFn)wave_kernel<48, SG, false>)
-                        : (pair ? (WaveFn)wave_kernel<48, SW, true> : (WaveFn)wave_kernel<48, SW, false>);
+    case 17:
+      return mode == SG ? (pair ? (WaveFn)wave_kernel<17, SG, true> : (WaveFn)wave_kernel<17, SG, false>)
+                        : (pair ? (WaveFn)wave_kernel<17, SW, true> : (WaveFn)wave_kernel<17, SW, false>);
+    case 18:
+      return mode == SG ? (pair ? (WaveFn)wave_kernel<18, SG, true> : (WaveFn)wave_kernel<18, SG, false>)
+                        : (pair ? (WaveFn)wave_kernel<18, SW, true> : (WaveFn)wave_kernel<18, SW, false>);
+    case 19:
+      return mode == SG ? (pair ? (WaveFn)wave_kernel<19, SG, true> : (WaveFn)wave_kernel<19, SG, false>)
+                        : (pair ? (WaveFn)wave_kernel<19, SW, true> : (WaveFn)wave_kernel<19, SW, false>);
+    case 20:
+      return mode == SG ? (pair ? (WaveFn)wave_kernel<20, SG, true> : (WaveFn)wave_kernel<20, SG, false>)
+                        : (pair ? (WaveFn)wave_kernel<20, SW, true> : (WaveFn)wave_kernel<20, SW, false>);
+    case 21:
+      return mode == SG ? (pair ? (WaveFn)wave_kernel<21, SG, true> : (WaveFn)wave_kernel<21, SG, false>)
+                        : (pair ? (WaveFn)wave_kernel<21, SW, true> : (WaveFn)wave_kernel<21, SW, false>);
+    case 22:
+      return mode == SG ? (pair ? (WaveFn)wave_kernel<22, SG, true> : (WaveFn)wave_kernel<22, SG, false>)
+                        : (pair ? (WaveFn)wave_kernel<22, SW, true> : (WaveFn)wave_kernel<22, SW, false>);
+    case 23:
+      return mode == SG ? (pair ? (WaveFn)wave_kernel<23, SG, true> : (WaveFn)wave_kernel<23, SG, false>)
+                        : (pair ? (WaveFn)wave_kernel<23, SW, true> : (WaveFn)wave_kernel<23, SW, false>);
+    case 24:
+      return mode == SG ? (pair ? (WaveFn)wave_kernel<24, SG, true> : (WaveFn)wave_kernel<24, SG, false>)
+                        : (pair ? (WaveFn)wave_kernel<24, SW, true> : (WaveFn)wave_kernel<24, SW, false>);
     default:
       return nullptr;
   }

@@ -1,4 +1,4 @@
-// wave_d.cu -- wavefront kernel instantiations for K = 50..64
+// wave_d.cu -- wavefront kernel instantiations for K = 25, 26, 27, 28, 29, 30, 31, 32
 // (split across files so the build compiles them in parallel).
 #include "kernels.cuh"
 #include "wave.cuh"
@@ -7,30 +7,30 @@ namespace ish {
 
 WaveFn wave_fn_d(int K, int mode, int pair) {
   switch (K) {
-    case 50:
-      return mode == SG ? (pair ? (WaveFn)wave_kernel<50, SG, true> : (WaveFn)wave_kernel<50, SG, false>)
-                        : (pair ? (WaveFn)wave_kernel<50, SW, true> : (WaveFn)wave_kernel<50, SW, false>);
-    case 52:
-      return mode == SG ? (pair ? (WaveFn)wave_kernel<52, SG, true> : (WaveFn)wave_kernel<52, SG, false>)
-                        : (pair ? (WaveFn)wave_kernel<52, SW, true> : (WaveFn)wave_kernel<52, SW, false>);
-    case 54:
-      return mode == SG ? (pair ? (WaveFn)wave_kernel<54, SG, true> : (WaveFn)wave_kernel<54, SG, false>)
-                        : (pair ? (WaveFn)wave_kernel<54, SW, true> : (WaveFn)wave_kernel<54, SW, false>);
-    case 56:
-      return mode == SG ? (pair ? (WaveFn)wave_kernel<56, SG, true> : (WaveFn)wave_kernel<56, SG, false>)
-                        : (pair ? (WaveFn)wave_kernel<56, SW, true> : (WaveFn)wave_kernel<56, SW, false>);
-    case 58:
-      return mode == SG ? (pair ? (WaveFn)wave_kernel<58, SG, true> : (WaveFn)wave_kernel<58, SG, false>)
-                        : (pair ? (WaveFn)wave_kernel<58, SW, true> : (WaveFn)wave_kernel<58, SW, false>);
-    case 60:
-      return mode == SG ? (pair ? (WaveFn)wave_kernel<60, SG, true> : (WaveFn)wave_kernel<60, SG, false>)
-                        : (pair ? (WaveFn)wave_kernel<60, SW, true> : (WaveFn)wave_kernel<60, SW, false>);
-    case 62:
-      return mode == SG ? (pair ? (WaveFn)wave_kernel<62, SG, true> : (WaveFn)wave_kernel<62, SG, false>)
-                        : (pair ? (WaveFn)wave_kernel<62, SW, true> : (WaveFn)wave_kernel<62, SW, false>);
-    case 64:
-      return mode == SG ? (pair ? (WaveFn)wave_kernel<64, SG, true> : (WaveFn)wave_kernel<64, SG, false>)
-                        : (pair ? (WaveFn)wave_kernel<64, SW, true> : (WaveFn)wave_kernel<64, SW, false>);
+    case 25:
+      return mode == SG ? (pair ? (WaveFn)wave_kernel<25, SG, true> : (WaveFn)wave_kernel<25, SG, false>)
+                        : (pair ? (WaveFn)wave_kernel<25, SW, true> : (WaveFn)wave_kernel<25, SW, false>);
+    case 26:
+      return mode == SG ? (pair ? (WaveFn)wave_kernel<26, SG, true> : (WaveFn)wave_kernel<26, SG, false>)
+                        : (pair ? (WaveFn)wave_kernel<26, SW, true> : (WaveFn)wave_kernel<26, SW, false>);
+    case 27:
+      return mode == SG ? (pair ? (WaveFn)wave_kernel<27, SG, true> : (WaveFn)wave_kernel<27, SG, false>)
+                        : (pair ? (WaveFn)wave_kernel<27, SW, true> : (WaveFn)wave_kernel<27, SW, false>);
+    case 28:
+      return mode == SG ? (pair ? (WaveFn)wave_kernel<28, SG, true> : (WaveFn)wave_kernel<28, SG, false>)
+                        : (pair ? (WaveFn)wave_kernel<28, SW, true> : (WaveFn)wave_kernel<28, SW, false>);
+    case 29:
+      return mode == SG ? (pair ? (WaveFn)wave_kernel<29, SG, true> : (WaveFn)wave_kernel<29, SG, false>)
+                        : (pair ? (WaveFn)wave_kernel<29, SW, true> : (WaveFn)wave_kernel<29, SW, false>);
+    case 30:
+      return mode == SG ? (pair ? (WaveFn)wave_kernel<30, SG, true> : (WaveFn)wave_kernel<30, SG, false>)
+                        : (pair ? (WaveFn)wave_kernel<30, SW, true> : (WaveFn)wave_kernel<30, SW, false>);
+    case 31:
+      return mode == SG ? (pair ? (WaveFn)wave_kernel<31, SG, true> : (WaveFn)wave_kernel<31, SG, false>)
+                        : (pair ? (WaveFn)wave_kernel<31, SW, true> : (WaveFn)wave_kernel<31, SW, false>);
+    case 32:
+      return mode == SG ? (pair ? (WaveFn)wave_kernel<32, SG, true> : (WaveFn)wave_kernel<32, SG, false>)
+                        : (pair ? (WaveFn)wave_kernel<32, SW, true> : (WaveFn)wave_kernel<32, SW, false>);
     default:
       return nullptr;
   }

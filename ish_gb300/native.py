@@ -10,7 +10,6 @@ import os
 
 import numpy as np
 
-from . import build as _build
 
 OK = 0
 EINVAL, ENOMEM, EOVERFLOW, ENODEV, EDEVICE, EAGAIN, ETIMEDOUT = -22, -12, -75, -19, -5, -11, -110
@@ -43,6 +42,8 @@ u64p = C.POINTER(C.c_uint64)
 
 
 def lib_path() -> str:
+    from . import build as _build
+
     return _build.LIB
 
 
@@ -51,6 +52,8 @@ def load(build_if_missing: bool = False):
     global _lib
     if _lib is not None:
         return _lib
+    from . import build as _build
+
     path = _build.LIB
     if not os.path.exists(path):
         if not build_if_missing:
