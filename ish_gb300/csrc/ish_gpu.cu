@@ -187,7 +187,7 @@ void choose_shape(int Q, int force_G, int force_K, int *G, int *K) {
 }
 
 int build_wave_layout(ish_ctx *ctx, Query &q, int G, int K, WaveLayout **out) {
-  const int pair_ok = q.alphabet * q.alphabet * G * ((K + 3) & ~3) * 4 <= 64 * 1024;
+  const int pair_ok = q.alphabet * q.alphabet * G * (((K + 3) & ~3) + 4) * 4 <= 64 * 1024;
   const long key = ((long)G << 20) | ((long)K << 8) | pair_ok;
   auto it = q.layouts.find(key);
   if (it != q.layouts.end()) {
@@ -207,8 +207,12 @@ int build_wave_layout(ish_ctx *ctx, Query &q, int G, int K, WaveLayout **out) {
     return q.M[(size_t)c * A + q.q[col]];
   };
   std::vector<uint8_t> host;
+  // Row strides are an odd number of 16-byte units: the eight threads of a
+  // quarter-warp read consecutive rows with 16-byte loads, and an odd stride
+  // spreads them over all 32 banks.
   if (L.pair) {
     L.kp = (K + 3) & ~3;
+    if (((L.kp / 4) & 1) == 0) L.kp += 4;
     std::vector<uint32_t> w((size_t)A * A * G * L.kp, 0u);
     for (int a = 0; a < A; ++a)
       for (int b = 0; b < A; ++b)
@@ -222,6 +226,7 @@ int build_wave_layout(ish_ctx *ctx, Query &q, int G, int K, WaveLayout **out) {
     memcpy(host.data(), w.data(), host.size());
   } else {
     L.kp = (K + 7) & ~7;
+    if (((L.kp / 8) & 1) == 0) L.kp += 8;
     std::vector<int16_t> w((size_t)A * G * L.kp, 0);
     for (int a = 0; a < A; ++a)
       for (int t = 0; t < G; ++t)
