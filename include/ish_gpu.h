@@ -129,6 +129,32 @@ ISH_API int ish_gpu_score_set(ish_ctx *ctx, int32_t query_id, int32_t set_id, in
                       int32_t *query_end, int32_t *target_end, uint8_t *hit, uint32_t *hit_idx,
                       uint32_t *n_hits);
 
+/* Score records that are already in device memory, into device outputs,
+ * without allocating anything.  No counterpart in the reference: this serves
+ * callers that cannot allocate device memory when they score (device memory
+ * owned by another allocator or arena, hosts that forbid cudaMalloc/cudaFree
+ * from worker threads, an exhausted device-memory budget).
+ *   d_records / records_bytes: device bytes of the encoded records;
+ *   d_offsets: device uint64[n+1], record i = d_records[d_offsets[i] .. d_offsets[i+1]);
+ *   enc_query, matrix: HOST arrays, as for ish_gpu_set_query;
+ *   d_score, d_query_end, d_target_end, d_hit: device outputs (any may be NULL),
+ *       same values as ish_gpu_score, in record order;
+ *   stream: cudaStream_t to run on (NULL = the legacy default stream);
+ *   err: optional buffer for a message (err_len bytes).
+ * Working memory is a fixed 32 MiB __device__ array inside the library that
+ * every GPU loading the library holds until exit; a query needing more
+ * (2*alphabet*qlen bytes of profile plus 1 KiB per query column) is rejected
+ * with ISH_EOVERFLOW.  All calls share that array: calls that overlap on the
+ * GPU race and must be serialised by the caller.  The first call on a device
+ * (with that device current) resolves the array's address; make it before
+ * any stream capture.  Blocks until the work on `stream` is done. */
+ISH_API int ish_gpu_score_noalloc(const uint8_t *d_records, uint64_t records_bytes, const uint64_t *d_offsets,
+                                  uint32_t n, const uint8_t *enc_query, uint32_t qlen, const int8_t *matrix,
+                                  uint32_t alphabet, int algo, uint32_t gap_open, uint32_t gap_ext,
+                                  uint32_t ends_free, int32_t max_score, float threshold, int32_t *d_score,
+                                  int32_t *d_query_end, int32_t *d_target_end, uint8_t *d_hit, void *stream,
+                                  char *err, size_t err_len);
+
 /* Device-side timing of the last scoring call on this context: milliseconds
  * from the first scoring kernel to the end of the hit compaction (CUDA events
  * on the engine's stream; excludes host<->device copies). */

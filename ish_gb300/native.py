@@ -23,6 +23,7 @@ EXPORTS = (
     "ish_gpu_abi_version", "ish_gpu_open", "ish_gpu_close", "ish_gpu_last_error", "ish_gpu_set_option",
     "ish_gpu_set_query", "ish_gpu_free_query", "ish_gpu_score", "ish_gpu_records_load", "ish_gpu_records_free",
     "ish_gpu_records_info", "ish_gpu_score_set", "ish_gpu_last_kernel_ms", "ish_gpu_calibrate",
+    "ish_gpu_score_noalloc",
 )
 
 
@@ -78,6 +79,9 @@ def load(build_if_missing: bool = False):
     L.ish_gpu_score_set.argtypes = [vp, C.c_int32, C.c_int32, i32p, i32p, i32p, u8p, u32p, u32p]
     L.ish_gpu_last_kernel_ms.argtypes = [vp, C.POINTER(C.c_double)]
     L.ish_gpu_calibrate.argtypes = [vp, C.POINTER(C.c_double)]
+    L.ish_gpu_score_noalloc.argtypes = [vp, C.c_uint64, vp, C.c_uint32, u8p, C.c_uint32, i8p, C.c_uint32, C.c_int,
+                                        C.c_uint32, C.c_uint32, C.c_uint32, C.c_int32, C.c_float, vp, vp, vp, vp,
+                                        vp, C.c_char_p, C.c_size_t]
     for name in EXPORTS:
         if name not in ("ish_gpu_close", "ish_gpu_last_error"):
             getattr(L, name).restype = C.c_int
