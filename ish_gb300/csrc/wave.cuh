@@ -204,7 +204,7 @@ __global__ void __launch_bounds__(256, (K <= 32 ? 2 : 1)) wave_kernel(const Wave
         const uint32_t u = __viaddmax_s16x2(T, NOPEN, VFLOOR);
         E[j] = __viaddmax_s16x2(E[j], NEXT, u);
         hdiag = H[j];
-        H[j] = __vmaxs2(T, F);
+        H[j] = __viaddmax_s16x2(T, 0u, F);  // DPX max (the legacy __vmaxs2 is emulated)
         F = __viaddmax_s16x2(F, NEXT, u);
       }
       prevH = (t == 0) ? dup16(p.hleft) : msgH;
@@ -215,7 +215,7 @@ __global__ void __launch_bounds__(256, (K <= 32 ? 2 : 1)) wave_kernel(const Wave
       if (MODE == SG && te) {
         // running max of column Q-1 (register K-1 of thread G-1); a strict
         // improvement records the row, so the FIRST row of the maximum wins
-        const uint32_t nb = __vmaxs2(best, H[K - 1]);
+        const uint32_t nb = __viaddmax_s16x2(best, 0u, H[K - 1]);
         if (nb != best) {
           if (lo16(nb) != lo16(best)) rowA = row;
           if (hi16(nb) != hi16(best)) rowB = row;
@@ -226,8 +226,8 @@ __global__ void __launch_bounds__(256, (K <= 32 ? 2 : 1)) wave_kernel(const Wave
         uint32_t cm = H[0];
 #pragma unroll
         for (int j = 1; j + 1 < K; j += 2) cm = __vimax3_s16x2(cm, H[j], H[j + 1]);
-        if ((K & 1) == 0 && K > 1) cm = __vmaxs2(cm, H[K - 1]);
-        const uint32_t nb = __vmaxs2(best, cm);
+        if ((K & 1) == 0 && K > 1) cm = __viaddmax_s16x2(cm, 0u, H[K - 1]);
+        const uint32_t nb = __viaddmax_s16x2(best, 0u, cm);
         if (nb != best) {
           const int ca = lo16(cm), cb = hi16(cm);
           const bool upA = ca > lo16(best), upB = cb > hi16(best);
