@@ -70,6 +70,7 @@ struct RecordSet {
   DevBuf codes, off_s, len_s, orig_s;
   std::vector<uint32_t> hist;  // length-bucket histogram (host copy)
   uint32_t n_empty = 0;
+  uint32_t max_code = 0;       // largest record code in the set
 };
 
 }  // namespace
@@ -88,7 +89,7 @@ struct ish_ctx {
   std::map<int32_t, RecordSet> sets;
   int32_t next_set = 1;
   // scratch
-  DevBuf raw, off_in, len_tmp, slot_tmp, poff_tmp, hist, scan_tmp;
+  DevBuf raw, off_in, len_tmp, slot_tmp, poff_tmp, hist, scan_tmp, max_code;
   DevBuf counter, error, out_score, out_qend, out_tend, out_hit, hit_idx, block_counts, nhits;
   DevBuf plain_scratch;
   float last_ms = 0.f;
@@ -327,9 +328,12 @@ int load_records(ish_ctx *ctx, const uint8_t *records, const uint64_t *offsets, 
   const uint64_t packed = bytes + 16ull * n + 16;
   CU(rs.codes.ensure(packed));
   const uint32_t pb = std::min<uint32_t>(ceil_div((uint64_t)n * 32, 256), (uint32_t)ctx->num_sms * 32);
+  CU(ctx->max_code.ensure(16));
+  CU(cudaMemsetAsync(ctx->max_code.p, 0, 4, s));
   k_pack<<<pb, 256, 0, s>>>(ctx->raw.as<uint8_t>(), bytes, ctx->off_in.as<uint64_t>(), ctx->poff_tmp.as<uint64_t>(), n,
-                            rs.codes.as<uint8_t>());
+                            rs.codes.as<uint8_t>(), ctx->max_code.as<uint32_t>());
   CU(cudaGetLastError());
+  CU(cudaMemcpyAsync(&rs.max_code, ctx->max_code.p, 4, cudaMemcpyDeviceToHost, s));
   CU(cudaStreamSynchronize(s));
   rs.n_empty = rs.hist[0];
   rs.max_len = 0;
@@ -486,6 +490,9 @@ int run_scoring(ish_ctx *ctx, Query &q, RecordSet &rs) {
     if (n_long)
       return fail(ctx, ISH_EINVAL, "%u records are longer than %llu residues with a non-free target start", n_long,
                   (unsigned long long)r.max_safe_len);
+    if (rs.max_code >= (uint32_t)q.alphabet)
+      return fail(ctx, ISH_EINVAL, "a record contains code %u >= the alphabet size %d of the query", rs.max_code,
+                  q.alphabet);
     if (ctx->kernel == ISH_KERNEL_PLAIN)
       rc = launch_plain(ctx, q, rs, 0, nonempty, out);
     else
@@ -582,7 +589,7 @@ void ish_gpu_close(ish_ctx *ctx) {
     kv.second.len_s.release();
     kv.second.orig_s.release();
   }
-  DevBuf *bufs[] = {&ctx->raw, &ctx->off_in, &ctx->len_tmp, &ctx->slot_tmp, &ctx->poff_tmp, &ctx->hist,
+  DevBuf *bufs[] = {&ctx->raw, &ctx->off_in, &ctx->len_tmp, &ctx->slot_tmp, &ctx->poff_tmp, &ctx->hist, &ctx->max_code,
                     &ctx->scan_tmp, &ctx->counter, &ctx->error, &ctx->out_score, &ctx->out_qend, &ctx->out_tend,
                     &ctx->out_hit, &ctx->hit_idx, &ctx->block_counts, &ctx->nhits, &ctx->plain_scratch};
   for (DevBuf *b : bufs) b->release();

@@ -69,14 +69,16 @@ __global__ void k_scatter(const uint32_t *len, const uint64_t *poff, uint32_t n,
 
 // One warp per record: copy src[off[i] .. off[i+1]) to dst[poff[i] ..) with
 // 16-byte stores, realigning 4-byte words with funnel shifts; the tail of the
-// 16-byte slot is zero-filled.
+// 16-byte slot is zero-filled.  The largest code of the set is reduced into
+// *max_code, so a query's alphabet can be checked once per set.
 __global__ void k_pack(const uint8_t *src, uint64_t src_bytes, const uint64_t *off, const uint64_t *poff,
-                       uint32_t n, uint8_t *dst) {
+                       uint32_t n, uint8_t *dst, uint32_t *max_code) {
   const uint32_t warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const uint32_t lane = threadIdx.x & 31;
   const uint32_t nwarps = (gridDim.x * blockDim.x) >> 5;
   const uint32_t *src32 = reinterpret_cast<const uint32_t *>(src);
   const uint64_t nwords = (src_bytes + 3) >> 2;
+  uint32_t mx = 0;
   for (uint32_t r = warp; r < n; r += nwarps) {
     const uint64_t s0 = off[r], len = off[r + 1] - off[r];
     uint4 *d = reinterpret_cast<uint4 *>(dst + poff[r]);
@@ -102,8 +104,12 @@ __global__ void k_pack(const uint8_t *src, uint64_t src_bytes, const uint64_t *o
         }
       }
       d[c] = make_uint4(o[0], o[1], o[2], o[3]);
+      mx = __vmaxu4(mx, __vmaxu4(__vmaxu4(o[0], o[1]), __vmaxu4(o[2], o[3])));
     }
   }
+  uint32_t m = max(max(mx & 0xffu, (mx >> 8) & 0xffu), max((mx >> 16) & 0xffu, mx >> 24));
+  for (int o = 16; o > 0; o >>= 1) m = max(m, __shfl_xor_sync(0xffffffffu, m, o));
+  if (lane == 0 && m) atomicMax(max_code, m);
 }
 
 // Exclusive scan of uint64 values (n <= 1024 * 1024 * 16 per call level).

@@ -15,7 +15,7 @@ __global__ void k_bucket_scan(uint32_t *hist);
 __global__ void k_scatter(const uint32_t *len, const uint64_t *poff, uint32_t n, uint32_t *cursor, uint32_t *len_s,
                           uint64_t *off_s, uint32_t *orig_s);
 __global__ void k_pack(const uint8_t *src, uint64_t src_bytes, const uint64_t *off, const uint64_t *poff, uint32_t n,
-                       uint8_t *dst);
+                       uint8_t *dst, uint32_t *max_code);
 __global__ void k_scan64_block(const uint64_t *in, uint64_t *out, uint32_t n, uint64_t *block_sums);
 __global__ void k_scan64_add(uint64_t *out, uint32_t n, const uint64_t *block_offsets);
 __global__ void k_trivial(RecordsDev rec, uint32_t first, uint32_t count, int mode, int qlen, OutDev out, Decision dec);

@@ -13,14 +13,16 @@
 // lanes" for short queries; G = 32 is a warp-wide anti-diagonal wavefront for
 // long queries.
 //
-// Per cell and record pair (two cells) the recurrence costs five DPX/SIMD
-// instructions:
-//   T = max(Hdiag + P, E);  u = T - open;  E = max(E - ext, u);  H = max(T, F);  F = max(F - ext, u)
-// (local alignment floors u at 0, which keeps E, F and H non-negative).  E
-// opens from T only, never from F: an F-then-E gap pair always has an
-// E-then-F twin of at least the same score, which this recurrence keeps, so H
-// is exactly the Gotoh H -- and the serial dependency along a row is the single
-// F instruction per cell.
+// Per cell and record pair (two cells) the recurrence costs five DPX
+// instructions, in two in-place passes over the thread's columns:
+//   backward:  T = max(Hdiag + P, E);  u = T - open;  E = max(E - ext, u);  H := T
+//   forward:   H = max(Fs - open, T);  Fs = max(Fs - ext, T)
+// with Fs = F + open carried along the row (local alignment floors u at 0,
+// which keeps E, T and H non-negative).  E opens from T only, never from F: an
+// F-then-E gap pair always has an E-then-F twin of at least the same score,
+// which this recurrence keeps, so H is exactly the Gotoh H.  The serial
+// dependency along a row is the single Fs instruction per cell, and both passes
+// update H and E in place (no register rotation between rows).
 //
 // End coordinates follow the reference exactly:
 //   semi-global, target end free: first row where H(i, Q-1) strictly beats the
@@ -56,6 +58,7 @@ __global__ void __launch_bounds__(256, (K <= 32 ? 2 : 1)) wave_kernel(const Wave
   const uint32_t NOPEN = dup16(-p.open);
   const uint32_t NEXT = dup16(-p.ext);
   const uint32_t VFLOOR = (MODE == SW) ? 0u : dup16(-32768);
+  const uint32_t FS_IN = dup16(p.fin + p.open);  // F + open entering the padding
   const bool te = (MODE == SG) && (p.ends & 8);
   const bool qe = (MODE == SG) && (p.ends & 2);
   const uint32_t npairs = (p.count + 1) >> 1;
@@ -152,21 +155,18 @@ __global__ void __launch_bounds__(256, (K <= 32 ? 2 : 1)) wave_kernel(const Wave
       }
 
       // ---- record codes of this row ----
+      // Codes were checked against the alphabet when the set was loaded and
+      // every record slot is zero-padded to 16 bytes.  Past a record's end the
+      // last word repeats: those rows only feed a lane whose result is final.
       if ((row & 3) == 0) {
         wA = nA;
         wB = nB;
         if (row + 4 < lenA) nA = __ldg(reinterpret_cast<const uint32_t *>(pa + row + 4));
         if (row + 4 < lenB) nB = __ldg(reinterpret_cast<const uint32_t *>(pb + row + 4));
       }
-      uint32_t cA = row < lenA ? (wA & 0xffu) : 0u;
-      uint32_t cB = row < lenB ? (wB & 0xffu) : 0u;
+      const uint32_t cA = wA & 0xffu, cB = wB & 0xffu;
       wA >>= 8;
       wB >>= 8;
-      if (cA >= (uint32_t)p.alphabet || cB >= (uint32_t)p.alphabet) {
-        atomicOr(p.error, 1);
-        cA = cA >= (uint32_t)p.alphabet ? 0u : cA;
-        cB = cB >= (uint32_t)p.alphabet ? 0u : cB;
-      }
 
       // ---- profile words of this row ----
       uint32_t P[K];
@@ -195,21 +195,24 @@ __global__ void __launch_bounds__(256, (K <= 32 ? 2 : 1)) wave_kernel(const Wave
         }
       }
 
-      // ---- the row ----
-      uint32_t hdiag = prevH;
-      uint32_t F = (t == 0) ? dup16(p.fin) : msgF;
+      // ---- the row: backward pass (columns independent), then the F chain ----
 #pragma unroll
-      for (int j = 0; j < K; ++j) {
-        const uint32_t T = __viaddmax_s16x2(hdiag, P[j], E[j]);
+      for (int j = K - 1; j >= 0; --j) {
+        const uint32_t T = __viaddmax_s16x2(j == 0 ? prevH : H[j - 1], P[j], E[j]);
         const uint32_t u = __viaddmax_s16x2(T, NOPEN, VFLOOR);
         E[j] = __viaddmax_s16x2(E[j], NEXT, u);
-        hdiag = H[j];
-        H[j] = __viaddmax_s16x2(T, 0u, F);  // DPX max (the legacy __vmaxs2 is emulated)
-        F = __viaddmax_s16x2(F, NEXT, u);
+        H[j] = T;
+      }
+      uint32_t Fs = (t == 0) ? FS_IN : msgF;
+#pragma unroll
+      for (int j = 0; j < K; ++j) {
+        const uint32_t T = H[j];
+        H[j] = __viaddmax_s16x2(Fs, NOPEN, T);
+        Fs = __viaddmax_s16x2(Fs, NEXT, T);
       }
       prevH = (t == 0) ? dup16(p.hleft) : msgH;
       outH = H[K - 1];
-      outF = F;
+      outF = Fs;
       outC = msgC;
 
       if (MODE == SG && te) {
@@ -376,11 +379,14 @@ __global__ void __launch_bounds__(256, (K <= 32 ? 2 : 1)) wave_kernel(const Wave
     // Every row thread 0 starts reaches thread G-1 within G-1 steps, so the
     // group is done once thread 0 is and no row is in flight.  The step budget
     // (all rows of the range plus the pipeline depth) is a hard stop.
-    const bool more = busy || (t == 0 && !f_done);
-    if (!__any_sync(FULL, more)) break;
-    if (++steps > p.max_steps) {
-      if (lane == 0) atomicOr(p.error, 2);
-      break;
+    // (checked every 8 steps; idle extra steps do nothing)
+    if ((++steps & 7) == 0) {
+      const bool more = busy || (t == 0 && !f_done);
+      if (!__any_sync(FULL, more)) break;
+      if (steps > p.max_steps) {
+        if (lane == 0) atomicOr(p.error, 2);
+        break;
+      }
     }
   }
 }
