@@ -380,11 +380,12 @@ int launch_wave(ish_ctx *ctx, Query &q, RecordSet &rs, uint32_t first, uint32_t 
   const int mode = q.algo == ISH_ALGO_LOCAL ? SW : SG;
   WaveFn fn = wave_fn(K, mode, L->pair);
   if (!fn) return fail(ctx, ISH_EOVERFLOW, "no wavefront kernel for K=%d", K);
-  const int groups = WAVE_THREADS / G;
+  const int threads = wave_block_threads(K);
+  const int groups = threads / G;
   const size_t smem = ((L->prof_bytes + 15) & ~15u) + (size_t)groups * 32 * 4;
   CU(cudaFuncSetAttribute((const void *)fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   int per_sm = 0;
-  CU(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, (const void *)fn, WAVE_THREADS, smem));
+  CU(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, (const void *)fn, threads, smem));
   if (per_sm < 1) return fail(ctx, ISH_EOVERFLOW, "wavefront kernel K=%d does not fit (smem %zu)", K, smem);
   const uint32_t pairs = (count + 1) / 2;
   const uint32_t want = ceil_div(pairs, groups);
@@ -417,7 +418,7 @@ int launch_wave(ish_ctx *ctx, Query &q, RecordSet &rs, uint32_t first, uint32_t 
   p.out = out;
   p.dec = Decision{q.max_score, q.thr};
   CU(cudaMemsetAsync(ctx->counter.p, 0, 4, ctx->stream));
-  fn<<<grid, WAVE_THREADS, smem, ctx->stream>>>(p);
+  fn<<<grid, threads, smem, ctx->stream>>>(p);
   CU(cudaGetLastError());
   return ISH_OK;
 }

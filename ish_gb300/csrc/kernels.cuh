@@ -29,7 +29,11 @@ __global__ void k_write_hits(const uint8_t *hit, uint32_t n, const uint32_t *blo
 // Wavefront kernels are instantiated for K = 2, 4, ..., WAVE_KMAX columns per
 // thread, both modes and both profile layouts.
 constexpr int WAVE_KMAX = 64;
-constexpr int WAVE_THREADS = 256;
+// Threads per block and blocks per SM (the register budget): 256 x 2 up to
+// K = 32 columns per thread, 128 x 3 up to K = 48 (12 warps per SM for wide
+// rows), 128 x 2 above.
+__host__ __device__ constexpr int wave_block_threads(int K) { return K <= 32 ? 256 : 128; }
+__host__ __device__ constexpr int wave_blocks_per_sm(int K) { return K <= 32 ? 2 : (K <= 48 ? 3 : 2); }
 typedef void (*WaveFn)(const WaveParams);
 // Returns the kernel for (K, mode, pair profile) or nullptr.
 WaveFn wave_fn(int K, int mode, int pair);

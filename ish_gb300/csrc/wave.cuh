@@ -34,12 +34,12 @@
 //     (ishlib/matcher/alignment/local_aln/striped.mojo:395-428).
 #pragma once
 
-#include "engine.cuh"
+#include "kernels.cuh"
 
 namespace ish {
 
 template <int K, int MODE, bool PAIR>
-__global__ void __launch_bounds__(256, (K <= 32 ? 2 : 1)) wave_kernel(const WaveParams p) {
+__global__ void __launch_bounds__(wave_block_threads(K), wave_blocks_per_sm(K)) wave_kernel(const WaveParams p) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const int tid = threadIdx.x;
   {
@@ -234,11 +234,17 @@ __global__ void __launch_bounds__(256, (K <= 32 ? 2 : 1)) wave_kernel(const Wave
         if (nb != best) {
           const int ca = lo16(cm), cb = hi16(cm);
           const bool upA = ca > lo16(best), upB = cb > hi16(best);
-          int qa = 0x7fff, qb = 0x7fff;
+          // rare path: stage the row in local memory and scan it with a rolled
+          // loop, so the scan adds no register pressure to the hot loop
+          uint32_t row_h[K];
 #pragma unroll
+          for (int j = 0; j < K; ++j) row_h[j] = H[j];
+          int qa = 0x7fff, qb = 0x7fff;
+#pragma unroll 1
           for (int j = K - 1; j >= 0; --j) {
-            if (lo16(H[j]) == ca) qa = col0 + j;
-            if (hi16(H[j]) == cb) qb = col0 + j;
+            const uint32_t h = row_h[j];
+            if (lo16(h) == ca) qa = col0 + j;
+            if (hi16(h) == cb) qb = col0 + j;
           }
           if (upA) {
             rowA = row;
@@ -271,10 +277,13 @@ __global__ void __launch_bounds__(256, (K <= 32 ? 2 : 1)) wave_kernel(const Wave
           uint32_t mx = 0, mq = 0;
           if (qe) {
             int bA = -32768, bB = -32768, qA = 0x7fff, qB = 0x7fff;
+            uint32_t row_h[K];  // staged as in the local-alignment scan
 #pragma unroll
+            for (int j = 0; j < K; ++j) row_h[j] = H[j];
+#pragma unroll 1
             for (int j = 0; j < K; ++j) {
               if (col0 + j >= 0) {
-                const int a = lo16(H[j]), b = hi16(H[j]);
+                const int a = lo16(row_h[j]), b = hi16(row_h[j]);
                 if (a > bA) {
                   bA = a;
                   qA = col0 + j;
