@@ -382,7 +382,8 @@ int launch_wave(ish_ctx *ctx, Query &q, RecordSet &rs, uint32_t first, uint32_t 
   if (!fn) return fail(ctx, ISH_EOVERFLOW, "no wavefront kernel for K=%d", K);
   const int threads = wave_block_threads(K);
   const int groups = threads / G;
-  const size_t smem = ((L->prof_bytes + 15) & ~15u) + (size_t)groups * 32 * 4;
+  const size_t save = mode == SW ? (size_t)threads * 2 * ((K + 3) & ~3) * 4 : 0;  // see wave.cuh (saveA/saveB)
+  const size_t smem = ((L->prof_bytes + 15) & ~15u) + (size_t)groups * 32 * 4 + save;
   CU(cudaFuncSetAttribute((const void *)fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   int per_sm = 0;
   CU(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, (const void *)fn, threads, smem));

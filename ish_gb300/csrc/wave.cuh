@@ -52,6 +52,11 @@ __global__ void __launch_bounds__(wave_block_threads(K), wave_blocks_per_sm(K)) 
   const int lane = tid & 31;
   const int t = lane & (G - 1);
   uint32_t *slots = reinterpret_cast<uint32_t *>(smem_raw + ((p.prof_bytes + 15u) & ~15u)) + (tid / G) * 32;
+  // local alignment: per thread, the H row of the last improvement of each lane
+  constexpr int KP4 = (K + 3) & ~3;
+  uint32_t *saveA = reinterpret_cast<uint32_t *>(smem_raw + ((p.prof_bytes + 15u) & ~15u)) +
+                    (blockDim.x / G) * 32 + tid * 2 * KP4;
+  uint32_t *saveB = saveA + KP4;
   __syncthreads();
 
   const unsigned FULL = 0xffffffffu;
@@ -81,7 +86,6 @@ __global__ void __launch_bounds__(wave_block_threads(K), wave_blocks_per_sm(K)) 
   // tracking
   uint32_t best = 0;         // SG: lane-wise running max of H(i, Q-1); SW: of this thread's cells
   int rowA = -1, rowB = -1;  // first row of the lane's maximum
-  int mqA = 0, mqB = 0;      // SW: smallest column of that maximum in that row
   uint32_t oR0 = 0, oR1 = 0, oR2 = 0, oR3 = 0;  // last-row partials for thread t+1
   bool has_out = false;
   // thread 0 of the group grabs record pairs
@@ -148,7 +152,6 @@ __global__ void __launch_bounds__(wave_block_threads(K), wave_blocks_per_sm(K)) 
         prevH = (t == 0) ? dup16(p.hleft) : dup16(p.hinit[t * K - 1]);
         best = (MODE == SW) ? 0u : dup16(p.neg_limit);
         rowA = rowB = -1;
-        mqA = mqB = 0;
         row = 0;
       } else {
         ++row;
@@ -232,28 +235,22 @@ __global__ void __launch_bounds__(wave_block_threads(K), wave_blocks_per_sm(K)) 
         if ((K & 1) == 0 && K > 1) cm = __viaddmax_s16x2(cm, 0u, H[K - 1]);
         const uint32_t nb = __viaddmax_s16x2(best, 0u, cm);
         if (nb != best) {
-          const int ca = lo16(cm), cb = hi16(cm);
-          const bool upA = ca > lo16(best), upB = cb > hi16(best);
-          // rare path: stage the row in local memory and scan it with a rolled
-          // loop, so the scan adds no register pressure to the hot loop
-          uint32_t row_h[K];
+          // keep this row (shared-memory stores only); the column of the
+          // maximum is looked up once, at the record's last row
+          const bool upA = lo16(cm) > lo16(best), upB = hi16(cm) > hi16(best);
+          uint32_t *dst = upA ? saveA : saveB;
 #pragma unroll
-          for (int j = 0; j < K; ++j) row_h[j] = H[j];
-          int qa = 0x7fff, qb = 0x7fff;
-#pragma unroll 1
-          for (int j = K - 1; j >= 0; --j) {
-            const uint32_t h = row_h[j];
-            if (lo16(h) == ca) qa = col0 + j;
-            if (hi16(h) == cb) qb = col0 + j;
+          for (int v = 0; v < KP4 / 4; ++v)
+            reinterpret_cast<uint4 *>(dst)[v] =
+                make_uint4(H[4 * v], 4 * v + 1 < K ? H[4 * v + 1] : 0u, 4 * v + 2 < K ? H[4 * v + 2] : 0u,
+                           4 * v + 3 < K ? H[4 * v + 3] : 0u);
+          if (upA && upB) {
+#pragma unroll
+            for (int v = 0; v < KP4 / 4; ++v)
+              reinterpret_cast<uint4 *>(saveB)[v] = reinterpret_cast<const uint4 *>(saveA)[v];
           }
-          if (upA) {
-            rowA = row;
-            mqA = qa;
-          }
-          if (upB) {
-            rowB = row;
-            mqB = qb;
-          }
+          if (upA) rowA = row;
+          if (upB) rowB = row;
           best = nb;
         }
       }
@@ -344,7 +341,13 @@ __global__ void __launch_bounds__(wave_block_threads(K), wave_blocks_per_sm(K)) 
             }
           }
         } else {
-          int bA = lo16(best), bB = hi16(best), rA = rowA, rB = rowB, qA = mqA, qB = mqB;
+          int bA = lo16(best), bB = hi16(best), rA = rowA, rB = rowB, qA = 0x7fff, qB = 0x7fff;
+          // smallest column of this thread's maximum in its first row
+#pragma unroll 1
+          for (int j = K - 1; j >= 0; --j) {
+            if (bA > 0 && lo16(saveA[j]) == bA) qA = col0 + j;
+            if (bB > 0 && hi16(saveB[j]) == bB) qB = col0 + j;
+          }
           if (t > 0) {
             const int ia = lo16(iR0), ib = hi16(iR0), ira = (int)iR2, irb = (int)iR3;
             const int iqa = (int)(int16_t)(iR1 & 0xffffu), iqb = (int)(int16_t)(iR1 >> 16);
