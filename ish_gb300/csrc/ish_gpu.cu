@@ -161,13 +161,15 @@ int neg_limit_of(int open, int mmin) {
 }
 
 // Columns per thread (K) and threads per group (G) for a query length: the
-// smallest modelled cost G*K*(1 + ROW_OVERHEAD/K) with G*K >= Q + 1.  Kernels
-// exist for every K <= 32 (two blocks per SM) and even K up to 64 (one block
-// per SM, charged double).
+// smallest modelled cost with G*K >= Q + 1.  Per thread-row the kernel spends
+// about five DPX instructions per column plus ~50 instructions of fixed work
+// (pipeline, codes, tracking), i.e. ROW_OVERHEAD column-equivalents; K <= 48
+// keeps 12-16 warps per SM, wider rows run at 8 (charged 25% more).  Kernels
+// exist for every K <= 32 and even K up to 64.
 int wave_k_available(int k) { return (k >= 1 && k <= 32) || (k > 32 && k <= WAVE_KMAX && !(k & 1)); }
 
 void choose_shape(int Q, int force_G, int force_K, int *G, int *K) {
-  const double ROW_OVERHEAD = 4.0;  // per-row instructions in units of cell pairs
+  const double ROW_OVERHEAD = 8.0;
   double bestc = 1e30;
   int bg = 0, bk = 0;
   for (int g = 1; g <= 32; g <<= 1) {
@@ -176,7 +178,7 @@ void choose_shape(int Q, int force_G, int force_K, int *G, int *K) {
     if (!force_K && k > 32) k = (k + 1) & ~1;
     if (!wave_k_available(k) || g * k < Q + 1) continue;
     double c = (double)g * k * (1.0 + ROW_OVERHEAD / k);
-    if (k > 32) c *= 2.0;
+    if (k > 48) c *= 1.25;
     if (c < bestc) {
       bestc = c;
       bg = g;
