@@ -278,11 +278,16 @@ def run_ours(args):
     dpx = ctx.calibrate()
     peak_gcups = dpx * 2 / INSTR_PER_CELL_PAIR / 1e9
     per_gpu = cells / (step_ms * 1e-3) / 1e9
+    # DRAM bytes per wave launch from the committed ncu capture (a smaller
+    # record set), scaled to this run's record stream.
     traffic = None
     prof = os.path.join(ROOT, "profiles", "wave_protein_traffic.json")
     if os.path.exists(prof):
         try:
-            traffic = json.load(open(prof)).get("dram_bytes_per_launch")
+            tj = json.load(open(prof))
+            per = tj["dram_bytes_per_launch_captured"]
+            traffic = int((per["semi_global"] + per["local"]) / 2 * int(wl.offsets[-1])
+                          / tj["captured_case"]["residues"])
         except Exception:
             traffic = None
 
