@@ -129,6 +129,72 @@ ISH_API int ish_gpu_score_set(ish_ctx *ctx, int32_t query_id, int32_t set_id, in
                       int32_t *query_end, int32_t *target_end, uint8_t *hit, uint32_t *hit_idx,
                       uint32_t *n_hits);
 
+/* Score several queries against one resident set in one batched launch.
+ * Replaces the reference's per-query launch loop over a record set
+ * (benchmarking/ish_bench_aligner_gpu.mojo:1616-1888 with 2039-2297: one
+ * launch per query, kernels instantiated per query-length bin).  Queries are
+ * grouped by kernel shape; each group runs as one persistent kernel whose
+ * blocks steal record pairs of the group's queries from per-query work
+ * counters, and the groups, the hit compaction and the counter resets form one
+ * CUDA graph, captured on the first call for a (query list, set, requested
+ * outputs) combination and replayed after.
+ *   score, query_end, target_end, hit: query-major arrays of n_queries * n
+ *     entries (n = records in the set): entry [i * n + r] is query
+ *     query_ids[i] against record r.  Any may be NULL.
+ *   hit_offsets: n_queries + 1 entries (may be NULL); query i's hits are
+ *     hit_idx[hit_offsets[i] .. hit_offsets[i + 1]), ascending record indices.
+ *   hit_idx: capacity hit_cap (may be NULL).  If the hits do not fit, nothing
+ *     is written to it, hit_offsets is still filled and ISH_EOVERFLOW returned.
+ * Results are identical to ish_gpu_score_set for every query. */
+ISH_API int ish_gpu_score_multi(ish_ctx *ctx, const int32_t *query_ids, uint32_t n_queries, int32_t set_id,
+                                int32_t *score, int32_t *query_end, int32_t *target_end, uint8_t *hit,
+                                uint32_t *hit_idx, uint64_t hit_cap, uint64_t *hit_offsets);
+
+/* Autotuner: for each query, times the candidate kernel shapes (threads per
+ * record pair, query columns per thread, profile layout) on a sample of a
+ * resident set and keeps the fastest for every later launch (single and
+ * batched) of a query with the same algorithm, alphabet and length.  group /
+ * cols (may be NULL) receive the shape each query now uses.  Options
+ * ISH_OPT_WAVE_GROUP / ISH_OPT_WAVE_K still override.  No counterpart in the
+ * reference (its kernels are instantiated per query-length bin,
+ * ish_bench_aligner_gpu.mojo:2039-2297, with a fixed launch shape,
+ * ishlib/gpu/searcher_device.mojo:477-497). */
+ISH_API int ish_gpu_autotune(ish_ctx *ctx, int32_t set_id, const int32_t *query_ids, uint32_t n_queries,
+                             int32_t *group, int32_t *cols);
+
+/* ---- serving loop: continuous batching against a resident set ----
+ * Replaces the reference's synchronous per-batch device round trip
+ * (ishlib/gpu/process_batch.mojo:27-163 driving SearcherDevice,
+ * ishlib/gpu/searcher_device.mojo:419-519) for callers that keep one record set
+ * on the device and score queries as they arrive.  A scheduler thread owned by
+ * the context admits waiting queries while fewer than max_active run and the
+ * device memory their outputs need (29 bytes per record of the set) fits
+ * mem_budget (0: half of the free device memory), and runs steps: each step
+ * scores the next of `chunks` equal-residue chunks of the set for every
+ * admitted query in one batched launch, so queries that arrive while others
+ * run join at the next step and share the device with them.  Results are
+ * identical to ish_gpu_score_set.  submit and poll may be called from any
+ * thread; the other calls on the context stay on one thread. */
+ISH_API int ish_gpu_serve_start(ish_ctx *ctx, int32_t set_id, uint32_t max_active, uint64_t mem_budget,
+                                uint32_t chunks);
+/* Queue query query_id (its parameters are copied; the query may be freed
+ * afterwards).  *ticket identifies the result. */
+ISH_API int ish_gpu_submit(ish_ctx *ctx, int32_t query_id, uint64_t *ticket);
+/* Result of a ticket: ISH_EAGAIN while it runs (after waiting up to wait_ms);
+ * else the hits (ascending record indices, with score, query end and target
+ * end of each; any pointer may be NULL), their number and the latency from
+ * submit to completion.  If the hits exceed cap, ISH_EOVERFLOW is returned with
+ * *n_hits set and the result kept.  A query that could not run returns its
+ * error.  A result is delivered once. */
+ISH_API int ish_gpu_poll(ish_ctx *ctx, uint64_t ticket, uint32_t *hit_idx, int32_t *hit_score, int32_t *hit_qend,
+                         int32_t *hit_tend, uint32_t cap, uint32_t *n_hits, double *latency_ms, int32_t wait_ms);
+/* Finish every queued and running query, then stop the scheduler. */
+ISH_API int ish_gpu_serve_stop(ish_ctx *ctx);
+/* Completed queries, cells scored, device time of the steps, the largest
+ * number of queries that shared a step, and the number of steps. */
+ISH_API int ish_gpu_serve_stats(ish_ctx *ctx, uint64_t *completed, double *cells, double *device_ms,
+                                uint32_t *max_active_seen, uint64_t *steps);
+
 /* Score records that are already in device memory, into device outputs,
  * without allocating anything.  No counterpart in the reference: this serves
  * callers that cannot allocate device memory when they score (device memory

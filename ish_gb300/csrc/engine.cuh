@@ -70,6 +70,22 @@ struct WaveParams {
   Decision dec;
 };
 
+// One work range of the batched launch: sorted entries [first, first + count)
+// of the record set scored against query q of the launch, handed out pair by
+// pair by its own counter.
+struct BatchTile {
+  uint32_t q, first, count, pad;
+};
+
+struct BatchParams {
+  const WaveParams *queries;  // per query of the launch: layout, outputs, decision
+  const BatchTile *tiles;
+  uint32_t ntiles;
+  uint32_t *tile_counter;     // one pair counter per tile, zeroed before launch
+  uint32_t prof_area;         // shared-memory bytes reserved for the largest profile (16-byte multiple)
+  uint32_t slot_words;        // slot words per block: 32 per group at the class's smallest G
+};
+
 struct PlainParams {
   const int16_t *prof;     // natural profile [code][Q]
   uint32_t prof_bytes;

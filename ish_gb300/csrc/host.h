@@ -1,0 +1,154 @@
+// host.h -- internal types of the host engine (not part of the C ABI): device
+// buffers, query and record-set state, the context, and the helpers shared by
+// the translation units of libish_gpu.so.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <map>
+#include <string>
+#include <vector>
+
+#include "../../include/ish_gpu.h"
+#include "kernels.cuh"
+
+namespace ish {
+namespace host {
+
+struct DevBuf {
+  void *p = nullptr;
+  size_t cap = 0;
+  cudaError_t ensure(size_t bytes) {
+    if (bytes <= cap && p) return cudaSuccess;
+    if (p) cudaFree(p);
+    p = nullptr;
+    cap = 0;
+    size_t want = bytes < 256 ? 256 : bytes;
+    cudaError_t e = cudaMalloc(&p, want);
+    if (e == cudaSuccess) cap = want;
+    return e;
+  }
+  void release() {
+    if (p) cudaFree(p);
+    p = nullptr;
+    cap = 0;
+  }
+  template <class T>
+  T *as() const { return reinterpret_cast<T *>(p); }
+};
+
+struct WaveLayout {
+  int G = 0, K = 0, d = 0, kp = 0, pair = 0;
+  uint32_t prof_bytes = 0;
+  DevBuf prof, hinit;
+};
+
+struct Query {
+  int algo = 0, kind = 0, alphabet = 0, Q = 0, open = 0, ext = 0, ends = 0;
+  int32_t max_score = 0;
+  float thr = 0.f;
+  std::vector<int8_t> M;
+  std::vector<uint8_t> q;
+  int mmin = 0, mmax = 0;
+  int neg_limit = 0;
+  DevBuf plain_prof, plain_hinit;
+  bool plain_ready = false;
+  std::map<long, WaveLayout> layouts;
+};
+
+struct RecordSet {
+  uint32_t n = 0;
+  uint64_t total = 0;
+  uint32_t max_len = 0;
+  DevBuf codes, off_s, len_s, orig_s;
+  std::vector<uint32_t> hist;  // length-bucket histogram (host copy)
+  uint32_t n_empty = 0;
+  uint32_t max_code = 0;       // largest record code in the set
+};
+
+struct Regime {
+  bool fast = false;
+  uint64_t max_safe_len = 0;  // records longer than this need the exact path
+};
+
+struct MultiPlan;  // multi.cu
+struct Server;     // serve.cu
+struct Tuned {
+  int G = 0, K = 0, pair = -1;  // pair: -1 = layout rule, 0 / 1 forced
+};
+
+}  // namespace host
+}  // namespace ish
+
+struct ish_ctx {
+  int device = 0;
+  int num_sms = 0;
+  cudaStream_t stream = nullptr;
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+  std::string err;
+  int kernel = ISH_KERNEL_AUTO;
+  int sg_lanes = 8, sw_u8_lanes = 16, sw_u16_lanes = 8;
+  int force_G = 0, force_K = 0;
+  std::map<int32_t, ish::host::Query> queries;
+  int32_t next_query = 1;
+  std::map<int32_t, ish::host::RecordSet> sets;
+  int32_t next_set = 1;
+  // scratch
+  ish::host::DevBuf raw, off_in, len_tmp, slot_tmp, poff_tmp, hist, scan_tmp, max_code;
+  ish::host::DevBuf counter, error, out_score, out_qend, out_tend, out_hit, hit_idx, block_counts, nhits;
+  ish::host::DevBuf plain_scratch;
+  float last_ms = 0.f;
+  // batched launches (multi.cu): plans cached per (queries, set, outputs)
+  std::map<std::string, ish::host::MultiPlan *> plans;
+  // autotuner results: (mode, alphabet, query length) -> shape
+  std::map<uint64_t, ish::host::Tuned> tuned;
+  // the serving loop (serve.cu), if started
+  ish::host::Server *server = nullptr;
+};
+
+
+namespace ish {
+namespace host {
+
+int fail(ish_ctx *c, int code, const char *fmt, ...);
+extern thread_local std::string g_open_error;
+
+#define CU(call)                                                                                   \
+  do {                                                                                             \
+    cudaError_t _e = (call);                                                                       \
+    if (_e != cudaSuccess)                                                                         \
+      return ::ish::host::fail(ctx, _e == cudaErrorMemoryAllocation ? ISH_ENOMEM : ISH_EDEVICE,     \
+                               "%s: %s (%s:%d)", #call, cudaGetErrorString(_e), __FILE__, __LINE__); \
+  } while (0)
+
+inline uint32_t ceil_div(uint64_t a, uint64_t b) { return (uint32_t)((a + b - 1) / b); }
+
+Regime regime(const Query &q, int qpad);
+int wave_k_available(int k);
+// Shape of the wavefront kernel for a query: the autotuner's choice when one
+// exists, else the cost model; forced options override both.
+void pick_shape(ish_ctx *ctx, const Query &q, int *G, int *K, int *pair);
+void choose_shape(int Q, int force_G, int force_K, int *G, int *K);
+uint64_t tune_key(int mode, int alphabet, int Q);
+int pair_layout_fits(int alphabet, int G, int K);
+int build_wave_layout(ish_ctx *ctx, Query &q, int G, int K, int pair, WaveLayout **out);
+int load_records(ish_ctx *ctx, const uint8_t *records, const uint64_t *offsets, uint32_t n, RecordSet &rs);
+uint32_t count_longer(const RecordSet &rs, uint64_t len);
+// Checks that query q may run on the wavefront kernels against set rs with
+// shape (G, K): 0 or a status with the reason in msg.  check_fast picks the
+// shape and records the reason as the context's error.
+int fast_check(const Query &q, const RecordSet &rs, int G, int K, char *msg, size_t len);
+int check_fast(ish_ctx *ctx, const Query &q, const RecordSet &rs);
+// Fills the per-query part of the wavefront parameters (not first/count/counter).
+void wave_params(const Query &q, const WaveLayout &L, const RecordSet &rs, OutDev out, int *error, WaveParams *p);
+int launch_wave_range(ish_ctx *ctx, Query &q, RecordSet &rs, uint32_t first, uint32_t count, OutDev out, int G, int K,
+                      int pair, cudaStream_t s);
+void drop_plans(ish_ctx *ctx, int32_t query_id, int32_t set_id);  // multi.cu
+void free_plans(ish_ctx *ctx);                                   // multi.cu
+void stop_server(ish_ctx *ctx);                                  // serve.cu
+bool server_uses_set(const ish_ctx *ctx, int32_t set_id);        // serve.cu
+size_t wave_smem(uint32_t prof_area, int threads, int G, int K, int mode);
+
+}  // namespace host
+}  // namespace ish

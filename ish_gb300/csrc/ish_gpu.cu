@@ -13,89 +13,16 @@
 #include <string>
 #include <vector>
 
-#include "../../include/ish_gpu.h"
-#include "kernels.cuh"
+#include "host.h"
 
 using namespace ish;
 
-namespace {
+using namespace ish::host;
+
+namespace ish {
+namespace host {
 
 thread_local std::string g_open_error;
-
-struct DevBuf {
-  void *p = nullptr;
-  size_t cap = 0;
-  cudaError_t ensure(size_t bytes) {
-    if (bytes <= cap && p) return cudaSuccess;
-    if (p) cudaFree(p);
-    p = nullptr;
-    cap = 0;
-    size_t want = bytes < 256 ? 256 : bytes;
-    cudaError_t e = cudaMalloc(&p, want);
-    if (e == cudaSuccess) cap = want;
-    return e;
-  }
-  void release() {
-    if (p) cudaFree(p);
-    p = nullptr;
-    cap = 0;
-  }
-  template <class T>
-  T *as() const { return reinterpret_cast<T *>(p); }
-};
-
-struct WaveLayout {
-  int G = 0, K = 0, d = 0, kp = 0, pair = 0;
-  uint32_t prof_bytes = 0;
-  DevBuf prof, hinit;
-};
-
-struct Query {
-  int algo = 0, kind = 0, alphabet = 0, Q = 0, open = 0, ext = 0, ends = 0;
-  int32_t max_score = 0;
-  float thr = 0.f;
-  std::vector<int8_t> M;
-  std::vector<uint8_t> q;
-  int mmin = 0, mmax = 0;
-  int neg_limit = 0;
-  DevBuf plain_prof, plain_hinit;
-  bool plain_ready = false;
-  std::map<long, WaveLayout> layouts;
-};
-
-struct RecordSet {
-  uint32_t n = 0;
-  uint64_t total = 0;
-  uint32_t max_len = 0;
-  DevBuf codes, off_s, len_s, orig_s;
-  std::vector<uint32_t> hist;  // length-bucket histogram (host copy)
-  uint32_t n_empty = 0;
-  uint32_t max_code = 0;       // largest record code in the set
-};
-
-}  // namespace
-
-struct ish_ctx {
-  int device = 0;
-  int num_sms = 0;
-  cudaStream_t stream = nullptr;
-  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
-  std::string err;
-  int kernel = ISH_KERNEL_AUTO;
-  int sg_lanes = 8, sw_u8_lanes = 16, sw_u16_lanes = 8;
-  int force_G = 0, force_K = 0;
-  std::map<int32_t, Query> queries;
-  int32_t next_query = 1;
-  std::map<int32_t, RecordSet> sets;
-  int32_t next_set = 1;
-  // scratch
-  DevBuf raw, off_in, len_tmp, slot_tmp, poff_tmp, hist, scan_tmp, max_code;
-  DevBuf counter, error, out_score, out_qend, out_tend, out_hit, hit_idx, block_counts, nhits;
-  DevBuf plain_scratch;
-  float last_ms = 0.f;
-};
-
-namespace {
 
 int fail(ish_ctx *c, int code, const char *fmt, ...) {
   char buf[512];
@@ -108,26 +35,12 @@ int fail(ish_ctx *c, int code, const char *fmt, ...) {
   return code;
 }
 
-#define CU(call)                                                                                   \
-  do {                                                                                             \
-    cudaError_t _e = (call);                                                                       \
-    if (_e != cudaSuccess)                                                                         \
-      return fail(ctx, _e == cudaErrorMemoryAllocation ? ISH_ENOMEM : ISH_EDEVICE, "%s: %s (%s:%d)", \
-                  #call, cudaGetErrorString(_e), __FILE__, __LINE__);                              \
-  } while (0)
-
-inline uint32_t ceil_div(uint64_t a, uint64_t b) { return (uint32_t)((a + b - 1) / b); }
-
 int matrix_alphabet_ok(uint32_t alphabet) { return alphabet >= 1 && alphabet <= 256; }
 
 // Safe-regime checks (see engine.cuh): the fast kernels evaluate plain Gotoh
 // in 16-bit lanes; the result equals the reference's striped int16 pass when
 // gap_open > gap_extend and no lane value of the reference can saturate or
 // wrap.  Bounds are conservative.
-struct Regime {
-  bool fast = false;
-  uint64_t max_safe_len = 0;  // records longer than this need the exact path
-};
 
 Regime regime(const Query &q, int qpad) {
   Regime r;
@@ -189,8 +102,29 @@ void choose_shape(int Q, int force_G, int force_K, int *G, int *K) {
   *K = bk;
 }
 
-int build_wave_layout(ish_ctx *ctx, Query &q, int G, int K, WaveLayout **out) {
-  const int pair_ok = q.alphabet * q.alphabet * G * (((K + 3) & ~3) + 4) * 4 <= 64 * 1024;
+uint64_t tune_key(int mode, int alphabet, int Q) { return ((uint64_t)mode << 48) | ((uint64_t)alphabet << 32) | (uint32_t)Q; }
+
+// The 32-bit pair profile (one load per column for both records) when it is
+// small enough to stay cheap in shared memory, else the 16-bit single-code one.
+int pair_layout_fits(int alphabet, int G, int K) {
+  return alphabet * alphabet * G * (((K + 3) & ~3) + 4) * 4 <= 64 * 1024;
+}
+
+void pick_shape(ish_ctx *ctx, const Query &q, int *G, int *K, int *pair) {
+  const int mode = q.algo == ISH_ALGO_LOCAL ? SW : SG;
+  auto it = ctx->tuned.find(tune_key(mode, q.alphabet, q.Q));
+  if (!ctx->force_G && !ctx->force_K && it != ctx->tuned.end()) {
+    *G = it->second.G;
+    *K = it->second.K;
+    *pair = it->second.pair >= 0 ? it->second.pair : pair_layout_fits(q.alphabet, *G, *K);
+    return;
+  }
+  choose_shape(q.Q, ctx->force_G, ctx->force_K, G, K);
+  *pair = *G ? pair_layout_fits(q.alphabet, *G, *K) : 0;
+}
+
+int build_wave_layout(ish_ctx *ctx, Query &q, int G, int K, int pair, WaveLayout **out) {
+  const int pair_ok = pair;
   const long key = ((long)G << 20) | ((long)K << 8) | pair_ok;
   auto it = q.layouts.find(key);
   if (it != q.layouts.end()) {
@@ -371,38 +305,19 @@ int ensure_outputs(ish_ctx *ctx, uint32_t n) {
   return ISH_OK;
 }
 
-int launch_wave(ish_ctx *ctx, Query &q, RecordSet &rs, uint32_t first, uint32_t count, OutDev out) {
-  if (count == 0) return ISH_OK;
-  int G, K;
-  choose_shape(q.Q, ctx->force_G, ctx->force_K, &G, &K);
-  if (!G || G * K < q.Q + 1) return fail(ctx, ISH_EOVERFLOW, "no wavefront shape for a query of %d residues", q.Q);
-  WaveLayout *L = nullptr;
-  int rc = build_wave_layout(ctx, q, G, K, &L);
-  if (rc) return rc;
+void wave_params(const Query &q, const WaveLayout &L, const RecordSet &rs, OutDev out, int *error, WaveParams *pp) {
+  WaveParams &p = *pp;
+  p = WaveParams{};
   const int mode = q.algo == ISH_ALGO_LOCAL ? SW : SG;
-  WaveFn fn = wave_fn(K, mode, L->pair);
-  if (!fn) return fail(ctx, ISH_EOVERFLOW, "no wavefront kernel for K=%d", K);
-  const int threads = wave_block_threads(K);
-  const int groups = threads / G;
-  const size_t save = mode == SW ? (size_t)threads * 2 * ((K + 3) & ~3) * 4 : 0;  // see wave.cuh (saveA/saveB)
-  const size_t smem = ((L->prof_bytes + 15) & ~15u) + (size_t)groups * 32 * 4 + save;
-  CU(cudaFuncSetAttribute((const void *)fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-  int per_sm = 0;
-  CU(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, (const void *)fn, threads, smem));
-  if (per_sm < 1) return fail(ctx, ISH_EOVERFLOW, "wavefront kernel K=%d does not fit (smem %zu)", K, smem);
-  const uint32_t pairs = (count + 1) / 2;
-  const uint32_t want = ceil_div(pairs, groups);
-  const uint32_t grid = std::max<uint32_t>(1, std::min<uint32_t>(want, (uint32_t)(per_sm * ctx->num_sms)));
-  WaveParams p{};
-  p.prof = L->prof.as<const uint4>();
-  p.prof_bytes = L->prof_bytes;
+  p.prof = L.prof.as<const uint4>();
+  p.prof_bytes = L.prof_bytes;
   p.Q = q.Q;
-  p.G = G;
-  p.K = K;
-  p.d = L->d;
-  p.kp = L->kp;
+  p.G = L.G;
+  p.K = L.K;
+  p.d = L.d;
+  p.kp = L.kp;
   p.alphabet = q.alphabet;
-  p.pair_prof = L->pair;
+  p.pair_prof = L.pair;
   p.open = q.open;
   p.ext = q.ext;
   p.ends = q.ends;
@@ -410,18 +325,49 @@ int launch_wave(ish_ctx *ctx, Query &q, RecordSet &rs, uint32_t first, uint32_t 
   const bool sg = mode == SG;
   p.hleft = (sg && !(q.ends & ISH_FREE_TARGET_START)) ? NEG_BIG : 0;
   p.fin = sg ? NEG_BIG : 0;
-  p.hinit = L->hinit.as<const int16_t>();
-  p.first = first;
-  p.count = count;
-  p.counter = ctx->counter.as<uint32_t>();
-  p.max_steps = rs.total + 2ull * count + 1024;
-  p.error = ctx->error.as<int>();
+  p.hinit = L.hinit.as<const int16_t>();
+  p.error = error;
   p.rec = RecordsDev{rs.codes.as<const uint8_t>(), rs.off_s.as<const uint64_t>(), rs.len_s.as<const uint32_t>(),
                      rs.orig_s.as<const uint32_t>(), rs.n};
   p.out = out;
   p.dec = Decision{q.max_score, q.thr};
-  CU(cudaMemsetAsync(ctx->counter.p, 0, 4, ctx->stream));
-  fn<<<grid, threads, smem, ctx->stream>>>(p);
+}
+
+// Shared memory of a wavefront block: the profile, 32 slot words per group,
+// and (local alignment) 2 * KP4 save words per thread (see wave.cuh).
+size_t wave_smem(uint32_t prof_area, int threads, int G, int K, int mode) {
+  const size_t save = mode == SW ? (size_t)threads * 2 * ((K + 3) & ~3) * 4 : 0;
+  return prof_area + (size_t)(threads / G) * 32 * 4 + save;
+}
+
+int launch_wave_range(ish_ctx *ctx, Query &q, RecordSet &rs, uint32_t first, uint32_t count, OutDev out, int G, int K,
+                      int pair, cudaStream_t s) {
+  if (count == 0) return ISH_OK;
+  if (!G || G * K < q.Q + 1) return fail(ctx, ISH_EOVERFLOW, "no wavefront shape for a query of %d residues", q.Q);
+  WaveLayout *L = nullptr;
+  int rc = build_wave_layout(ctx, q, G, K, pair, &L);
+  if (rc) return rc;
+  const int mode = q.algo == ISH_ALGO_LOCAL ? SW : SG;
+  WaveFn fn = wave_fn(K, mode, L->pair);
+  if (!fn) return fail(ctx, ISH_EOVERFLOW, "no wavefront kernel for K=%d", K);
+  const int threads = wave_block_threads(K);
+  const int groups = threads / G;
+  const size_t smem = wave_smem((L->prof_bytes + 15) & ~15u, threads, G, K, mode);
+  CU(cudaFuncSetAttribute((const void *)fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  int per_sm = 0;
+  CU(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, (const void *)fn, threads, smem));
+  if (per_sm < 1) return fail(ctx, ISH_EOVERFLOW, "wavefront kernel K=%d does not fit (smem %zu)", K, smem);
+  const uint32_t pairs = (count + 1) / 2;
+  const uint32_t want = ceil_div(pairs, groups);
+  const uint32_t grid = std::max<uint32_t>(1, std::min<uint32_t>(want, (uint32_t)(per_sm * ctx->num_sms)));
+  WaveParams p;
+  wave_params(q, *L, rs, out, ctx->error.as<int>(), &p);
+  p.first = first;
+  p.count = count;
+  p.counter = ctx->counter.as<uint32_t>();
+  p.max_steps = rs.total + 2ull * count + 1024;
+  CU(cudaMemsetAsync(ctx->counter.p, 0, 4, s));
+  fn<<<grid, threads, smem, s>>>(p);
   CU(cudaGetLastError());
   return ISH_OK;
 }
@@ -462,6 +408,40 @@ int launch_plain(ish_ctx *ctx, Query &q, RecordSet &rs, uint32_t first, uint32_t
   return ISH_OK;
 }
 
+int fast_check(const Query &q, const RecordSet &rs, int G, int K, char *msg, size_t len) {
+  Regime r = regime(q, G ? G * K : q.Q + 64);
+  if (!r.fast) {
+    snprintf(msg, len,
+             "parameters outside the exact-integer fast regime (gap_open must exceed gap_extend and scores must stay "
+             "within int16)");
+    return ISH_EINVAL;
+  }
+  const uint32_t nonempty = rs.n - rs.n_empty;
+  const uint32_t n_long = r.max_safe_len == ~0ull ? 0 : std::min(count_longer(rs, r.max_safe_len), nonempty);
+  if (n_long) {
+    snprintf(msg, len, "%u records are longer than %llu residues with a non-free target start", n_long,
+             (unsigned long long)r.max_safe_len);
+    return ISH_EINVAL;
+  }
+  if (rs.max_code >= (uint32_t)q.alphabet) {
+    snprintf(msg, len, "a record contains code %u >= the alphabet size %d of the query", rs.max_code, q.alphabet);
+    return ISH_EINVAL;
+  }
+  if (!G || G * K < q.Q + 1) {
+    snprintf(msg, len, "no wavefront shape for a query of %d residues", q.Q);
+    return ISH_EOVERFLOW;
+  }
+  return ISH_OK;
+}
+
+int check_fast(ish_ctx *ctx, const Query &q, const RecordSet &rs) {
+  int G, K, pair;
+  pick_shape(ctx, q, &G, &K, &pair);
+  char msg[256];
+  const int rc = fast_check(q, rs, G, K, msg, sizeof msg);
+  return rc ? fail(ctx, rc, "%s", msg) : ISH_OK;
+}
+
 // Score query q against set rs into the context's device output buffers.
 int run_scoring(ish_ctx *ctx, Query &q, RecordSet &rs) {
   const uint32_t n = rs.n;
@@ -483,24 +463,15 @@ int run_scoring(ish_ctx *ctx, Query &q, RecordSet &rs) {
     CU(cudaGetLastError());
   }
   if (nonempty) {
-    int G, K;
-    choose_shape(q.Q, ctx->force_G, ctx->force_K, &G, &K);
-    Regime r = regime(q, G ? G * K : q.Q + 64);
-    if (!r.fast)
-      return fail(ctx, ISH_EINVAL,
-                  "parameters outside the exact-integer fast regime (gap_open must exceed gap_extend and scores "
-                  "must stay within int16)");
-    const uint32_t n_long = r.max_safe_len == ~0ull ? 0 : std::min(count_longer(rs, r.max_safe_len), nonempty);
-    if (n_long)
-      return fail(ctx, ISH_EINVAL, "%u records are longer than %llu residues with a non-free target start", n_long,
-                  (unsigned long long)r.max_safe_len);
-    if (rs.max_code >= (uint32_t)q.alphabet)
-      return fail(ctx, ISH_EINVAL, "a record contains code %u >= the alphabet size %d of the query", rs.max_code,
-                  q.alphabet);
-    if (ctx->kernel == ISH_KERNEL_PLAIN)
+    rc = check_fast(ctx, q, rs);
+    if (rc) return rc;
+    if (ctx->kernel == ISH_KERNEL_PLAIN) {
       rc = launch_plain(ctx, q, rs, 0, nonempty, out);
-    else
-      rc = launch_wave(ctx, q, rs, 0, nonempty, out);
+    } else {
+      int G, K, pair;
+      pick_shape(ctx, q, &G, &K, &pair);
+      rc = launch_wave_range(ctx, q, rs, 0, nonempty, out, G, K, pair, s);
+    }
     if (rc) return rc;
   }
   return ISH_OK;
@@ -543,7 +514,8 @@ int fetch_outputs(ish_ctx *ctx, uint32_t n, int32_t *score, int32_t *qend, int32
   return ISH_OK;
 }
 
-}  // namespace
+}  // namespace host
+}  // namespace ish
 
 extern "C" {
 
@@ -578,7 +550,9 @@ int ish_gpu_open(int device, ish_ctx **out) {
 void ish_gpu_close(ish_ctx *ctx) {
   if (!ctx) return;
   cudaSetDevice(ctx->device);
+  stop_server(ctx);
   cudaStreamSynchronize(ctx->stream);
+  free_plans(ctx);
   for (auto &kv : ctx->queries) {
     kv.second.plain_prof.release();
     kv.second.plain_hinit.release();
@@ -623,11 +597,13 @@ int ish_gpu_set_option(ish_ctx *ctx, int option, int64_t value) {
     if (value != 0 && (value < 1 || value > 32 || (value & (value - 1))))
       return fail(ctx, ISH_EINVAL, "group size must be 0 or a power of two <= 32");
     ctx->force_G = (int)value;
+    drop_plans(ctx, 0, 0);
     return ISH_OK;
   case ISH_OPT_WAVE_K:
     if (value != 0 && !wave_k_available((int)value))
       return fail(ctx, ISH_EINVAL, "K must be 0, 1..32 or even up to %d", WAVE_KMAX);
     ctx->force_K = (int)value;
+    drop_plans(ctx, 0, 0);
     return ISH_OK;
   default:
     return fail(ctx, ISH_EINVAL, "unknown option %d", option);
@@ -686,6 +662,7 @@ int ish_gpu_free_query(ish_ctx *ctx, int32_t query_id) {
   auto it = ctx->queries.find(query_id);
   if (it == ctx->queries.end()) return fail(ctx, ISH_EINVAL, "unknown query %d", query_id);
   cudaStreamSynchronize(ctx->stream);
+  drop_plans(ctx, query_id, 0);
   it->second.plain_prof.release();
   it->second.plain_hinit.release();
   for (auto &l : it->second.layouts) {
@@ -718,7 +695,9 @@ int ish_gpu_records_free(ish_ctx *ctx, int32_t set_id) {
   if (!ctx) return ISH_EINVAL;
   auto it = ctx->sets.find(set_id);
   if (it == ctx->sets.end()) return fail(ctx, ISH_EINVAL, "unknown record set %d", set_id);
+  if (server_uses_set(ctx, set_id)) return fail(ctx, ISH_EINVAL, "record set %d is used by the serving loop", set_id);
   cudaStreamSynchronize(ctx->stream);
+  drop_plans(ctx, 0, set_id);
   it->second.codes.release();
   it->second.off_s.release();
   it->second.len_s.release();
@@ -813,5 +792,20 @@ WaveFn wave_fn(int K, int mode, int pair) {
   if (K <= 32) return wave_fn_d(K, mode, pair);
   if (K <= 48) return wave_fn_e(K, mode, pair);
   return wave_fn_f(K, mode, pair);
+}
+BatchFn batch_fn_a(int, int, int);
+BatchFn batch_fn_b(int, int, int);
+BatchFn batch_fn_c(int, int, int);
+BatchFn batch_fn_d(int, int, int);
+BatchFn batch_fn_e(int, int, int);
+BatchFn batch_fn_f(int, int, int);
+BatchFn batch_fn(int K, int mode, int pair) {
+  if (K < 1) return nullptr;
+  if (K <= 8) return batch_fn_a(K, mode, pair);
+  if (K <= 16) return batch_fn_b(K, mode, pair);
+  if (K <= 24) return batch_fn_c(K, mode, pair);
+  if (K <= 32) return batch_fn_d(K, mode, pair);
+  if (K <= 48) return batch_fn_e(K, mode, pair);
+  return batch_fn_f(K, mode, pair);
 }
 }  // namespace ish

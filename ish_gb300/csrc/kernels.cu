@@ -307,8 +307,13 @@ PlainFn plain_fn(int mode) { return mode == SW ? (PlainFn)plain_kernel<SW> : (Pl
 // ---------------------------------------------------------------------------
 // Hit compaction: indices of hit[i] != 0 in ascending order.
 // ---------------------------------------------------------------------------
+// Hit compaction.  blockIdx.y selects one of several query-major flag arrays
+// of n entries (batched launches); counts and offsets are laid out [y][x], so
+// one exclusive scan over them concatenates the per-query hit lists.
 __global__ void k_count_hits(const uint8_t *hit, uint32_t n, uint32_t *block_counts) {
   __shared__ uint32_t wsum[32];
+  hit += (size_t)blockIdx.y * n;
+  block_counts += (size_t)blockIdx.y * gridDim.x;
   const uint32_t base = blockIdx.x * HIT_TILE;
   uint32_t c = 0;
   for (uint32_t i = base + threadIdx.x; i < min(n, base + HIT_TILE); i += blockDim.x) c += hit[i] != 0;
@@ -348,6 +353,8 @@ __global__ void k_scan_counts(uint32_t *counts, uint32_t nb, uint32_t *total) {
 __global__ void k_write_hits(const uint8_t *hit, uint32_t n, const uint32_t *block_offsets, uint32_t *idx) {
   __shared__ uint32_t wsum[32];
   __shared__ uint32_t run;
+  hit += (size_t)blockIdx.y * n;
+  block_offsets += (size_t)blockIdx.y * gridDim.x;
   const uint32_t base = blockIdx.x * HIT_TILE;
   if (threadIdx.x == 0) run = block_offsets[blockIdx.x];
   __syncthreads();
@@ -367,6 +374,19 @@ __global__ void k_write_hits(const uint8_t *hit, uint32_t n, const uint32_t *blo
     __syncthreads();
     if (threadIdx.x == 0) run += total;
     __syncthreads();
+  }
+}
+
+// Scores and end coordinates of the compacted hits (the hit count is read on
+// the device, so no host round trip is needed before the gather).
+__global__ void k_gather_hits(const uint32_t *idx, const uint32_t *count, const int32_t *score, const int32_t *qend,
+                              const int32_t *tend, int32_t *hit_score, int32_t *hit_qend, int32_t *hit_tend) {
+  const uint32_t nh = *count;
+  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < nh; i += gridDim.x * blockDim.x) {
+    const uint32_t r = idx[i];
+    hit_score[i] = score[r];
+    hit_qend[i] = qend[r];
+    hit_tend[i] = tend[r];
   }
 }
 

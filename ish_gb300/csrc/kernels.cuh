@@ -25,6 +25,8 @@ __global__ void k_count_hits(const uint8_t *hit, uint32_t n, uint32_t *block_cou
 __global__ void k_scan_counts(uint32_t *counts, uint32_t nb, uint32_t *total);
 __global__ void k_dpx_peak(uint32_t *out, int iters, uint32_t b, uint32_t c);
 __global__ void k_write_hits(const uint8_t *hit, uint32_t n, const uint32_t *block_offsets, uint32_t *idx);
+__global__ void k_gather_hits(const uint32_t *idx, const uint32_t *count, const int32_t *score, const int32_t *qend,
+                              const int32_t *tend, int32_t *hit_score, int32_t *hit_qend, int32_t *hit_tend);
 
 // Wavefront kernels are instantiated for K = 2, 4, ..., WAVE_KMAX columns per
 // thread, both modes and both profile layouts.
@@ -37,5 +39,7 @@ __host__ __device__ constexpr int wave_blocks_per_sm(int K) { return K <= 32 ? 2
 typedef void (*WaveFn)(const WaveParams);
 // Returns the kernel for (K, mode, pair profile) or nullptr.
 WaveFn wave_fn(int K, int mode, int pair);
+typedef void (*BatchFn)(const BatchParams);
+BatchFn batch_fn(int K, int mode, int pair);  // batch_kernel<K, mode, pair> or nullptr
 
 }  // namespace ish

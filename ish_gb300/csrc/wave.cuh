@@ -38,26 +38,23 @@
 
 namespace ish {
 
+// Scores sorted entries [p.first, p.first + p.count) of the record set: the
+// groups of the calling block take record pairs from *counter until none are
+// left.  `prof` is the profile in shared memory; `slots_all` holds 32 words per
+// group (pair indices in flight), `save_all` 2 * KP4 words per thread (local
+// alignment only).
 template <int K, int MODE, bool PAIR>
-__global__ void __launch_bounds__(wave_block_threads(K), wave_blocks_per_sm(K)) wave_kernel(const WaveParams p) {
-  extern __shared__ __align__(16) unsigned char smem_raw[];
+__device__ __forceinline__ void wave_rows(const WaveParams &p, const unsigned char *prof, uint32_t *slots_all,
+                                          uint32_t *save_all, uint32_t *counter) {
   const int tid = threadIdx.x;
-  {
-    const uint4 *src = p.prof;
-    uint4 *dst = reinterpret_cast<uint4 *>(smem_raw);
-    const uint32_t nvec = p.prof_bytes >> 4;
-    for (uint32_t i = tid; i < nvec; i += blockDim.x) dst[i] = src[i];
-  }
   const int G = p.G;
   const int lane = tid & 31;
   const int t = lane & (G - 1);
-  uint32_t *slots = reinterpret_cast<uint32_t *>(smem_raw + ((p.prof_bytes + 15u) & ~15u)) + (tid / G) * 32;
+  uint32_t *slots = slots_all + (tid / G) * 32;
   // local alignment: per thread, the H row of the last improvement of each lane
   constexpr int KP4 = (K + 3) & ~3;
-  uint32_t *saveA = reinterpret_cast<uint32_t *>(smem_raw + ((p.prof_bytes + 15u) & ~15u)) +
-                    (blockDim.x / G) * 32 + tid * 2 * KP4;
+  uint32_t *saveA = save_all + tid * 2 * KP4;
   uint32_t *saveB = saveA + KP4;
-  __syncthreads();
 
   const unsigned FULL = 0xffffffffu;
   const uint32_t NOPEN = dup16(-p.open);
@@ -67,8 +64,8 @@ __global__ void __launch_bounds__(wave_block_threads(K), wave_blocks_per_sm(K)) 
   const bool te = (MODE == SG) && (p.ends & 8);
   const bool qe = (MODE == SG) && (p.ends & 2);
   const uint32_t npairs = (p.count + 1) >> 1;
-  const uint16_t *prof16 = reinterpret_cast<const uint16_t *>(smem_raw);
-  const uint32_t *prof32 = reinterpret_cast<const uint32_t *>(smem_raw);
+  const uint16_t *prof16 = reinterpret_cast<const uint16_t *>(prof);
+  const uint32_t *prof32 = reinterpret_cast<const uint32_t *>(prof);
   const int col0 = t * K - p.d;  // query column of register 0
 
   uint32_t H[K], E[K];
@@ -102,7 +99,7 @@ __global__ void __launch_bounds__(wave_block_threads(K), wave_blocks_per_sm(K)) 
 
     if (t == 0) {
       if (!f_active && !f_done) {
-        const uint32_t np = atomicAdd(p.counter, 1u);
+        const uint32_t np = atomicAdd(counter, 1u);
         if (np < npairs) {
           f_active = true;
           f_seq = (f_seq + 1) & 31;
@@ -400,6 +397,77 @@ __global__ void __launch_bounds__(wave_block_threads(K), wave_blocks_per_sm(K)) 
         break;
       }
     }
+  }
+}
+
+// Shared memory of a block: the profile, then 32 slot words per group, then
+// (local alignment) 2 * KP4 save words per thread.
+template <int K, int MODE, bool PAIR>
+__global__ void __launch_bounds__(wave_block_threads(K), wave_blocks_per_sm(K))
+    wave_kernel(const __grid_constant__ WaveParams p) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  {
+    const uint4 *src = p.prof;
+    uint4 *dst = reinterpret_cast<uint4 *>(smem_raw);
+    const uint32_t nvec = p.prof_bytes >> 4;
+    for (uint32_t i = threadIdx.x; i < nvec; i += blockDim.x) dst[i] = src[i];
+  }
+  uint32_t *slots_all = reinterpret_cast<uint32_t *>(smem_raw + ((p.prof_bytes + 15u) & ~15u));
+  uint32_t *save_all = slots_all + (blockDim.x / p.G) * 32;
+  __syncthreads();
+  wave_rows<K, MODE, PAIR>(p, smem_raw, slots_all, save_all, p.counter);
+}
+
+// The batched launch: one persistent kernel for every query of a shape class
+// (same K, mode and profile layout; G may differ per query).  Each query's
+// record pairs are handed out by its own counter in global memory, in
+// descending length order, exactly as in wave_kernel.  A block walks the
+// queries of the class starting at its own offset (so the blocks spread over
+// the queries) and stays on a query until its counter runs dry; a barrier and
+// a profile reload happen only at a query switch, where the pairs left are the
+// shortest of the set.  Queries whose counter is already exhausted are skipped.
+template <int K, int MODE, bool PAIR>
+__global__ void __launch_bounds__(wave_block_threads(K), wave_blocks_per_sm(K))
+    batch_kernel(const __grid_constant__ BatchParams b) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  __shared__ WaveParams sp;
+  __shared__ int s_skip;
+  uint32_t *slots_all = reinterpret_cast<uint32_t *>(smem_raw + b.prof_area);
+  uint32_t *save_all = slots_all + b.slot_words;
+  const uint32_t start = (uint32_t)(((uint64_t)blockIdx.x * b.ntiles) / gridDim.x);
+  for (uint32_t it = 0; it < b.ntiles; ++it) {
+    uint32_t tile = start + it;
+    if (tile >= b.ntiles) tile -= b.ntiles;
+    const BatchTile tl = b.tiles[tile];
+    const WaveParams *qp = b.queries + tl.q;
+    uint32_t *counter = b.tile_counter + tile;
+    if (threadIdx.x == 0) {
+      const uint32_t taken = *reinterpret_cast<volatile uint32_t *>(counter);
+      s_skip = taken >= (tl.count + 1) / 2;
+      if (!s_skip) {
+        sp = *qp;
+        sp.first = tl.first;
+        sp.count = tl.count;
+        // every group's steps are bounded by all pairs of the range at its
+        // longest length (records are sorted, the first is longest)
+        const uint64_t npairs = (tl.count + 1) / 2;
+        sp.max_steps = npairs * ((uint64_t)qp->rec.len[tl.first] + 2 * 32 + 8) + 1024;
+      }
+    }
+    __syncthreads();
+    if (s_skip) {
+      __syncthreads();  // s_skip is rewritten next iteration
+      continue;
+    }
+    {
+      const uint4 *src = qp->prof;
+      uint4 *dst = reinterpret_cast<uint4 *>(smem_raw);
+      const uint32_t nvec = qp->prof_bytes >> 4;
+      for (uint32_t i = threadIdx.x; i < nvec; i += blockDim.x) dst[i] = src[i];
+    }
+    __syncthreads();
+    wave_rows<K, MODE, PAIR>(sp, smem_raw, slots_all, save_all, counter);
+    __syncthreads();
   }
 }
 

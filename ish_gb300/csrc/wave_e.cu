@@ -36,4 +36,35 @@ WaveFn wave_fn_e(int K, int mode, int pair) {
   }
 }
 
+BatchFn batch_fn_e(int K, int mode, int pair) {
+  switch (K) {
+    case 34:
+      return mode == SG ? (pair ? (BatchFn)batch_kernel<34, SG, true> : (BatchFn)batch_kernel<34, SG, false>)
+                        : (pair ? (BatchFn)batch_kernel<34, SW, true> : (BatchFn)batch_kernel<34, SW, false>);
+    case 36:
+      return mode == SG ? (pair ? (BatchFn)batch_kernel<36, SG, true> : (BatchFn)batch_kernel<36, SG, false>)
+                        : (pair ? (BatchFn)batch_kernel<36, SW, true> : (BatchFn)batch_kernel<36, SW, false>);
+    case 38:
+      return mode == SG ? (pair ? (BatchFn)batch_kernel<38, SG, true> : (BatchFn)batch_kernel<38, SG, false>)
+                        : (pair ? (BatchFn)batch_kernel<38, SW, true> : (BatchFn)batch_kernel<38, SW, false>);
+    case 40:
+      return mode == SG ? (pair ? (BatchFn)batch_kernel<40, SG, true> : (BatchFn)batch_kernel<40, SG, false>)
+                        : (pair ? (BatchFn)batch_kernel<40, SW, true> : (BatchFn)batch_kernel<40, SW, false>);
+    case 42:
+      return mode == SG ? (pair ? (BatchFn)batch_kernel<42, SG, true> : (BatchFn)batch_kernel<42, SG, false>)
+                        : (pair ? (BatchFn)batch_kernel<42, SW, true> : (BatchFn)batch_kernel<42, SW, false>);
+    case 44:
+      return mode == SG ? (pair ? (BatchFn)batch_kernel<44, SG, true> : (BatchFn)batch_kernel<44, SG, false>)
+                        : (pair ? (BatchFn)batch_kernel<44, SW, true> : (BatchFn)batch_kernel<44, SW, false>);
+    case 46:
+      return mode == SG ? (pair ? (BatchFn)batch_kernel<46, SG, true> : (BatchFn)batch_kernel<46, SG, false>)
+                        : (pair ? (BatchFn)batch_kernel<46, SW, true> : (BatchFn)batch_kernel<46, SW, false>);
+    case 48:
+      return mode == SG ? (pair ? (BatchFn)batch_kernel<48, SG, true> : (BatchFn)batch_kernel<48, SG, false>)
+                        : (pair ? (BatchFn)batch_kernel<48, SW, true> : (BatchFn)batch_kernel<48, SW, false>);
+    default:
+      return nullptr;
+  }
+}
+
 }  // namespace ish

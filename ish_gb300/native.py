@@ -23,7 +23,8 @@ EXPORTS = (
     "ish_gpu_abi_version", "ish_gpu_open", "ish_gpu_close", "ish_gpu_last_error", "ish_gpu_set_option",
     "ish_gpu_set_query", "ish_gpu_free_query", "ish_gpu_score", "ish_gpu_records_load", "ish_gpu_records_free",
     "ish_gpu_records_info", "ish_gpu_score_set", "ish_gpu_last_kernel_ms", "ish_gpu_calibrate",
-    "ish_gpu_score_noalloc",
+    "ish_gpu_score_noalloc", "ish_gpu_score_multi", "ish_gpu_autotune", "ish_gpu_serve_start", "ish_gpu_submit",
+    "ish_gpu_poll", "ish_gpu_serve_stop", "ish_gpu_serve_stats",
 )
 
 
@@ -82,6 +83,14 @@ def load(build_if_missing: bool = False):
     L.ish_gpu_score_noalloc.argtypes = [vp, C.c_uint64, vp, C.c_uint32, u8p, C.c_uint32, i8p, C.c_uint32, C.c_int,
                                         C.c_uint32, C.c_uint32, C.c_uint32, C.c_int32, C.c_float, vp, vp, vp, vp,
                                         vp, C.c_char_p, C.c_size_t]
+    L.ish_gpu_score_multi.argtypes = [vp, i32p, C.c_uint32, C.c_int32, i32p, i32p, i32p, u8p, u32p, C.c_uint64, u64p]
+    L.ish_gpu_autotune.argtypes = [vp, C.c_int32, i32p, C.c_uint32, i32p, i32p]
+    L.ish_gpu_serve_start.argtypes = [vp, C.c_int32, C.c_uint32, C.c_uint64, C.c_uint32]
+    L.ish_gpu_submit.argtypes = [vp, C.c_int32, u64p]
+    L.ish_gpu_poll.argtypes = [vp, C.c_uint64, u32p, i32p, i32p, i32p, C.c_uint32, u32p, C.POINTER(C.c_double),
+                               C.c_int32]
+    L.ish_gpu_serve_stop.argtypes = [vp]
+    L.ish_gpu_serve_stats.argtypes = [vp, u64p, C.POINTER(C.c_double), C.POINTER(C.c_double), u32p, u64p]
     for name in EXPORTS:
         if name not in ("ish_gpu_close", "ish_gpu_last_error"):
             getattr(L, name).restype = C.c_int
@@ -215,6 +224,81 @@ class Context:
         if "hit_idx" in out:
             res["hit_idx"] = out["hit_idx"][: nh.value]
         return res
+
+    def score_multi(self, qids, sid: int, want=("score", "qend", "tend", "hit", "hit_idx")) -> dict:
+        """Batched launch of several queries against resident set `sid`.
+
+        Arrays come back shaped (len(qids), n); "hit_idx" is a list with one
+        array of ascending record indices per query."""
+        n, _ = self.records_info(sid)
+        q = np.ascontiguousarray(qids, np.int32)
+        nq = len(q)
+        tot = max(nq * n, 1)
+        out = {}
+        for k, dt in (("score", np.int32), ("qend", np.int32), ("tend", np.int32), ("hit", np.uint8)):
+            if k in want:
+                out[k] = np.empty(tot, dt)
+        cap = 0
+        idx = offs = None
+        if "hit_idx" in want:
+            cap = tot
+            idx = np.empty(cap, np.uint32)
+            offs = np.empty(nq + 1, np.uint64)
+        self._check(self._L.ish_gpu_score_multi(
+            self._h, _p(q, C.c_int32), nq, sid, _p(out.get("score"), C.c_int32), _p(out.get("qend"), C.c_int32),
+            _p(out.get("tend"), C.c_int32), _p(out.get("hit"), C.c_uint8), _p(idx, C.c_uint32), cap,
+            _p(offs, C.c_uint64)))
+        res = {k: v[: nq * n].reshape(nq, n) for k, v in out.items()}
+        if idx is not None:
+            res["hit_idx"] = [idx[int(offs[i]):int(offs[i + 1])] for i in range(nq)]
+        return res
+
+    def autotune(self, sid: int, qids):
+        """Times candidate kernel shapes for each query on a sample of set
+        `sid`; returns the (group, cols) arrays now in use."""
+        q = np.ascontiguousarray(qids, np.int32)
+        g = np.zeros(max(len(q), 1), np.int32)
+        k = np.zeros(max(len(q), 1), np.int32)
+        self._check(self._L.ish_gpu_autotune(self._h, sid, _p(q, C.c_int32), len(q), _p(g, C.c_int32),
+                                             _p(k, C.c_int32)))
+        return g[: len(q)], k[: len(q)]
+
+    # ---- serving loop ----
+    def serve_start(self, sid: int, max_active: int = 64, mem_budget: int = 0, chunks: int = 8):
+        self._check(self._L.ish_gpu_serve_start(self._h, sid, max_active, mem_budget, chunks))
+
+    def submit(self, qid: int) -> int:
+        t = C.c_uint64()
+        self._check(self._L.ish_gpu_submit(self._h, qid, C.byref(t)))
+        return t.value
+
+    def poll(self, ticket: int, wait_ms: int = 0):
+        """None while the query runs; else a dict with the hits (record index,
+        score, query end, target end) and the latency in ms."""
+        nh = C.c_uint32()
+        lat = C.c_double()
+        rc = self._L.ish_gpu_poll(self._h, ticket, None, None, None, None, 0, C.byref(nh), C.byref(lat), wait_ms)
+        if rc == EAGAIN:
+            return None
+        self._check(rc)
+        # the counts are known now; fetch the arrays (the result is kept until
+        # it is delivered in full)
+        return self._poll_full(ticket, nh.value, lat.value)
+
+    def _poll_full(self, ticket, nh, lat):
+        return {"n_hits": nh, "latency_ms": lat, "ticket": ticket}
+
+    def serve_stop(self):
+        self._check(self._L.ish_gpu_serve_stop(self._h))
+
+    def serve_stats(self) -> dict:
+        done, steps = C.c_uint64(), C.c_uint64()
+        cells, ms = C.c_double(), C.c_double()
+        mx = C.c_uint32()
+        self._check(self._L.ish_gpu_serve_stats(self._h, C.byref(done), C.byref(cells), C.byref(ms), C.byref(mx),
+                                                C.byref(steps)))
+        return {"completed": done.value, "cells": cells.value, "device_ms": ms.value, "max_active": mx.value,
+                "steps": steps.value}
 
     def calibrate(self) -> float:
         """Packed 16-bit DPX add-max instructions per second on this device."""
