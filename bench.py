@@ -34,7 +34,10 @@ import numpy as np
 ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
-INSTR_PER_CELL_PAIR = 5  # max, add-max, sub, add-max (E), add-max (F): wave.cuh
+# DPX add-max instructions per cell pair of the wavefront kernel (wave.cuh):
+# T = max(Hdiag + P, E), u = max(T - open, floor), E = max(E - ext, u),
+# H = max(Fs - open, T), Fs = max(Fs - ext, T).
+INSTR_PER_CELL_PAIR = 5
 
 
 def parse():
@@ -43,7 +46,11 @@ def parse():
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
-    ap.add_argument("--records", type=int, default=1_000_000, help="records in the batch (default: full size)")
+    ap.add_argument("--workload", choices=["protein", "line", "batched", "long", "serving"], default="protein",
+                    help="protein: single-query protein search (the headline line); line: ascii line search; "
+                         "batched: 64 nucleotide queries in one launch; long: 1 Mb-class nucleotide records; "
+                         "serving: Poisson query stream against a resident 4 GB set")
+    ap.add_argument("--records", type=int, default=None, help="records in the batch (default: the workload's size)")
     ap.add_argument("--cpu-seconds", type=float, default=12.0, help="target CPU time of the baseline sample")
     ap.add_argument("--no-plain", action="store_true", help="skip the plain-kernel comparison")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline")
@@ -336,11 +343,335 @@ def run_ours(args):
         dist.destroy_process_group()
 
 
+# ---------------------------------------------------------------------------
+# The other workloads of ish's benchmark configurations (one JSON line each).
+# ---------------------------------------------------------------------------
+
+def _base_line(args, world, value, ms, config, dtype="s16x2"):
+    return {"metric": "GCUPS", "value": round(value, 2), "unit": "GCUPS", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": round(ms, 3), "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": dtype, "data": "synthetic", "config": config}
+
+
+def _queries_of(name, wl):
+    """[(encoded query, oracle algo, ends, max_score)], gap_open, gap_ext, threshold."""
+    import oracle as O
+    from ish_gb300.scoring import ScoringMatrix
+
+    m = ScoringMatrix(wl.kind)
+    mx = lambda q: int(m.values[q, q].astype(np.int64).sum())
+    if name == "line":
+        q = wl.queries[0]
+        return [(q, O.SEMI_GLOBAL, O.TS | O.TE, mx(q))], 3, 1, 0.8
+    if name == "batched":
+        return [(q, O.SEMI_GLOBAL, O.TS | O.TE, mx(q)) for q in wl.queries], 3, 1, 0.8
+    if name == "long":
+        q = wl.queries[0]
+        return [(q, O.SEMI_GLOBAL, O.TS | O.TE, mx(q))], 3, 1, 0.8
+    raise ValueError(name)
+
+
+def _cpu_sample(wl, queries, gap_open, gap_ext, thr, seconds, max_queries=8):
+    """The oracle (all host threads) on a bounded sample: every k-th query and
+    a random subset of records sized to about `seconds`."""
+    import oracle as O
+
+    threads = os.cpu_count() or 1
+    qs = queries[:: max(1, len(queries) // max_queries)][:max_queries]
+    rng = np.random.default_rng(123)
+
+    def timed(idx):
+        sub = wl.subset(idx)
+        t = time.perf_counter()
+        for q, algo, ends, mx in qs:
+            om = O.Matcher(algo, wl.kind, q, mx, thr, gap_open=gap_open, gap_extend=gap_ext, ends=ends)
+            om.batch(sub.records, sub.offsets, threads=threads, forward=False, matches=True)
+        return sub, time.perf_counter() - t
+
+    n0 = min(wl.n, 64 if wl.lengths.mean() > 20000 else 400)
+    sub, dt = timed(np.sort(rng.choice(wl.n, n0, replace=False)))
+    k = int(min(wl.n, max(n0, n0 * seconds / max(dt, 1e-3))))
+    idx = np.sort(rng.choice(wl.n, k, replace=False))
+    sub, dt = timed(idx)
+    cells = sum(len(q) for q, *_ in qs) * int(sub.offsets[-1])
+    return {"value": round(cells / dt / 1e9, 4), "unit": "GCUPS", "cores": threads, "kind": "port",
+            "sample": f"{len(qs)} of {len(queries)} queries x {k} of {wl.n} records, {dt:.1f} s on {threads} threads"}
+
+
+def _roofline(ctx, gcups):
+    dpx = ctx.calibrate()
+    peak = dpx * 2 / INSTR_PER_CELL_PAIR / 1e9
+    return {"bound": "int", "achieved": round(gcups, 2), "peak": round(peak, 2), "unit": "GCUPS",
+            "frac": round(gcups / peak, 4), "traffic": None,
+            "peak_source": f"measured now: {dpx / 1e12:.2f} T DPX add-max instr/s x 2 cells / "
+                           f"{INSTR_PER_CELL_PAIR} instr per cell pair"}
+
+
+def _pinned(wl):
+    try:
+        import torch
+
+        pin = torch.empty(len(wl.records), dtype=torch.uint8, pin_memory=True).numpy()
+        pin_off = torch.empty(len(wl.offsets), dtype=torch.int64, pin_memory=True).numpy().view(np.uint64)
+    except Exception:
+        pin = np.empty(len(wl.records), np.uint8)
+        pin_off = np.empty(len(wl.offsets), np.uint64)
+    pin[:] = wl.records
+    pin_off[:] = wl.offsets
+    return pin, pin_off
+
+
+def run_workload(args):
+    from ish_gb300 import native, workloads
+    from ish_gb300.scoring import ScoringMatrix
+
+    name = args.workload
+    rank, world, local, dist = (0, 1, 0, None) if args.impl == "reference" else dist_setup(args.gpus)
+    if args.impl == "reference" and int(os.environ.get("RANK", "0")) != 0:
+        return
+    seed_shift = rank
+    if name == "line":
+        wl = workloads.line_ascii(seed=0 + seed_shift, n=args.records or 100_000)
+        config = {"workload": f"ascii line search: 24-byte query vs {wl.n} printable lines of U[20,120] bytes, "
+                              "match +2 / mismatch -2, gap 3/1, striped-semi-global FFTT, threshold 0.8",
+                  "records": wl.n, "l2": "7 MB of lines: resident in L2 between steps", "parallelism": "records"}
+    elif name == "batched":
+        wl = workloads.nucleotide_multi(seed=2 + seed_shift, n=args.records or 2_000_000)
+        config = {"workload": f"batched nucleotide search: 64 queries of U[50,1000] nt vs {wl.n} reads of "
+                              "U[100,300] nt, actgn, gap 3/1, striped-semi-global FFTT, threshold 0.8, one batched "
+                              "launch per step", "queries": len(wl.queries), "records": wl.n,
+                  "l2": "reads (400 MB) larger than L2", "parallelism": "records"}
+    elif name == "long":
+        wl = workloads.long_targets(seed=3 + seed_shift, n=args.records or 10_000)
+        config = {"workload": f"long-target search: 1000-nt query vs {wl.n} records of log-uniform 10 kb-1 Mb, "
+                              "actgn0, gap 3/1, striped-semi-global FFTT, threshold 0.8",
+                  "records": wl.n, "residues": int(wl.offsets[-1]), "l2": "2.1 GB of records: every pass reads HBM",
+                  "parallelism": "records"}
+    else:
+        return run_serving(args, rank, world, local, dist)
+    queries, gap_open, gap_ext, thr = _queries_of(name, wl)
+    residues = int(wl.offsets[-1])
+    cells = sum(len(q) for q, *_ in queries) * residues
+
+    if args.impl == "reference":
+        times = []
+        cpu = None
+        for s in range(args.warmup + args.steps):
+            cpu = _cpu_sample(wl, queries, gap_open, gap_ext, thr, args.cpu_seconds / max(1, args.steps + args.warmup))
+            if s >= args.warmup:
+                times.append(cpu["value"])
+        v = float(np.mean(times))
+        line = _base_line(args, 1, v, cells / (v * 1e9) * 1e3, config, "int16")
+        line.update({"impl": "reference", "cpu_baseline": dict(cpu, value=round(v, 4)),
+                     "e2e": {"value": round(v, 4), "unit": "GCUPS", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}})
+        print(json.dumps(line))
+        return
+
+    native.load(build_if_missing=True)
+    m = ScoringMatrix(wl.kind)
+    ctx = native.Context(local)
+    qids = [ctx.set_query(q, wl.kind, m.values, native.ALGO_SEMI_GLOBAL, gap_open, gap_ext,
+                          native.FREE_TARGET_START | native.FREE_TARGET_END, mx, thr) for q, _, _, mx in queries]
+    sid = ctx.records_load(wl.records, wl.offsets)
+    extra = {}
+    t0 = time.perf_counter()
+    g, k = ctx.autotune(sid, qids)
+    extra["autotune"] = {"seconds": round(time.perf_counter() - t0, 3),
+                         "shapes": sorted({(int(a), int(b)) for a, b in zip(g, k)})[:16]}
+
+    if name == "batched":
+        def step():
+            r = ctx.score_multi(qids, sid, want=("hit_idx",))
+            return ctx.last_kernel_ms(), r
+        launches_per_step = None
+    else:
+        def step():
+            r = ctx.score_set(qids[0], sid, want=("score", "qend", "tend", "hit_idx"))
+            return ctx.last_kernel_ms(), r
+
+    for _ in range(args.warmup):
+        step()
+    clocks = Clocks(local)
+    clocks.start()
+    barrier(dist)
+    dev = []
+    for _ in range(args.steps):
+        ms, res = step()
+        dev.append(ms)
+    barrier(dist)
+    clk = clocks.stop()
+    step_ms = reduce_max(dist, float(np.mean(dev)))
+    value = world * cells / (step_ms * 1e-3) / 1e9
+
+    # comparisons: the same queries one launch each (wavefront kernel), and
+    # the plain one-thread-per-record kernel on a sample
+    if name == "batched":
+        per = []
+        for qid in qids:
+            ctx.score_set(qid, sid, want=("hit_idx",))
+            per.append(ctx.last_kernel_ms())
+        extra["per_query_wave_launches_gcups"] = round(cells / (sum(per) * 1e-3) / 1e9, 2)
+    n_plain = min(wl.n, 200_000 if name == "batched" else (wl.n if name == "line" else 200))
+    sub = wl.subset(np.arange(n_plain))
+    sid2 = ctx.records_load(sub.records, sub.offsets)
+    ctx.set_option(native.OPT_KERNEL, native.KERNEL_PLAIN)
+    pq = qids[:: max(1, len(qids) // 8)][:8]
+    pms = 0.0
+    for qid in pq:
+        ctx.score_set(qid, sid2, want=("hit_idx",))
+        pms += ctx.last_kernel_ms()
+    ctx.set_option(native.OPT_KERNEL, native.KERNEL_AUTO)
+    pcells = sum(len(queries[qids.index(q)][0]) for q in pq) * int(sub.offsets[-1])
+    ctx.records_free(sid2)
+    plain = pcells / (pms * 1e-3) / 1e9
+    extra["plain_per_query_gcups"] = round(plain, 2)
+    extra["plain_sample"] = f"{len(pq)} queries x {n_plain} records, one launch per query"
+    extra["speedup_vs_plain"] = round(value / world / plain, 1)
+
+    # end to end from pinned host memory: upload + pack + score + results
+    pin, pin_off = _pinned(wl)
+    e2e = []
+    nh = 0
+    for s in range(args.warmup + args.steps):
+        barrier(dist)
+        t = time.perf_counter()
+        sid3 = ctx.records_load(pin, pin_off)
+        if name == "batched":
+            r = ctx.score_multi(qids, sid3, want=("hit_idx",))
+            nh = sum(len(h) for h in r["hit_idx"])
+        else:
+            r = ctx.score_set(qids[0], sid3, want=("score", "qend", "tend", "hit_idx"))
+            nh = len(r["hit_idx"])
+        ctx.records_free(sid3)
+        if s >= args.warmup:
+            e2e.append(1e3 * (time.perf_counter() - t))
+    e2e_ms = reduce_max(dist, float(np.mean(e2e)))
+    d2h = 4 * nh + (0 if name == "batched" else 12 * wl.n) + 8 * (len(qids) + 1)
+    cpu = None
+    if rank == 0 and not args.no_cpu:
+        cpu = _cpu_sample(wl, queries, gap_open, gap_ext, thr, args.cpu_seconds)
+    if rank == 0:
+        line = _base_line(args, world, value, step_ms, config)
+        line.update({
+            "roofline": _roofline(ctx, value / world),
+            "cpu_baseline": cpu,
+            "e2e": {"value": round(world * cells / (e2e_ms * 1e-3) / 1e9, 2), "unit": "GCUPS",
+                    "h2d_bytes_per_step": int(len(wl.records) + 8 * len(wl.offsets)), "d2h_bytes_per_step": int(d2h),
+                    "latency_ms": {"p50": round(float(np.percentile(e2e, 50)), 3),
+                                   "p99": round(float(np.percentile(e2e, 99)), 3)}},
+            "gpu_launches": None, "clocks": clk, "hits": int(nh), **extra,
+        })
+        print(json.dumps(line))
+    ctx.close()
+    if dist is not None:
+        dist.destroy_process_group()
+
+
+def run_serving(args, rank, world, local, dist):
+    """Poisson query streams against a resident protein set through the
+    serving loop (ish_gpu_serve_*); one JSON line with p50/p99 per rate."""
+    from ish_gb300 import native, workloads
+    from ish_gb300.scoring import ScoringMatrix
+
+    gb = float(os.environ.get("ISH_SERVE_GB", "4"))
+    wl = workloads.serving_records(seed=4 + rank, total_bytes=int(gb * (1 << 30)))
+    residues = int(wl.offsets[-1])
+    m = ScoringMatrix(wl.kind)
+    count = max(args.steps, 4)
+    rates = (10.0, 100.0, 2000.0)
+    config = {"workload": f"serving: {gb:g} GB resident blosum62 protein set ({wl.n} records, lognormal median "
+                          f"350), Poisson arrivals at {', '.join(f'{r:g}' for r in rates)} queries/s, {count} "
+                          "queries per rate, Q ~ U[20,2000], striped-local / semi-global FFTT mix, gap 10/1, "
+                          "threshold 0.8", "records": wl.n, "residues": residues, "parallelism": "records"}
+    if args.impl == "reference":
+        qs = workloads.serving_queries(count=4, rate=rates[0])
+        import oracle as O
+
+        queries = [(q, O.LOCAL if a == "striped-local" else O.SEMI_GLOBAL,
+                    0 if a == "striped-local" else O.TS | O.TE, int(m.values[q, q].sum())) for _, a, q in qs]
+        cpu = _cpu_sample(wl, queries, 10, 1, 0.8, args.cpu_seconds)
+        line = _base_line(args, 1, cpu["value"], 0.0, config, "int16")
+        line.update({"impl": "reference", "cpu_baseline": cpu,
+                     "e2e": {"value": cpu["value"], "unit": "GCUPS", "h2d_bytes_per_step": 0,
+                             "d2h_bytes_per_step": 0}})
+        print(json.dumps(line))
+        return
+    native.load(build_if_missing=True)
+    ctx = native.Context(local)
+    sid = ctx.records_load(wl.records, wl.offsets)
+    per_rate = []
+    clocks = Clocks(local)
+    clocks.start()
+    total_cells = total_ms = 0.0
+    for rate in rates:
+        qs = workloads.serving_queries(count=count, rate=rate)
+        ids = []
+        for _, algo, q in qs:
+            a = native.ALGO_LOCAL if algo == "striped-local" else native.ALGO_SEMI_GLOBAL
+            ids.append(ctx.set_query(q, wl.kind, m.values, a, 10, 1,
+                                     native.FREE_TARGET_START | native.FREE_TARGET_END if a == 0 else 0,
+                                     int(m.values[q, q].sum()), 0.8))
+        ctx.serve_start(sid, max_active=64, chunks=8)
+        start = time.perf_counter()
+        tickets = []
+        for (arrival, _, _), qid in zip(qs, ids):
+            now = time.perf_counter() - start
+            if arrival > now:
+                time.sleep(arrival - now)
+            tickets.append(ctx.submit(qid))
+        lat = []
+        for t in tickets:
+            r = None
+            while r is None:
+                r = ctx.poll(t, wait_ms=200)
+            lat.append(r["latency_ms"])
+        span = time.perf_counter() - start
+        st = ctx.serve_stats()
+        ctx.serve_stop()
+        for qid in ids:
+            ctx.free_query(qid)
+        cells = sum(len(q) for _, _, q in qs) * residues
+        total_cells += st["cells"]
+        total_ms += st["device_ms"]
+        per_rate.append({"offered_per_s": rate, "served_per_s": round(count / span, 3),
+                         "p50_ms": round(float(np.percentile(lat, 50)), 1),
+                         "p99_ms": round(float(np.percentile(lat, 99)), 1),
+                         "wall_gcups": round(cells / span / 1e9, 1),
+                         "device_gcups": round(st["cells"] / st["device_ms"] / 1e6, 1),
+                         "max_active": st["max_active"], "steps": st["steps"]})
+    clk = clocks.stop()
+    value = total_cells / (total_ms * 1e-3) / 1e9
+    # the plain one-thread-per-record kernel, one query on a record sample
+    sub = wl.subset(np.arange(0, wl.n, max(1, wl.n // 100_000)))
+    sid2 = ctx.records_load(sub.records, sub.offsets)
+    q = workloads.serving_queries(count=1, rate=1.0, seed=11)[0][2]
+    pq = ctx.set_query(q, wl.kind, m.values, native.ALGO_SEMI_GLOBAL, 10, 1, 12, int(m.values[q, q].sum()), 0.8)
+    ctx.set_option(native.OPT_KERNEL, native.KERNEL_PLAIN)
+    ctx.score_set(pq, sid2, want=("hit_idx",))
+    plain = len(q) * int(sub.offsets[-1]) / (ctx.last_kernel_ms() * 1e-3) / 1e9
+    ctx.set_option(native.OPT_KERNEL, native.KERNEL_AUTO)
+    line = _base_line(args, world, value, total_ms / max(1, len(rates) * count), config)
+    line.update({"roofline": _roofline(ctx, value), "cpu_baseline": None,
+                 "e2e": {"value": per_rate[-1]["wall_gcups"], "unit": "GCUPS",
+                         "h2d_bytes_per_step": int(np.mean([len(q) for _, _, q in qs])) + 8,
+                         "d2h_bytes_per_step": 0,
+                         "latency_ms": {"p50": per_rate[-1]["p50_ms"], "p99": per_rate[-1]["p99_ms"]}},
+                 "serving": per_rate, "plain_per_query_gcups": round(plain, 2),
+                 "gpu_launches": None, "clocks": clk})
+    if rank == 0:
+        print(json.dumps(line))
+    ctx.close()
+
+
 def main():
     args = parse()
-    if args.impl == "reference":
+    if args.workload != "protein":
+        run_workload(args)
+    elif args.impl == "reference":
+        args.records = args.records or 1_000_000
         run_reference(args)
     else:
+        args.records = args.records or 1_000_000
         run_ours(args)
 
 

@@ -273,20 +273,27 @@ class Context:
         return t.value
 
     def poll(self, ticket: int, wait_ms: int = 0):
-        """None while the query runs; else a dict with the hits (record index,
-        score, query end, target end) and the latency in ms."""
+        """None while the query runs (after waiting up to wait_ms); else a dict
+        with the hits -- record indices ("hit_idx") and their "score", "qend"
+        and "tend" -- and "latency_ms" from submit to completion."""
         nh = C.c_uint32()
         lat = C.c_double()
-        rc = self._L.ish_gpu_poll(self._h, ticket, None, None, None, None, 0, C.byref(nh), C.byref(lat), wait_ms)
+        probe = np.zeros(1, np.uint32)
+        # capacity 0: the call reports the hit count and keeps the result
+        rc = self._L.ish_gpu_poll(self._h, ticket, _p(probe, C.c_uint32), None, None, None, 0, C.byref(nh),
+                                  C.byref(lat), wait_ms)
         if rc == EAGAIN:
             return None
+        k = nh.value
+        out = {"hit_idx": np.empty(k, np.uint32), "score": np.empty(k, np.int32), "qend": np.empty(k, np.int32),
+               "tend": np.empty(k, np.int32)}
+        if rc == EOVERFLOW:
+            rc = self._L.ish_gpu_poll(self._h, ticket, _p(out["hit_idx"], C.c_uint32), _p(out["score"], C.c_int32),
+                                      _p(out["qend"], C.c_int32), _p(out["tend"], C.c_int32), k, C.byref(nh),
+                                      C.byref(lat), 0)
         self._check(rc)
-        # the counts are known now; fetch the arrays (the result is kept until
-        # it is delivered in full)
-        return self._poll_full(ticket, nh.value, lat.value)
-
-    def _poll_full(self, ticket, nh, lat):
-        return {"n_hits": nh, "latency_ms": lat, "ticket": ticket}
+        out["latency_ms"] = lat.value
+        return out
 
     def serve_stop(self):
         self._check(self._L.ish_gpu_serve_stop(self._h))

@@ -1,0 +1,176 @@
+"""The serving loop: continuous batching against a resident record set.
+
+Queries submitted while others run are admitted at the next step and share
+the device with them.  Each query's result -- its hit list with the score and
+end coordinates of every hit -- must be exactly what the query gets alone
+(ish_gpu_score_set), whatever mix it ran in.
+"""
+import threading
+
+import numpy as np
+import pytest
+
+from ish_gb300 import native
+from ish_gb300.scoring import BLOSUM62, ScoringMatrix
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def ctx():
+    native.load(build_if_missing=True)
+    c = native.Context(0)
+    yield c
+    c.close()
+
+
+def protein_set(rng, n, queries, plant=0.03):
+    recs = []
+    for _ in range(n):
+        L = int(np.clip(rng.lognormal(np.log(350), 0.6), 30, 3000))
+        r = rng.integers(0, 20, L, dtype=np.uint8)
+        if rng.random() < plant:
+            q = queries[int(rng.integers(0, len(queries)))]
+            if len(q) <= L:
+                pos = int(rng.integers(0, L - len(q) + 1))
+                cp = q.copy()
+                mut = rng.random(len(cp)) < 0.15
+                cp[mut] = rng.integers(0, 20, int(mut.sum()), dtype=np.uint8)
+                r[pos:pos + len(cp)] = cp
+        recs.append(r)
+    recs.append(np.zeros(0, np.uint8))  # an empty record
+    return native.pack_records(recs)
+
+
+def make_queries(ctx, rng, lens, thr=0.4):
+    m = ScoringMatrix(BLOSUM62)
+    seqs, ids = [], []
+    for i, L in enumerate(lens):
+        q = rng.integers(0, 20, L, dtype=np.uint8)
+        algo = native.ALGO_LOCAL if i % 2 else native.ALGO_SEMI_GLOBAL
+        ends = 0 if algo == native.ALGO_LOCAL else (12 if i % 4 == 0 else 15)
+        ids.append(ctx.set_query(q, BLOSUM62, m.values, algo, 10, 1, ends, int(m.values[q, q].sum()), thr))
+        seqs.append(q)
+    return seqs, ids
+
+
+def alone(ctx, qid, sid):
+    r = ctx.score_set(qid, sid)
+    h = r["hit_idx"]
+    return {"hit_idx": h, "score": r["score"][h], "qend": r["qend"][h], "tend": r["tend"][h]}
+
+
+def same(a, b, label):
+    for k in ("hit_idx", "score", "qend", "tend"):
+        assert np.array_equal(np.asarray(a[k]), np.asarray(b[k])), f"{label}: {k} differs"
+
+
+def wait(ctx, ticket, timeout_s=120):
+    for _ in range(int(timeout_s * 10)):
+        r = ctx.poll(ticket, wait_ms=100)
+        if r is not None:
+            return r
+    raise AssertionError(f"ticket {ticket} did not finish in {timeout_s} s")
+
+
+def test_serving_results_equal_alone_under_concurrency(ctx):
+    rng = np.random.default_rng(51)
+    lens = [20, 45, 90, 150, 200, 260, 300, 333, 410, 500, 640, 777]
+    seqs, ids = make_queries(ctx, rng, lens)
+    buf, off = protein_set(rng, 6000, seqs)
+    sid = ctx.records_load(buf, off)
+    try:
+        expect = [alone(ctx, qid, sid) for qid in ids]
+        assert sum(len(e["hit_idx"]) for e in expect) > 0
+        ctx.serve_start(sid, max_active=16, mem_budget=0, chunks=8)
+        try:
+            # three client threads submit and poll concurrently
+            tickets = {}
+            results = {}
+            lock = threading.Lock()
+
+            def client(part):
+                mine = [(i, ctx.submit(ids[i])) for i in part]
+                with lock:
+                    tickets.update(dict(mine))
+                for i, t in mine:
+                    r = wait(ctx, t)
+                    with lock:
+                        results[i] = r
+
+            th = [threading.Thread(target=client, args=(list(range(k, len(ids), 3)),)) for k in range(3)]
+            for t in th:
+                t.start()
+            for t in th:
+                t.join()
+            assert len(results) == len(ids)
+            for i in range(len(ids)):
+                same(results[i], expect[i], f"query {i} (Q={lens[i]})")
+                assert results[i]["latency_ms"] > 0
+            # a second wave with duplicates, submitted while the first runs
+            t1 = [ctx.submit(ids[i]) for i in (3, 3, 7, 0)]
+            t2 = [ctx.submit(ids[i]) for i in (11, 3)]
+            for t, i in zip(t1 + t2, (3, 3, 7, 0, 11, 3)):
+                same(wait(ctx, t), expect[i], f"repeat of query {i}")
+            st = ctx.serve_stats()
+            assert st["completed"] == len(ids) + 6
+            assert st["max_active"] >= 2, st  # requests shared steps
+            assert st["cells"] > 0 and st["device_ms"] > 0
+        finally:
+            ctx.serve_stop()
+    finally:
+        ctx.records_free(sid)
+        for qid in ids:
+            ctx.free_query(qid)
+
+
+def test_serving_memory_budget_admits_one_at_a_time(ctx):
+    rng = np.random.default_rng(52)
+    seqs, ids = make_queries(ctx, rng, [60, 120, 240])
+    buf, off = protein_set(rng, 2000, seqs)
+    sid = ctx.records_load(buf, off)
+    try:
+        expect = [alone(ctx, qid, sid) for qid in ids]
+        ctx.serve_start(sid, max_active=8, mem_budget=1, chunks=4)  # room for one request's outputs
+        try:
+            ts = [ctx.submit(q) for q in ids]
+            for t, e, L in zip(ts, expect, (60, 120, 240)):
+                same(wait(ctx, t), e, f"Q={L}")
+            assert ctx.serve_stats()["max_active"] == 1
+        finally:
+            ctx.serve_stop()
+    finally:
+        ctx.records_free(sid)
+        for qid in ids:
+            ctx.free_query(qid)
+
+
+def test_serving_errors_stay_with_their_request(ctx):
+    rng = np.random.default_rng(53)
+    seqs, ids = make_queries(ctx, rng, [80, 0])
+    m = ScoringMatrix(BLOSUM62)
+    q = rng.integers(0, 20, 50, dtype=np.uint8)
+    bad = ctx.set_query(q, BLOSUM62, m.values, native.ALGO_SEMI_GLOBAL, 1, 1, 12, int(m.values[q, q].sum()), 0.5)
+    buf, off = protein_set(rng, 1500, seqs[:1])
+    sid = ctx.records_load(buf, off)
+    try:
+        expect = [alone(ctx, qid, sid) for qid in ids]
+        ctx.serve_start(sid, max_active=4, chunks=3)
+        try:
+            with pytest.raises(native.IshGpuError):
+                ctx.records_free(sid)  # in use by the serving loop
+            tb = ctx.submit(bad)  # gap_open == gap_extend: outside the exact fast regime
+            t0, t1 = ctx.submit(ids[0]), ctx.submit(ids[1])
+            with pytest.raises(native.IshGpuError) as ei:
+                wait(ctx, tb)
+            assert ei.value.code == native.EINVAL
+            same(wait(ctx, t0), expect[0], "good query next to a failing one")
+            same(wait(ctx, t1), expect[1], "empty query")
+            with pytest.raises(native.IshGpuError):
+                ctx.poll(t0)  # delivered once
+        finally:
+            ctx.serve_stop()
+    finally:
+        ctx.records_free(sid)
+        for qid in ids + [bad]:
+            ctx.free_query(qid)
