@@ -234,10 +234,12 @@ def run_ours(args):
     clocks.start()
     barrier(dist)
     dev_ms = []
+    launches0 = ctx.launch_count()
     t0 = time.perf_counter()
     for _ in range(args.steps):
         ms, res = step()
         dev_ms.append(ms)
+    launches = ctx.launch_count() - launches0
     wall_ms = 1e3 * (time.perf_counter() - t0) / args.steps
     barrier(dist)
     clk = clocks.stop()
@@ -331,7 +333,7 @@ def run_ours(args):
                     "d2h_bytes_per_step": d2h,
                     "latency_ms": {"p50": round(float(np.percentile(lat, 50)), 3),
                                    "p99": round(float(np.percentile(lat, 99)), 3)}},
-            "gpu_launches": 8 * args.steps,
+            "gpu_launches": launches,
             "clocks": clk,
             "plain_kernel_gcups": round(plain, 2) if plain else None,
             "wall_ms_per_step": round(wall_ms, 3),
@@ -495,9 +497,11 @@ def run_workload(args):
     clocks.start()
     barrier(dist)
     dev = []
+    launches0 = ctx.launch_count()
     for _ in range(args.steps):
         ms, res = step()
         dev.append(ms)
+    launches = ctx.launch_count() - launches0
     barrier(dist)
     clk = clocks.stop()
     step_ms = reduce_max(dist, float(np.mean(dev)))
@@ -559,7 +563,7 @@ def run_workload(args):
                     "h2d_bytes_per_step": int(len(wl.records) + 8 * len(wl.offsets)), "d2h_bytes_per_step": int(d2h),
                     "latency_ms": {"p50": round(float(np.percentile(e2e, 50)), 3),
                                    "p99": round(float(np.percentile(e2e, 99)), 3)}},
-            "gpu_launches": None, "clocks": clk, "hits": int(nh), **extra,
+            "gpu_launches": launches, "clocks": clk, "hits": int(nh), **extra,
         })
         print(json.dumps(line))
     ctx.close()
@@ -603,6 +607,7 @@ def run_serving(args, rank, world, local, dist):
     clocks = Clocks(local)
     clocks.start()
     total_cells = total_ms = 0.0
+    launches0 = ctx.launch_count()
     for rate in rates:
         qs = workloads.serving_queries(count=count, rate=rate)
         ids = []
@@ -640,6 +645,7 @@ def run_serving(args, rank, world, local, dist):
                          "device_gcups": round(st["cells"] / st["device_ms"] / 1e6, 1),
                          "max_active": st["max_active"], "steps": st["steps"]})
     clk = clocks.stop()
+    launches = ctx.launch_count() - launches0
     value = total_cells / (total_ms * 1e-3) / 1e9
     # the plain one-thread-per-record kernel, one query on a record sample
     sub = wl.subset(np.arange(0, wl.n, max(1, wl.n // 100_000)))
@@ -657,7 +663,7 @@ def run_serving(args, rank, world, local, dist):
                          "d2h_bytes_per_step": 0,
                          "latency_ms": {"p50": per_rate[-1]["p50_ms"], "p99": per_rate[-1]["p99_ms"]}},
                  "serving": per_rate, "plain_per_query_gcups": round(plain, 2),
-                 "gpu_launches": None, "clocks": clk})
+                 "gpu_launches": launches, "clocks": clk})
     if rank == 0:
         print(json.dumps(line))
     ctx.close()

@@ -162,6 +162,17 @@ ISH_API int ish_gpu_score_multi(ish_ctx *ctx, const int32_t *query_ids, uint32_t
 ISH_API int ish_gpu_autotune(ish_ctx *ctx, int32_t set_id, const int32_t *query_ids, uint32_t n_queries,
                              int32_t *group, int32_t *cols);
 
+/* Match starts of hits, computed on the device: for hit i (record hit_idx[i]
+ * of a resident set, forward target end target_end[i] as returned by the
+ * scoring calls) start[i] is the target start the CPU matcher reports, i.e.
+ * MatchResult(start, target_end + 1).  Replaces the per-hit CPU find_start of
+ * ishlib/cpu/process_batch.mojo:56-61 (StripedSemiGlobalMatcher.find_start,
+ * ishlib/matcher/striped_semi_global_matcher.mojo:259-276; the reverse pass of
+ * semi_global_aln_start_end, semi_global_aln/striped.mojo:160-191; for local
+ * alignment the reverse sw of ssw_align, local_aln/striped.mojo:232-259). */
+ISH_API int ish_gpu_match_starts(ish_ctx *ctx, int32_t query_id, int32_t set_id, const uint32_t *hit_idx,
+                                 const int32_t *target_end, uint32_t n_hits, int64_t *start);
+
 /* ---- serving loop: continuous batching against a resident set ----
  * Replaces the reference's synchronous per-batch device round trip
  * (ishlib/gpu/process_batch.mojo:27-163 driving SearcherDevice,
@@ -231,6 +242,11 @@ ISH_API int ish_gpu_last_kernel_ms(ish_ctx *ctx, double *ms);
  * integer cell-update roofline of the engine is derived from it.  No
  * counterpart in the reference: measurement support for the engine. */
 ISH_API int ish_gpu_calibrate(ish_ctx *ctx, double *dpx_ops_per_s);
+
+/* Number of CUDA kernels the library has launched on this context (a batched
+ * launch counts the kernel nodes of its graph).  No counterpart in the
+ * reference: measurement support. */
+ISH_API int ish_gpu_launch_count(ish_ctx *ctx, uint64_t *count);
 
 #ifdef __cplusplus
 }

@@ -5,8 +5,10 @@
 
 #include <cuda_runtime.h>
 
+#include <atomic>
 #include <cstdint>
 #include <map>
+#include <memory>
 #include <string>
 #include <vector>
 
@@ -55,7 +57,26 @@ struct Query {
   DevBuf plain_prof, plain_hinit;
   bool plain_ready = false;
   std::map<long, WaveLayout> layouts;
+  std::unique_ptr<Query> reverse;  // reversed query with swapped free ends (start finding)
 };
+
+// Parameters and sequence of a query without its device state.
+inline void clone_params(const Query &src, Query &dst) {
+  dst.algo = src.algo;
+  dst.kind = src.kind;
+  dst.alphabet = src.alphabet;
+  dst.Q = src.Q;
+  dst.open = src.open;
+  dst.ext = src.ext;
+  dst.ends = src.ends;
+  dst.max_score = src.max_score;
+  dst.thr = src.thr;
+  dst.M = src.M;
+  dst.q = src.q;
+  dst.mmin = src.mmin;
+  dst.mmax = src.mmax;
+  dst.neg_limit = src.neg_limit;
+}
 
 struct RecordSet {
   uint32_t n = 0;
@@ -65,6 +86,7 @@ struct RecordSet {
   std::vector<uint32_t> hist;  // length-bucket histogram (host copy)
   uint32_t n_empty = 0;
   uint32_t max_code = 0;       // largest record code in the set
+  DevBuf inv;                  // sorted entry of each original record (built on first use)
 };
 
 struct Regime {
@@ -105,6 +127,9 @@ struct ish_ctx {
   std::map<uint64_t, ish::host::Tuned> tuned;
   // the serving loop (serve.cu), if started
   ish::host::Server *server = nullptr;
+  // kernels launched by the library on this context (graph replays count
+  // their kernel nodes; the serving thread adds its own)
+  std::atomic<uint64_t> launches{0};
 };
 
 
@@ -125,6 +150,8 @@ extern thread_local std::string g_open_error;
 inline uint32_t ceil_div(uint64_t a, uint64_t b) { return (uint32_t)((a + b - 1) / b); }
 
 Regime regime(const Query &q, int qpad);
+void release_query(Query &q);
+void release_set(RecordSet &rs);
 int wave_k_available(int k);
 // Shape of the wavefront kernel for a query: the autotuner's choice when one
 // exists, else the cost model; forced options override both.

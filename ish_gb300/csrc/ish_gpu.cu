@@ -35,6 +35,23 @@ int fail(ish_ctx *c, int code, const char *fmt, ...) {
   return code;
 }
 
+void release_query(Query &q) {
+  q.plain_prof.release();
+  q.plain_hinit.release();
+  for (auto &l : q.layouts) {
+    l.second.prof.release();
+    l.second.hinit.release();
+  }
+  q.layouts.clear();
+  if (q.reverse) release_query(*q.reverse);
+  q.reverse.reset();
+}
+
+void release_set(RecordSet &rs) {
+  DevBuf *b[] = {&rs.codes, &rs.off_s, &rs.len_s, &rs.orig_s, &rs.inv};
+  for (DevBuf *x : b) x->release();
+}
+
 int matrix_alphabet_ok(uint32_t alphabet) { return alphabet >= 1 && alphabet <= 256; }
 
 // Safe-regime checks (see engine.cuh): the fast kernels evaluate plain Gotoh
@@ -241,26 +258,32 @@ int load_records(ish_ctx *ctx, const uint8_t *records, const uint64_t *offsets, 
   const uint32_t nb = std::min<uint32_t>(ceil_div(n, 256), (uint32_t)ctx->num_sms * 16);
   k_lengths<<<nb, 256, 0, s>>>(ctx->off_in.as<uint64_t>(), n, ctx->len_tmp.as<uint32_t>(), ctx->slot_tmp.as<uint64_t>(),
                                 ctx->hist.as<uint32_t>());
+  ++ctx->launches;
   // exclusive scan of slot sizes -> packed offsets
   const uint32_t tiles = ceil_div(n, SCAN_TILE);
   CU(ctx->scan_tmp.ensure((size_t)(tiles + 1) * 8 * 2));
   uint64_t *bsum = ctx->scan_tmp.as<uint64_t>();
   uint64_t *boff = bsum + tiles + 1;
   k_scan64_block<<<tiles, 1024, 0, s>>>(ctx->slot_tmp.as<uint64_t>(), ctx->poff_tmp.as<uint64_t>(), n, bsum);
+  ++ctx->launches;
   if (tiles > 1) {
     if (tiles > SCAN_TILE) return fail(ctx, ISH_EINVAL, "too many records in one set (%u)", n);
     k_scan64_block<<<1, 1024, 0, s>>>(bsum, boff, tiles, nullptr);
+    ++ctx->launches;
     k_scan64_add<<<tiles, 1024, 0, s>>>(ctx->poff_tmp.as<uint64_t>(), n, boff);
+    ++ctx->launches;
   }
   // host copy of the histogram, then turn it into descending bucket cursors
   rs.hist.assign(NBUCKETS, 0);
   CU(cudaMemcpyAsync(rs.hist.data(), ctx->hist.p, (size_t)NBUCKETS * 4, cudaMemcpyDeviceToHost, s));
   k_bucket_scan<<<1, 1024, 0, s>>>(ctx->hist.as<uint32_t>());
+  ++ctx->launches;
   CU(rs.len_s.ensure((size_t)n * 4));
   CU(rs.off_s.ensure((size_t)n * 8));
   CU(rs.orig_s.ensure((size_t)n * 4));
   k_scatter<<<nb, 256, 0, s>>>(ctx->len_tmp.as<uint32_t>(), ctx->poff_tmp.as<uint64_t>(), n, ctx->hist.as<uint32_t>(),
                                rs.len_s.as<uint32_t>(), rs.off_s.as<uint64_t>(), rs.orig_s.as<uint32_t>());
+  ++ctx->launches;
   const uint64_t packed = bytes + 16ull * n + 16;
   CU(rs.codes.ensure(packed));
   const uint32_t pb = std::min<uint32_t>(ceil_div((uint64_t)n * 32, 256), (uint32_t)ctx->num_sms * 32);
@@ -268,6 +291,7 @@ int load_records(ish_ctx *ctx, const uint8_t *records, const uint64_t *offsets, 
   CU(cudaMemsetAsync(ctx->max_code.p, 0, 4, s));
   k_pack<<<pb, 256, 0, s>>>(ctx->raw.as<uint8_t>(), bytes, ctx->off_in.as<uint64_t>(), ctx->poff_tmp.as<uint64_t>(), n,
                             rs.codes.as<uint8_t>(), ctx->max_code.as<uint32_t>());
+  ++ctx->launches;
   CU(cudaGetLastError());
   CU(cudaMemcpyAsync(&rs.max_code, ctx->max_code.p, 4, cudaMemcpyDeviceToHost, s));
   CU(cudaStreamSynchronize(s));
@@ -368,6 +392,7 @@ int launch_wave_range(ish_ctx *ctx, Query &q, RecordSet &rs, uint32_t first, uin
   p.max_steps = rs.total + 2ull * count + 1024;
   CU(cudaMemsetAsync(ctx->counter.p, 0, 4, s));
   fn<<<grid, threads, smem, s>>>(p);
+  ++ctx->launches;
   CU(cudaGetLastError());
   return ISH_OK;
 }
@@ -404,6 +429,7 @@ int launch_plain(ish_ctx *ctx, Query &q, RecordSet &rs, uint32_t first, uint32_t
   PlainFn fn = plain_fn(q.algo == ISH_ALGO_LOCAL ? SW : SG);
   CU(cudaFuncSetAttribute((const void *)fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)std::max<size_t>(smem, 1)));
   fn<<<blocks, threads, smem, ctx->stream>>>(p);
+  ++ctx->launches;
   CU(cudaGetLastError());
   return ISH_OK;
 }
@@ -460,6 +486,7 @@ int run_scoring(ish_ctx *ctx, Query &q, RecordSet &rs) {
         RecordsDev{rs.codes.as<const uint8_t>(), rs.off_s.as<const uint64_t>(), rs.len_s.as<const uint32_t>(),
                    rs.orig_s.as<const uint32_t>(), rs.n},
         nonempty, n_empty, mode, q.Q, out, Decision{q.max_score, q.thr});
+    ++ctx->launches;
     CU(cudaGetLastError());
   }
   if (nonempty) {
@@ -487,9 +514,12 @@ int fetch_outputs(ish_ctx *ctx, uint32_t n, int32_t *score, int32_t *qend, int32
     CU(ctx->hit_idx.ensure((size_t)n * 4 + 4));
     CU(ctx->nhits.ensure(16));
     k_count_hits<<<nb, 1024, 0, s>>>(ctx->out_hit.as<uint8_t>(), n, ctx->block_counts.as<uint32_t>());
+    ++ctx->launches;
     k_scan_counts<<<1, 1024, 0, s>>>(ctx->block_counts.as<uint32_t>(), nb, ctx->nhits.as<uint32_t>());
+    ++ctx->launches;
     k_write_hits<<<nb, 1024, 0, s>>>(ctx->out_hit.as<uint8_t>(), n, ctx->block_counts.as<uint32_t>(),
                                      ctx->hit_idx.as<uint32_t>());
+    ++ctx->launches;
     CU(cudaGetLastError());
   }
   CU(cudaEventRecord(ctx->ev1, s));
@@ -553,20 +583,8 @@ void ish_gpu_close(ish_ctx *ctx) {
   stop_server(ctx);
   cudaStreamSynchronize(ctx->stream);
   free_plans(ctx);
-  for (auto &kv : ctx->queries) {
-    kv.second.plain_prof.release();
-    kv.second.plain_hinit.release();
-    for (auto &l : kv.second.layouts) {
-      l.second.prof.release();
-      l.second.hinit.release();
-    }
-  }
-  for (auto &kv : ctx->sets) {
-    kv.second.codes.release();
-    kv.second.off_s.release();
-    kv.second.len_s.release();
-    kv.second.orig_s.release();
-  }
+  for (auto &kv : ctx->queries) release_query(kv.second);
+  for (auto &kv : ctx->sets) release_set(kv.second);
   DevBuf *bufs[] = {&ctx->raw, &ctx->off_in, &ctx->len_tmp, &ctx->slot_tmp, &ctx->poff_tmp, &ctx->hist, &ctx->max_code,
                     &ctx->scan_tmp, &ctx->counter, &ctx->error, &ctx->out_score, &ctx->out_qend, &ctx->out_tend,
                     &ctx->out_hit, &ctx->hit_idx, &ctx->block_counts, &ctx->nhits, &ctx->plain_scratch};
@@ -663,12 +681,7 @@ int ish_gpu_free_query(ish_ctx *ctx, int32_t query_id) {
   if (it == ctx->queries.end()) return fail(ctx, ISH_EINVAL, "unknown query %d", query_id);
   cudaStreamSynchronize(ctx->stream);
   drop_plans(ctx, query_id, 0);
-  it->second.plain_prof.release();
-  it->second.plain_hinit.release();
-  for (auto &l : it->second.layouts) {
-    l.second.prof.release();
-    l.second.hinit.release();
-  }
+  release_query(it->second);
   ctx->queries.erase(it);
   return ISH_OK;
 }
@@ -679,10 +692,7 @@ int ish_gpu_records_load(ish_ctx *ctx, const uint8_t *records, const uint64_t *o
   RecordSet rs;
   int rc = load_records(ctx, records, offsets, n, rs);
   if (rc) {
-    rs.codes.release();
-    rs.off_s.release();
-    rs.len_s.release();
-    rs.orig_s.release();
+    release_set(rs);
     return rc;
   }
   const int32_t id = ctx->next_set++;
@@ -698,10 +708,7 @@ int ish_gpu_records_free(ish_ctx *ctx, int32_t set_id) {
   if (server_uses_set(ctx, set_id)) return fail(ctx, ISH_EINVAL, "record set %d is used by the serving loop", set_id);
   cudaStreamSynchronize(ctx->stream);
   drop_plans(ctx, 0, set_id);
-  it->second.codes.release();
-  it->second.off_s.release();
-  it->second.len_s.release();
-  it->second.orig_s.release();
+  release_set(it->second);
   ctx->sets.erase(it);
   return ISH_OK;
 }
@@ -743,10 +750,7 @@ int ish_gpu_score(ish_ctx *ctx, int32_t query_id, const uint8_t *records, const 
   if (!rc) rc = run_scoring(ctx, qi->second, rs);
   if (!rc) rc = fetch_outputs(ctx, n, score, query_end, target_end, hit, hit_idx, n_hits);
   cudaStreamSynchronize(ctx->stream);
-  rs.codes.release();
-  rs.off_s.release();
-  rs.len_s.release();
-  rs.orig_s.release();
+  release_set(rs);
   return rc;
 }
 
@@ -758,13 +762,21 @@ int ish_gpu_calibrate(ish_ctx *ctx, double *dpx_ops_per_s) {
   cudaStream_t s = ctx->stream;
   k_dpx_peak<<<blocks, threads, 0, s>>>(ctx->counter.as<uint32_t>(), 256, 0x00010001u, 0xfffbfffbu);  // warm-up
   CU(cudaEventRecord(ctx->ev0, s));
+  ++ctx->launches;
   k_dpx_peak<<<blocks, threads, 0, s>>>(ctx->counter.as<uint32_t>(), iters, 0x00010001u, 0xfffbfffbu);
+  ++ctx->launches;
   CU(cudaEventRecord(ctx->ev1, s));
   CU(cudaGetLastError());
   CU(cudaStreamSynchronize(s));
   float ms = 0.f;
   CU(cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1));
   *dpx_ops_per_s = (double)blocks * threads * iters * 8 / (ms * 1e-3);
+  return ISH_OK;
+}
+
+int ish_gpu_launch_count(ish_ctx *ctx, uint64_t *count) {
+  if (!ctx || !count) return ISH_EINVAL;
+  *count = ctx->launches.load();
   return ISH_OK;
 }
 

@@ -33,6 +33,7 @@ struct MultiPlan {
   int32_t set_id = 0;
   unsigned want = 0;
   uint32_t n = 0, nq = 0, nb = 0, n_counters = 0;
+  uint32_t kernels = 0;  // kernel nodes of the graph
   std::vector<MultiClass> classes;
   DevBuf counters, score, qend, tend, hit, block_counts, hit_idx, nhits;
   std::vector<cudaStream_t> side;
@@ -224,6 +225,7 @@ int enqueue_plan(ish_ctx *ctx, MultiPlan &P, RecordSet &rs, cudaStream_t s) {
     b.prof_area = c.prof_area;
     b.slot_words = (uint32_t)((c.threads / c.Gmin) * 32);
     if (c.ntiles) c.fn<<<c.grid, c.threads, c.smem, cs>>>(b);
+    if (c.ntiles) ++P.kernels;
     CU(cudaGetLastError());
     if (i > 0) {
       CU(cudaEventRecord(P.events[i], cs));
@@ -243,13 +245,17 @@ int enqueue_plan(ish_ctx *ctx, MultiPlan &P, RecordSet &rs, cudaStream_t s) {
                (P.want & (W_HIT | W_COMPACT)) ? P.hit.as<uint8_t>() + (size_t)i * n : nullptr};
     k_trivial<<<std::max<uint32_t>(1, std::min<uint32_t>(ceil_div(n_empty, 256), 1024)), 256, 0, s>>>(
         rec, n - n_empty, n_empty, q.algo == ISH_ALGO_LOCAL ? SW : SG, q.Q, out, Decision{q.max_score, q.thr});
+    ++P.kernels;
     CU(cudaGetLastError());
   }
   if (P.want & W_COMPACT) {
     const dim3 g(P.nb, P.nq);
     k_count_hits<<<g, 1024, 0, s>>>(P.hit.as<uint8_t>(), n, P.block_counts.as<uint32_t>());
+    ++P.kernels;
     k_scan_counts<<<1, 1024, 0, s>>>(P.block_counts.as<uint32_t>(), P.nb * P.nq, P.nhits.as<uint32_t>());
+    ++P.kernels;
     k_write_hits<<<g, 1024, 0, s>>>(P.hit.as<uint8_t>(), n, P.block_counts.as<uint32_t>(), P.hit_idx.as<uint32_t>());
+    ++P.kernels;
     CU(cudaGetLastError());
   }
   return ISH_OK;
@@ -346,6 +352,7 @@ int ish_gpu_score_multi(ish_ctx *ctx, const int32_t *query_ids, uint32_t n_queri
   cudaStream_t s = ctx->stream;
   CU(cudaEventRecord(ctx->ev0, s));
   CU(cudaGraphLaunch(P->exec, s));
+  ctx->launches += P->kernels;
   CU(cudaEventRecord(ctx->ev1, s));
   const size_t total = (size_t)n_queries * n;
   if (score) CU(cudaMemcpyAsync(score, P->score.p, total * 4, cudaMemcpyDeviceToHost, s));

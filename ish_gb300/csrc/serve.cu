@@ -96,23 +96,6 @@ namespace {
 
 inline uint64_t bucket_len(uint32_t b) { return b < 32768 ? b : 32768 + ((uint64_t)(b - 32768) << 5) + 31; }
 
-void clone_params(const Query &src, Query &dst) {
-  dst.algo = src.algo;
-  dst.kind = src.kind;
-  dst.alphabet = src.alphabet;
-  dst.Q = src.Q;
-  dst.open = src.open;
-  dst.ext = src.ext;
-  dst.ends = src.ends;
-  dst.max_score = src.max_score;
-  dst.thr = src.thr;
-  dst.M = src.M;
-  dst.q = src.q;
-  dst.mmin = src.mmin;
-  dst.mmax = src.mmax;
-  dst.neg_limit = src.neg_limit;
-}
-
 void free_layouts(Query &q) {
   for (auto &l : q.layouts) {
     l.second.prof.release();
@@ -323,6 +306,7 @@ int step(Server &S, char *msg) {
       cudaStream_t cs = c == 0 ? s : S.side[c - 1];
       if (c > 0) SCU(cudaStreamWaitEvent(cs, S.fork, 0));
       fn<<<per_sm * S.ctx->num_sms, threads, smem, cs>>>(b);
+      ++S.ctx->launches;
       SCU(cudaGetLastError());
       if (c > 0) {
         SCU(cudaEventRecord(S.join[c - 1], cs));
@@ -343,16 +327,21 @@ int step(Server &S, char *msg) {
     if (n_empty) {
       k_trivial<<<std::max<uint32_t>(1, std::min<uint32_t>(ceil_div(n_empty, 256), 1024)), 256, 0, s>>>(
           rec, n - n_empty, n_empty, r->mode, r->q.Q, out, Decision{r->q.max_score, r->q.thr});
+      ++S.ctx->launches;
     }
     const uint32_t nb = std::max<uint32_t>(1, ceil_div(n, HIT_TILE));
     if (n) {
       k_count_hits<<<nb, 1024, 0, s>>>(b.hit.as<uint8_t>(), n, b.counts.as<uint32_t>());
+      ++S.ctx->launches;
       k_scan_counts<<<1, 1024, 0, s>>>(b.counts.as<uint32_t>(), nb, b.nhits.as<uint32_t>());
+      ++S.ctx->launches;
       k_write_hits<<<nb, 1024, 0, s>>>(b.hit.as<uint8_t>(), n, b.counts.as<uint32_t>(), b.idx.as<uint32_t>());
+      ++S.ctx->launches;
       k_gather_hits<<<S.ctx->num_sms * 4, 256, 0, s>>>(b.idx.as<uint32_t>(), b.nhits.as<uint32_t>(),
                                                       b.score.as<int32_t>(), b.qend.as<int32_t>(),
                                                       b.tend.as<int32_t>(), b.hs.as<int32_t>(), b.hq.as<int32_t>(),
                                                       b.ht.as<int32_t>());
+      ++S.ctx->launches;
       SCU(cudaGetLastError());
       SCU(cudaMemcpyAsync(&S.h_nhits[done.size()], b.nhits.p, 4, cudaMemcpyDeviceToHost, s));
     } else {

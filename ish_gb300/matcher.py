@@ -51,6 +51,13 @@ class BatchResult:
     target_end: np.ndarray  # int32: 0-based inclusive (-1: no alignment)
     hit: np.ndarray         # uint8: 1 iff the CPU matcher's first_match would match
     hit_idx: np.ndarray     # uint32: indices of the hits, ascending
+    hit_start: np.ndarray | None = None  # int64 per hit: first_match's MatchResult.start (device reverse pass)
+
+    def matches(self):
+        """(record index, start, end) per hit: first_match's MatchResult(start, end)
+        as ishlib/cpu/process_batch.mojo:56-66 builds it for GPU hits."""
+        starts = self.hit_start if self.hit_start is not None else np.full(len(self.hit_idx), -1, np.int64)
+        return [(int(i), int(s), int(self.target_end[i]) + 1) for i, s in zip(self.hit_idx, starts)]
 
 
 class _GpuMatcherBase:
@@ -94,16 +101,26 @@ class _GpuMatcherBase:
         return self.matrix.decode(codes)
 
     # batch scoring on the GPU
-    def batch_match(self, records, offsets=None) -> BatchResult:
-        """Score encoded records: a list of arrays, or (concatenated bytes, offsets)."""
+    def batch_match(self, records, offsets=None, starts: bool = True) -> BatchResult:
+        """Score encoded records: a list of arrays, or (concatenated bytes, offsets).
+        With `starts`, the match start of every hit is found on the device too."""
         if offsets is None:
             records, offsets = native.pack_records(records)
-        r = self.ctx.score(self.query_id, records, offsets)
-        return BatchResult(r["score"], r["qend"], r["tend"], r["hit"], r["hit_idx"])
+        if not starts:
+            r = self.ctx.score(self.query_id, records, offsets)
+            return BatchResult(r["score"], r["qend"], r["tend"], r["hit"], r["hit_idx"])
+        sid = self.ctx.records_load(records, offsets)
+        try:
+            return self.batch_match_resident(sid, starts=True)
+        finally:
+            self.ctx.records_free(sid)
 
-    def batch_match_resident(self, set_id: int) -> BatchResult:
+    def batch_match_resident(self, set_id: int, starts: bool = True) -> BatchResult:
         r = self.ctx.score_set(self.query_id, set_id)
-        return BatchResult(r["score"], r["qend"], r["tend"], r["hit"], r["hit_idx"])
+        hs = None
+        if starts:
+            hs = self.ctx.match_starts(self.query_id, set_id, r["hit_idx"], r["tend"][r["hit_idx"]])
+        return BatchResult(r["score"], r["qend"], r["tend"], r["hit"], r["hit_idx"], hs)
 
 
 class StripedSemiGlobalMatcher(_GpuMatcherBase):

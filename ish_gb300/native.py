@@ -24,7 +24,8 @@ EXPORTS = (
     "ish_gpu_set_query", "ish_gpu_free_query", "ish_gpu_score", "ish_gpu_records_load", "ish_gpu_records_free",
     "ish_gpu_records_info", "ish_gpu_score_set", "ish_gpu_last_kernel_ms", "ish_gpu_calibrate",
     "ish_gpu_score_noalloc", "ish_gpu_score_multi", "ish_gpu_autotune", "ish_gpu_serve_start", "ish_gpu_submit",
-    "ish_gpu_poll", "ish_gpu_serve_stop", "ish_gpu_serve_stats",
+    "ish_gpu_poll", "ish_gpu_serve_stop", "ish_gpu_serve_stats", "ish_gpu_match_starts",
+    "ish_gpu_launch_count",
 )
 
 
@@ -85,6 +86,8 @@ def load(build_if_missing: bool = False):
                                         vp, C.c_char_p, C.c_size_t]
     L.ish_gpu_score_multi.argtypes = [vp, i32p, C.c_uint32, C.c_int32, i32p, i32p, i32p, u8p, u32p, C.c_uint64, u64p]
     L.ish_gpu_autotune.argtypes = [vp, C.c_int32, i32p, C.c_uint32, i32p, i32p]
+    L.ish_gpu_launch_count.argtypes = [vp, u64p]
+    L.ish_gpu_match_starts.argtypes = [vp, C.c_int32, C.c_int32, u32p, i32p, C.c_uint32, C.POINTER(C.c_int64)]
     L.ish_gpu_serve_start.argtypes = [vp, C.c_int32, C.c_uint32, C.c_uint64, C.c_uint32]
     L.ish_gpu_submit.argtypes = [vp, C.c_int32, u64p]
     L.ish_gpu_poll.argtypes = [vp, C.c_uint64, u32p, i32p, i32p, i32p, C.c_uint32, u32p, C.POINTER(C.c_double),
@@ -263,6 +266,15 @@ class Context:
                                              _p(k, C.c_int32)))
         return g[: len(q)], k[: len(q)]
 
+    def match_starts(self, qid: int, sid: int, hit_idx, target_end) -> np.ndarray:
+        """Target starts of hits (device reverse pass): MatchResult(start, end + 1)."""
+        h = np.ascontiguousarray(hit_idx, np.uint32)
+        e = np.ascontiguousarray(target_end, np.int32)
+        out = np.empty(max(len(h), 1), np.int64)
+        self._check(self._L.ish_gpu_match_starts(self._h, qid, sid, _p(h, C.c_uint32), _p(e, C.c_int32), len(h),
+                                                 _p(out, C.c_int64)))
+        return out[: len(h)]
+
     # ---- serving loop ----
     def serve_start(self, sid: int, max_active: int = 64, mem_budget: int = 0, chunks: int = 8):
         self._check(self._L.ish_gpu_serve_start(self._h, sid, max_active, mem_budget, chunks))
@@ -312,6 +324,12 @@ class Context:
         r = C.c_double()
         self._check(self._L.ish_gpu_calibrate(self._h, C.byref(r)))
         return r.value
+
+    def launch_count(self) -> int:
+        """CUDA kernels the library has launched on this context."""
+        c = C.c_uint64()
+        self._check(self._L.ish_gpu_launch_count(self._h, C.byref(c)))
+        return c.value
 
     def last_kernel_ms(self) -> float:
         ms = C.c_double()

@@ -352,8 +352,9 @@ int ish_o_sg_start_end_i16(const uint8_t *rec, int T, int Q, int open, int ext, 
                            float cutoff, ish_o_start_end *out) {
     ish_o_end fwd = ish_o_sg_aln_i16(rec, T, Q, open, ext, prof, W, max_s, min_s, ends);
     if ((float)fwd.score < cutoff) return 0; /* 157-158 */
-    int rlen = fwd.reference + 1;            /* reference[0 : end + 1] */
+    int rlen = fwd.reference + 1;            /* reference[0 : end + 1]; the slice clamps to T */
     if (rlen < 0) rlen = 0;
+    if (rlen > T) rlen = T;
     uint8_t *rev = (uint8_t *)malloc(rlen > 0 ? (size_t)rlen : 1);
     for (int i = 0; i < rlen; i++) rev[i] = rec[rlen - 1 - i];
     /* swapped free ends (178-182) */
