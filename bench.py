@@ -515,7 +515,8 @@ def run_workload(args):
             ctx.score_set(qid, sid, want=("hit_idx",))
             per.append(ctx.last_kernel_ms())
         extra["per_query_wave_launches_gcups"] = round(cells / (sum(per) * 1e-3) / 1e9, 2)
-    n_plain = min(wl.n, 200_000 if name == "batched" else (wl.n if name == "line" else 200))
+    # (one thread per record: on 10 kb-1 Mb records a few records already take seconds)
+    n_plain = min(wl.n, 200_000 if name == "batched" else (wl.n if name == "line" else 24))
     sub = wl.subset(np.arange(n_plain))
     sid2 = ctx.records_load(sub.records, sub.offsets)
     ctx.set_option(native.OPT_KERNEL, native.KERNEL_PLAIN)

@@ -77,6 +77,7 @@ extern "C" {
 #define ISH_OPT_SW_U16_LANES 4 /* uint16 lanes of the local word pass (default 8) */
 #define ISH_OPT_WAVE_GROUP 5  /* force threads per record pair (0 = autotuned) */
 #define ISH_OPT_WAVE_K 6      /* force query columns per thread (0 = autotuned) */
+#define ISH_OPT_PROFILE_LAYOUT 7 /* force the profile layout: -1 auto, 0 16-bit, 1 pair, 2 32-bit */
 
 typedef struct ish_ctx ish_ctx;
 

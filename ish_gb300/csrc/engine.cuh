@@ -23,6 +23,16 @@ enum Mode : int { SG = 0, SW = 1 };
 // added to it.
 constexpr int NEG_BIG = -20000;
 
+// Layouts of the wavefront profile in shared memory (for code c, thread t
+// and the thread's column j):
+//   PROF_S16:  16-bit scores, [c][t][j]; a record pair's word is assembled
+//              with one PRMT per column (large alphabets x long queries);
+//   PROF_PAIR: packed 32-bit words for every (code A, code B) pair,
+//              [cA][cB][t][j] (small alphabets);
+//   PROF_S32:  32-bit words with the score in the low half, [c][t][j]; the
+//              pair's word is one IMAD (the default).
+enum ProfLayout : int { PROF_S16 = 0, PROF_PAIR = 1, PROF_S32 = 2 };
+
 // Control word of the wavefront pipeline (one per row step).
 constexpr uint32_t CTL_NEW = 1u << 16;   // row 0 of a new record pair
 constexpr uint32_t CTL_IDLE = 1u << 17;  // no work in this slot
@@ -56,7 +66,8 @@ struct WaveParams {
   uint32_t prof_bytes;     // bytes copied into shared memory
   int Q, G, K, d, kp;      // query length, threads per group, columns per thread, front padding, profile stride
   int alphabet;
-  int pair_prof;           // 1: 32-bit pair-code profile, 0: 16-bit single-code profile
+  int layout;              // PROF_S16, PROF_PAIR or PROF_S32 (see below)
+  uint32_t lane_mul;       // 65536: b * lane_mul + a packs two PROF_S32 words
   int open, ext, ends;
   int neg_limit;           // v_neg_limit of the reference (semi_global_aln/striped.mojo:329-334)
   int hleft, fin;          // left boundary value and F entering the padding

@@ -41,7 +41,7 @@ struct DevBuf {
 };
 
 struct WaveLayout {
-  int G = 0, K = 0, d = 0, kp = 0, pair = 0;
+  int G = 0, K = 0, d = 0, kp = 0, layout = 0;
   uint32_t prof_bytes = 0;
   DevBuf prof, hinit;
 };
@@ -97,7 +97,7 @@ struct Regime {
 struct MultiPlan;  // multi.cu
 struct Server;     // serve.cu
 struct Tuned {
-  int G = 0, K = 0, pair = -1;  // pair: -1 = layout rule, 0 / 1 forced
+  int G = 0, K = 0, layout = -1;  // layout: -1 = the layout rule (choose_layout), else forced
 };
 
 }  // namespace host
@@ -111,7 +111,7 @@ struct ish_ctx {
   std::string err;
   int kernel = ISH_KERNEL_AUTO;
   int sg_lanes = 8, sw_u8_lanes = 16, sw_u16_lanes = 8;
-  int force_G = 0, force_K = 0;
+  int force_G = 0, force_K = 0, force_layout = -1;
   std::map<int32_t, ish::host::Query> queries;
   int32_t next_query = 1;
   std::map<int32_t, ish::host::RecordSet> sets;
@@ -155,11 +155,13 @@ void release_set(RecordSet &rs);
 int wave_k_available(int k);
 // Shape of the wavefront kernel for a query: the autotuner's choice when one
 // exists, else the cost model; forced options override both.
-void pick_shape(ish_ctx *ctx, const Query &q, int *G, int *K, int *pair);
+void pick_shape(ish_ctx *ctx, const Query &q, int *G, int *K, int *layout);
 void choose_shape(int Q, int force_G, int force_K, int *G, int *K);
 uint64_t tune_key(int mode, int alphabet, int Q);
-int pair_layout_fits(int alphabet, int G, int K);
-int build_wave_layout(ish_ctx *ctx, Query &q, int G, int K, int pair, WaveLayout **out);
+int layout_stride(int layout, int K);
+size_t layout_bytes(int layout, int alphabet, int G, int K);
+int choose_layout(int alphabet, int G, int K, int mode);
+int build_wave_layout(ish_ctx *ctx, Query &q, int G, int K, int layout, WaveLayout **out);
 int load_records(ish_ctx *ctx, const uint8_t *records, const uint64_t *offsets, uint32_t n, RecordSet &rs);
 uint32_t count_longer(const RecordSet &rs, uint64_t len);
 // Checks that query q may run on the wavefront kernels against set rs with
@@ -170,7 +172,7 @@ int check_fast(ish_ctx *ctx, const Query &q, const RecordSet &rs);
 // Fills the per-query part of the wavefront parameters (not first/count/counter).
 void wave_params(const Query &q, const WaveLayout &L, const RecordSet &rs, OutDev out, int *error, WaveParams *p);
 int launch_wave_range(ish_ctx *ctx, Query &q, RecordSet &rs, uint32_t first, uint32_t count, OutDev out, int G, int K,
-                      int pair, cudaStream_t s);
+                      int layout, cudaStream_t s);
 void drop_plans(ish_ctx *ctx, int32_t query_id, int32_t set_id);  // multi.cu
 void free_plans(ish_ctx *ctx);                                   // multi.cu
 void stop_server(ish_ctx *ctx);                                  // serve.cu

@@ -121,28 +121,50 @@ void choose_shape(int Q, int force_G, int force_K, int *G, int *K) {
 
 uint64_t tune_key(int mode, int alphabet, int Q) { return ((uint64_t)mode << 48) | ((uint64_t)alphabet << 32) | (uint32_t)Q; }
 
-// The 32-bit pair profile (one load per column for both records) when it is
-// small enough to stay cheap in shared memory, else the 16-bit single-code one.
-int pair_layout_fits(int alphabet, int G, int K) {
-  return alphabet * alphabet * G * (((K + 3) & ~3) + 4) * 4 <= 64 * 1024;
+// Row stride (in words) of a profile layout.  Strides are an odd number of
+// 16-byte units: the eight threads of a quarter-warp read consecutive rows
+// with 16-byte loads, and an odd stride spreads them over all 32 banks.
+int layout_stride(int layout, int K) {
+  if (layout == PROF_S16) {
+    int kp = (K + 7) & ~7;
+    return ((kp / 8) & 1) ? kp : kp + 8;
+  }
+  int kp = (K + 3) & ~3;
+  return ((kp / 4) & 1) ? kp : kp + 4;
 }
 
-void pick_shape(ish_ctx *ctx, const Query &q, int *G, int *K, int *pair) {
+size_t layout_bytes(int layout, int alphabet, int G, int K) {
+  const size_t kp = (size_t)layout_stride(layout, K);
+  if (layout == PROF_PAIR) return (size_t)alphabet * alphabet * G * kp * 4;
+  if (layout == PROF_S32) return (size_t)alphabet * G * kp * 4;
+  return (size_t)alphabet * G * kp * 2;
+}
+
+// The pair layout (no per-column work to assemble a record pair's word) when
+// it takes at most 64 KB; else 32-bit single-code words (one IMAD per column)
+// when a block still fits twice on an SM; else 16-bit words (one PRMT).
+int choose_layout(int alphabet, int G, int K, int mode) {
+  if (layout_bytes(PROF_PAIR, alphabet, G, K) <= 64 * 1024) return PROF_PAIR;
+  if (wave_smem((uint32_t)layout_bytes(PROF_S32, alphabet, G, K), wave_block_threads(K), G, K, mode) <= 112 * 1024)
+    return PROF_S32;
+  return PROF_S16;
+}
+
+void pick_shape(ish_ctx *ctx, const Query &q, int *G, int *K, int *layout) {
   const int mode = q.algo == ISH_ALGO_LOCAL ? SW : SG;
   auto it = ctx->tuned.find(tune_key(mode, q.alphabet, q.Q));
-  if (!ctx->force_G && !ctx->force_K && it != ctx->tuned.end()) {
+  if (!ctx->force_G && !ctx->force_K && ctx->force_layout < 0 && it != ctx->tuned.end()) {
     *G = it->second.G;
     *K = it->second.K;
-    *pair = it->second.pair >= 0 ? it->second.pair : pair_layout_fits(q.alphabet, *G, *K);
+    *layout = it->second.layout >= 0 ? it->second.layout : choose_layout(q.alphabet, *G, *K, mode);
     return;
   }
   choose_shape(q.Q, ctx->force_G, ctx->force_K, G, K);
-  *pair = *G ? pair_layout_fits(q.alphabet, *G, *K) : 0;
+  *layout = ctx->force_layout >= 0 ? ctx->force_layout : (*G ? choose_layout(q.alphabet, *G, *K, mode) : PROF_S16);
 }
 
-int build_wave_layout(ish_ctx *ctx, Query &q, int G, int K, int pair, WaveLayout **out) {
-  const int pair_ok = pair;
-  const long key = ((long)G << 20) | ((long)K << 8) | pair_ok;
+int build_wave_layout(ish_ctx *ctx, Query &q, int G, int K, int layout, WaveLayout **out) {
+  const long key = ((long)G << 20) | ((long)K << 8) | layout;
   auto it = q.layouts.find(key);
   if (it != q.layouts.end()) {
     *out = &it->second;
@@ -152,7 +174,8 @@ int build_wave_layout(ish_ctx *ctx, Query &q, int G, int K, int pair, WaveLayout
   L.G = G;
   L.K = K;
   L.d = G * K - q.Q;
-  L.pair = pair_ok;
+  L.layout = layout;
+  L.kp = layout_stride(layout, K);
   const int A = q.alphabet;
   const bool sg = q.algo == ISH_ALGO_SEMI_GLOBAL;
   const int ppad = (sg && !(q.ends & ISH_FREE_TARGET_START)) ? -(q.open + q.ext) : 0;
@@ -161,12 +184,7 @@ int build_wave_layout(ish_ctx *ctx, Query &q, int G, int K, int pair, WaveLayout
     return q.M[(size_t)c * A + q.q[col]];
   };
   std::vector<uint8_t> host;
-  // Row strides are an odd number of 16-byte units: the eight threads of a
-  // quarter-warp read consecutive rows with 16-byte loads, and an odd stride
-  // spreads them over all 32 banks.
-  if (L.pair) {
-    L.kp = (K + 3) & ~3;
-    if (((L.kp / 4) & 1) == 0) L.kp += 4;
+  if (layout == PROF_PAIR) {
     std::vector<uint32_t> w((size_t)A * A * G * L.kp, 0u);
     for (int a = 0; a < A; ++a)
       for (int b = 0; b < A; ++b)
@@ -178,9 +196,14 @@ int build_wave_layout(ish_ctx *ctx, Query &q, int G, int K, int pair, WaveLayout
           }
     host.resize(w.size() * 4);
     memcpy(host.data(), w.data(), host.size());
+  } else if (layout == PROF_S32) {
+    std::vector<uint32_t> w((size_t)A * G * L.kp, 0u);
+    for (int a = 0; a < A; ++a)
+      for (int t = 0; t < G; ++t)
+        for (int j = 0; j < K; ++j) w[((size_t)a * G + t) * L.kp + j] = (uint32_t)P(a, t * K + j - L.d) & 0xffffu;
+    host.resize(w.size() * 4);
+    memcpy(host.data(), w.data(), host.size());
   } else {
-    L.kp = (K + 7) & ~7;
-    if (((L.kp / 8) & 1) == 0) L.kp += 8;
     std::vector<int16_t> w((size_t)A * G * L.kp, 0);
     for (int a = 0; a < A; ++a)
       for (int t = 0; t < G; ++t)
@@ -341,7 +364,8 @@ void wave_params(const Query &q, const WaveLayout &L, const RecordSet &rs, OutDe
   p.d = L.d;
   p.kp = L.kp;
   p.alphabet = q.alphabet;
-  p.pair_prof = L.pair;
+  p.layout = L.layout;
+  p.lane_mul = 65536u;
   p.open = q.open;
   p.ext = q.ext;
   p.ends = q.ends;
@@ -365,14 +389,14 @@ size_t wave_smem(uint32_t prof_area, int threads, int G, int K, int mode) {
 }
 
 int launch_wave_range(ish_ctx *ctx, Query &q, RecordSet &rs, uint32_t first, uint32_t count, OutDev out, int G, int K,
-                      int pair, cudaStream_t s) {
+                      int layout, cudaStream_t s) {
   if (count == 0) return ISH_OK;
   if (!G || G * K < q.Q + 1) return fail(ctx, ISH_EOVERFLOW, "no wavefront shape for a query of %d residues", q.Q);
   WaveLayout *L = nullptr;
-  int rc = build_wave_layout(ctx, q, G, K, pair, &L);
+  int rc = build_wave_layout(ctx, q, G, K, layout, &L);
   if (rc) return rc;
   const int mode = q.algo == ISH_ALGO_LOCAL ? SW : SG;
-  WaveFn fn = wave_fn(K, mode, L->pair);
+  WaveFn fn = wave_fn(K, mode, L->layout);
   if (!fn) return fail(ctx, ISH_EOVERFLOW, "no wavefront kernel for K=%d", K);
   const int threads = wave_block_threads(K);
   const int groups = threads / G;
@@ -461,8 +485,8 @@ int fast_check(const Query &q, const RecordSet &rs, int G, int K, char *msg, siz
 }
 
 int check_fast(ish_ctx *ctx, const Query &q, const RecordSet &rs) {
-  int G, K, pair;
-  pick_shape(ctx, q, &G, &K, &pair);
+  int G, K, layout;
+  pick_shape(ctx, q, &G, &K, &layout);
   char msg[256];
   const int rc = fast_check(q, rs, G, K, msg, sizeof msg);
   return rc ? fail(ctx, rc, "%s", msg) : ISH_OK;
@@ -495,9 +519,9 @@ int run_scoring(ish_ctx *ctx, Query &q, RecordSet &rs) {
     if (ctx->kernel == ISH_KERNEL_PLAIN) {
       rc = launch_plain(ctx, q, rs, 0, nonempty, out);
     } else {
-      int G, K, pair;
-      pick_shape(ctx, q, &G, &K, &pair);
-      rc = launch_wave_range(ctx, q, rs, 0, nonempty, out, G, K, pair, s);
+      int G, K, layout;
+      pick_shape(ctx, q, &G, &K, &layout);
+      rc = launch_wave_range(ctx, q, rs, 0, nonempty, out, G, K, layout, s);
     }
     if (rc) return rc;
   }
@@ -615,6 +639,11 @@ int ish_gpu_set_option(ish_ctx *ctx, int option, int64_t value) {
     if (value != 0 && (value < 1 || value > 32 || (value & (value - 1))))
       return fail(ctx, ISH_EINVAL, "group size must be 0 or a power of two <= 32");
     ctx->force_G = (int)value;
+    drop_plans(ctx, 0, 0);
+    return ISH_OK;
+  case ISH_OPT_PROFILE_LAYOUT:
+    if (value < -1 || value > PROF_S32) return fail(ctx, ISH_EINVAL, "profile layout must be -1, 0, 1 or 2");
+    ctx->force_layout = (int)value;
     drop_plans(ctx, 0, 0);
     return ISH_OK;
   case ISH_OPT_WAVE_K:
@@ -796,14 +825,14 @@ WaveFn wave_fn_c(int, int, int);
 WaveFn wave_fn_d(int, int, int);
 WaveFn wave_fn_e(int, int, int);
 WaveFn wave_fn_f(int, int, int);
-WaveFn wave_fn(int K, int mode, int pair) {
+WaveFn wave_fn(int K, int mode, int layout) {
   if (K < 1) return nullptr;
-  if (K <= 8) return wave_fn_a(K, mode, pair);
-  if (K <= 16) return wave_fn_b(K, mode, pair);
-  if (K <= 24) return wave_fn_c(K, mode, pair);
-  if (K <= 32) return wave_fn_d(K, mode, pair);
-  if (K <= 48) return wave_fn_e(K, mode, pair);
-  return wave_fn_f(K, mode, pair);
+  if (K <= 8) return wave_fn_a(K, mode, layout);
+  if (K <= 16) return wave_fn_b(K, mode, layout);
+  if (K <= 24) return wave_fn_c(K, mode, layout);
+  if (K <= 32) return wave_fn_d(K, mode, layout);
+  if (K <= 48) return wave_fn_e(K, mode, layout);
+  return wave_fn_f(K, mode, layout);
 }
 BatchFn batch_fn_a(int, int, int);
 BatchFn batch_fn_b(int, int, int);
@@ -811,13 +840,13 @@ BatchFn batch_fn_c(int, int, int);
 BatchFn batch_fn_d(int, int, int);
 BatchFn batch_fn_e(int, int, int);
 BatchFn batch_fn_f(int, int, int);
-BatchFn batch_fn(int K, int mode, int pair) {
+BatchFn batch_fn(int K, int mode, int layout) {
   if (K < 1) return nullptr;
-  if (K <= 8) return batch_fn_a(K, mode, pair);
-  if (K <= 16) return batch_fn_b(K, mode, pair);
-  if (K <= 24) return batch_fn_c(K, mode, pair);
-  if (K <= 32) return batch_fn_d(K, mode, pair);
-  if (K <= 48) return batch_fn_e(K, mode, pair);
-  return batch_fn_f(K, mode, pair);
+  if (K <= 8) return batch_fn_a(K, mode, layout);
+  if (K <= 16) return batch_fn_b(K, mode, layout);
+  if (K <= 24) return batch_fn_c(K, mode, layout);
+  if (K <= 32) return batch_fn_d(K, mode, layout);
+  if (K <= 48) return batch_fn_e(K, mode, layout);
+  return batch_fn_f(K, mode, layout);
 }
 }  // namespace ish

@@ -37,9 +37,9 @@ constexpr int WAVE_KMAX = 64;
 __host__ __device__ constexpr int wave_block_threads(int K) { return K <= 32 ? 256 : 128; }
 __host__ __device__ constexpr int wave_blocks_per_sm(int K) { return K <= 32 ? 2 : (K <= 48 ? 3 : 2); }
 typedef void (*WaveFn)(const WaveParams);
-// Returns the kernel for (K, mode, pair profile) or nullptr.
-WaveFn wave_fn(int K, int mode, int pair);
+// Returns the kernel for (K, mode, profile layout) or nullptr.
+WaveFn wave_fn(int K, int mode, int layout);
 typedef void (*BatchFn)(const BatchParams);
-BatchFn batch_fn(int K, int mode, int pair);  // batch_kernel<K, mode, pair> or nullptr
+BatchFn batch_fn(int K, int mode, int layout);  // batch_kernel<K, mode, layout> or nullptr
 
 }  // namespace ish

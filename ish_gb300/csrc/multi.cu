@@ -20,7 +20,7 @@ namespace ish {
 namespace host {
 
 struct MultiClass {
-  int K = 0, mode = 0, pair = 0, threads = 0, Gmin = 32;
+  int K = 0, mode = 0, layout = 0, threads = 0, Gmin = 32;
   BatchFn fn = nullptr;
   size_t smem = 0;
   uint32_t grid = 0, ntiles = 0, prof_area = 0, counter_base = 0;
@@ -110,7 +110,7 @@ int build_plan(ish_ctx *ctx, const int32_t *qids, uint32_t nq, int32_t set_id, R
   // ---- shape classes ----
   struct Member {
     uint32_t pos;
-    int G, K, pair, mode;
+    int G, K, layout, mode;
     WaveLayout *L;
   };
   std::vector<Member> members;
@@ -121,24 +121,24 @@ int build_plan(ish_ctx *ctx, const int32_t *qids, uint32_t nq, int32_t set_id, R
     if (rc) return rc;
     Member m;
     m.pos = i;
-    pick_shape(ctx, q, &m.G, &m.K, &m.pair);
+    pick_shape(ctx, q, &m.G, &m.K, &m.layout);
     if (!m.G || m.G * m.K < q.Q + 1)
       return fail(ctx, ISH_EOVERFLOW, "no wavefront shape for a query of %d residues", q.Q);
     m.mode = q.algo == ISH_ALGO_LOCAL ? SW : SG;
-    rc = build_wave_layout(ctx, q, m.G, m.K, m.pair, &m.L);
+    rc = build_wave_layout(ctx, q, m.G, m.K, m.layout, &m.L);
     if (rc) return rc;
-    m.pair = m.L->pair;
+    m.layout = m.L->layout;
     members.push_back(m);
   }
   std::map<long, size_t> cls_of;
   for (const Member &m : members) {
-    const long key = ((long)m.K << 8) | (m.mode << 1) | m.pair;
+    const long key = ((long)m.K << 8) | (m.mode << 4) | m.layout;
     auto it = cls_of.find(key);
     if (it == cls_of.end()) {
       MultiClass c;
       c.K = m.K;
       c.mode = m.mode;
-      c.pair = m.pair;
+      c.layout = m.layout;
       it = cls_of.emplace(key, P.classes.size()).first;
       P.classes.push_back(std::move(c));
     }
@@ -150,7 +150,7 @@ int build_plan(ish_ctx *ctx, const int32_t *qids, uint32_t nq, int32_t set_id, R
 
   // ---- per class: kernel, occupancy, parameters, tiles ----
   for (MultiClass &c : P.classes) {
-    c.fn = batch_fn(c.K, c.mode, c.pair);
+    c.fn = batch_fn(c.K, c.mode, c.layout);
     if (!c.fn) return fail(ctx, ISH_EOVERFLOW, "no batch kernel for K=%d", c.K);
     c.threads = wave_block_threads(c.K);
     const size_t slot_words = (size_t)(c.threads / c.Gmin) * 32;
@@ -421,9 +421,9 @@ int ish_gpu_autotune(ish_ctx *ctx, int32_t set_id, const int32_t *query_ids, uin
     if (q.Q > 0 && nonempty > 0 && !ctx->tuned.count(key)) {
       if ((rc = check_fast(ctx, q, rs))) break;
       // candidates: every group size whose modelled cost is within 1.6x of
-      // the best, with both profile layouts where the pair layout fits
+      // the best, each with its profile layout and the alternative one
       struct Cand {
-        int G, K, pair;
+        int G, K, layout;
         double model;
       };
       std::vector<Cand> cands;
@@ -434,8 +434,15 @@ int ish_gpu_autotune(ish_ctx *ctx, int32_t set_id, const int32_t *query_ids, uin
         if (!wave_k_available(k)) continue;
         const double m = (double)g * (k + 8) * (k > 48 ? 1.25 : 1.0);
         best_model = std::min(best_model, m);
-        cands.push_back({g, k, 0, m});
-        if (pair_layout_fits(q.alphabet, g, k)) cands.push_back({g, k, 1, m});
+        // the layout rule's pick, and the 16/32-bit alternative to it (the
+        // 32-bit profile saves an ALU instruction per column but can cost
+        // occupancy)
+        const int pick = choose_layout(q.alphabet, g, k, mode);
+        cands.push_back({g, k, pick, m});
+        const int other = pick == PROF_S32 ? PROF_S16 : (pick == PROF_S16 ? PROF_S32 : -1);
+        if (other >= 0 &&
+            wave_smem((uint32_t)layout_bytes(other, q.alphabet, g, k), wave_block_threads(k), g, k, mode) <= 227 * 1024)
+          cands.push_back({g, k, other, m});
       }
       cands.erase(std::remove_if(cands.begin(), cands.end(), [&](const Cand &c) { return c.model > 1.6 * best_model; }),
                   cands.end());
@@ -468,7 +475,7 @@ int ish_gpu_autotune(ish_ctx *ctx, int32_t set_id, const int32_t *query_ids, uin
         float t = 1e30f;
         for (int rep = 0; rep < 3 && rc == ISH_OK; ++rep) {
           CU(cudaEventRecord(ctx->ev0, s));
-          rc = launch_wave_range(ctx, q, rs, first, count, out, c.G, c.K, c.pair, s);
+          rc = launch_wave_range(ctx, q, rs, first, count, out, c.G, c.K, c.layout, s);
           CU(cudaEventRecord(ctx->ev1, s));
           CU(cudaStreamSynchronize(s));
           float ms = 0.f;
@@ -478,15 +485,15 @@ int ish_gpu_autotune(ish_ctx *ctx, int32_t set_id, const int32_t *query_ids, uin
         if (rc) break;
         if (t < best_t) {
           best_t = t;
-          best = Tuned{c.G, c.K, c.pair};
+          best = Tuned{c.G, c.K, c.layout};
         }
       }
       if (rc) break;
       if (best.G) ctx->tuned[key] = best;
     }
     if (group || cols) {
-      int G = 0, K = 0, pair = 0;
-      if (q.Q > 0) pick_shape(ctx, q, &G, &K, &pair);
+      int G = 0, K = 0, layout = 0;
+      if (q.Q > 0) pick_shape(ctx, q, &G, &K, &layout);
       if (group) group[i] = G;
       if (cols) cols[i] = K;
     }

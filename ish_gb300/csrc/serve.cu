@@ -45,7 +45,7 @@ struct Bundle {
 struct Request {
   uint64_t ticket = 0;
   Query q;  // private copy: parameters and sequence (its layouts belong to the scheduler)
-  int G = 0, K = 0, pair = 0, mode = 0;
+  int G = 0, K = 0, layout = 0, mode = 0;
   WaveLayout *L = nullptr;
   Bundle *b = nullptr;
   WaveParams params{};
@@ -183,12 +183,12 @@ int admit(Server &S, Request *r, char *msg, size_t) {
   if (r->q.Q > 0 && rs.n > rs.n_empty) {
     int rc = fast_check(r->q, rs, r->G, r->K, msg, 256);
     if (rc) return rc;
-    rc = build_wave_layout(S.ctx, r->q, r->G, r->K, r->pair, &r->L);
+    rc = build_wave_layout(S.ctx, r->q, r->G, r->K, r->layout, &r->L);
     if (rc) {
       snprintf(msg, 256, "profile upload failed");
       return rc;
     }
-    r->pair = r->L->pair;
+    r->layout = r->L->layout;
   }
   if (S.pool.empty()) {
     Bundle *b = new Bundle();
@@ -235,7 +235,7 @@ int step(Server &S, char *msg) {
   cudaStream_t s = S.s;
   // ---- classes of this step ----
   struct Cls {
-    int K, mode, pair, Gmin = 32;
+    int K, mode, layout, Gmin = 32;
     uint32_t prof_area = 0, first = 0, count = 0;
   };
   std::vector<Cls> cls;
@@ -244,9 +244,9 @@ int step(Server &S, char *msg) {
     if (r->next_chunk >= S.chunks.size()) continue;
     size_t c = 0;
     for (; c < cls.size(); ++c)
-      if (cls[c].K == r->K && cls[c].mode == r->mode && cls[c].pair == r->pair) break;
+      if (cls[c].K == r->K && cls[c].mode == r->mode && cls[c].layout == r->layout) break;
     if (c == cls.size()) {
-      cls.push_back(Cls{r->K, r->mode, r->pair});
+      cls.push_back(Cls{r->K, r->mode, r->layout});
       members.emplace_back();
     }
     cls[c].Gmin = std::min(cls[c].Gmin, r->G);
@@ -280,7 +280,7 @@ int step(Server &S, char *msg) {
     }
     for (size_t c = 0; c < cls.size(); ++c) {
       const Cls &C = cls[c];
-      BatchFn fn = batch_fn(C.K, C.mode, C.pair);
+      BatchFn fn = batch_fn(C.K, C.mode, C.layout);
       if (!fn) {
         snprintf(msg, 256, "no batch kernel for K=%d", C.K);
         return ISH_EOVERFLOW;
@@ -548,7 +548,7 @@ int ish_gpu_submit(ish_ctx *ctx, int32_t query_id, uint64_t *ticket) {
   if (qi == ctx->queries.end()) return fail(ctx, ISH_EINVAL, "unknown query %d", query_id);
   Request *r = new Request();
   clone_params(qi->second, r->q);
-  pick_shape(ctx, r->q, &r->G, &r->K, &r->pair);
+  pick_shape(ctx, r->q, &r->G, &r->K, &r->layout);
   r->mode = r->q.algo == ISH_ALGO_LOCAL ? SW : SG;
   r->t_submit = Clock::now();
   {

@@ -112,9 +112,9 @@ extern "C" int ish_gpu_match_starts(ish_ctx *ctx, int32_t query_id, int32_t set_
   for (uint32_t i = 0; i < n_hits; ++i)
     if (hit_idx[i] >= n) return fail(ctx, ISH_EINVAL, "hit index %u >= %u records", hit_idx[i], n);
   Query &rq = reverse_of(q);
-  int G = 0, K = 0, pair = 0;
+  int G = 0, K = 0, layout = 0;
   if (rq.Q > 0) {  // an empty query scores nothing: reverse end 0, start = len(prefix) - 1
-    pick_shape(ctx, rq, &G, &K, &pair);
+    pick_shape(ctx, rq, &G, &K, &layout);
     Regime r = regime(rq, G ? G * K : rq.Q + 64);
     if (!r.fast || !G || G * K < rq.Q + 1)
       return fail(ctx, ISH_EINVAL, "start finding: parameters outside the exact-integer fast regime");
@@ -209,7 +209,7 @@ extern "C" int ish_gpu_match_starts(ish_ctx *ctx, int32_t query_id, int32_t set_
     rev.orig_s.p = orig.p;
     SCU(cudaMemsetAsync(rev_end.p, 0, (size_t)n_hits * 4, s));
     OutDev out{nullptr, nullptr, rev_end.as<int32_t>(), nullptr};
-    if (rq.Q > 0) rc = launch_wave_range(ctx, rq, rev, 0, n_hits, out, G, K, pair, s);
+    if (rq.Q > 0) rc = launch_wave_range(ctx, rq, rev, 0, n_hits, out, G, K, layout, s);
     rev.off_s.p = rev.len_s.p = rev.orig_s.p = nullptr;  // owned by poff / rlen / orig
     if (rc) break;
     k_starts<<<hb, 256, 0, s>>>(rlen.as<uint32_t>(), rev_end.as<int32_t>(), n_hits, d_start.as<int64_t>());

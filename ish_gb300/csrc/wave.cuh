@@ -43,7 +43,7 @@ namespace ish {
 // left.  `prof` is the profile in shared memory; `slots_all` holds 32 words per
 // group (pair indices in flight), `save_all` 2 * KP4 words per thread (local
 // alignment only).
-template <int K, int MODE, bool PAIR>
+template <int K, int MODE, int LAYOUT>
 __device__ __forceinline__ void wave_rows(const WaveParams &p, const unsigned char *prof, uint32_t *slots_all,
                                           uint32_t *save_all, uint32_t *counter) {
   const int tid = threadIdx.x;
@@ -163,6 +163,12 @@ __device__ __forceinline__ void wave_rows(const WaveParams &p, const unsigned ch
         wB = nB;
         if (row + 4 < lenA) nA = __ldg(reinterpret_cast<const uint32_t *>(pa + row + 4));
         if (row + 4 < lenB) nB = __ldg(reinterpret_cast<const uint32_t *>(pb + row + 4));
+        // long records: pull the codes 256 rows ahead into L1, so the group's
+        // loads above hit L1 even when few warps are left to hide latency
+        if ((row & 127) == 0) {
+          if (row + 256 < lenA) asm volatile("prefetch.global.L1 [%0];" ::"l"(pa + row + 256));
+          if (row + 256 < lenB) asm volatile("prefetch.global.L1 [%0];" ::"l"(pb + row + 256));
+        }
       }
       const uint32_t cA = wA & 0xffu, cB = wB & 0xffu;
       wA >>= 8;
@@ -170,7 +176,7 @@ __device__ __forceinline__ void wave_rows(const WaveParams &p, const unsigned ch
 
       // ---- profile words of this row ----
       uint32_t P[K];
-      if (PAIR) {
+      if (LAYOUT == PROF_PAIR) {
         const uint4 *r4 = reinterpret_cast<const uint4 *>(prof32 + ((cA * p.alphabet + cB) * G + t) * p.kp);
 #pragma unroll
         for (int v = 0; v < (K + 3) / 4; ++v) {
@@ -180,7 +186,25 @@ __device__ __forceinline__ void wave_rows(const WaveParams &p, const unsigned ch
           if (4 * v + 2 < K) P[4 * v + 2] = w.z;
           if (4 * v + 3 < K) P[4 * v + 3] = w.w;
         }
+      } else if (LAYOUT == PROF_S32) {
+        // 32-bit words holding the 16-bit score in the low half; the packed
+        // pair is b * 65536 + a, one integer multiply-add (the multiplier is a
+        // runtime value, so this stays an IMAD on the FMA pipe, which the DPX
+        // recurrence on the ALU pipe leaves idle)
+        const uint4 *ra = reinterpret_cast<const uint4 *>(prof32 + (cA * G + t) * p.kp);
+        const uint4 *rb = reinterpret_cast<const uint4 *>(prof32 + (cB * G + t) * p.kp);
+        const uint32_t mul = p.lane_mul;
+#pragma unroll
+        for (int v = 0; v < (K + 3) / 4; ++v) {
+          const uint4 a = ra[v], b = rb[v];
+          if (4 * v + 0 < K) P[4 * v + 0] = b.x * mul + a.x;
+          if (4 * v + 1 < K) P[4 * v + 1] = b.y * mul + a.y;
+          if (4 * v + 2 < K) P[4 * v + 2] = b.z * mul + a.z;
+          if (4 * v + 3 < K) P[4 * v + 3] = b.w * mul + a.w;
+        }
       } else {
+        // 16-bit words (profiles too large for the 32-bit layout): one PRMT
+        // per packed pair
         const uint4 *ra = reinterpret_cast<const uint4 *>(prof16 + (cA * G + t) * p.kp);
         const uint4 *rb = reinterpret_cast<const uint4 *>(prof16 + (cB * G + t) * p.kp);
 #pragma unroll
@@ -402,7 +426,7 @@ __device__ __forceinline__ void wave_rows(const WaveParams &p, const unsigned ch
 
 // Shared memory of a block: the profile, then 32 slot words per group, then
 // (local alignment) 2 * KP4 save words per thread.
-template <int K, int MODE, bool PAIR>
+template <int K, int MODE, int LAYOUT>
 __global__ void __launch_bounds__(wave_block_threads(K), wave_blocks_per_sm(K))
     wave_kernel(const __grid_constant__ WaveParams p) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -415,7 +439,7 @@ __global__ void __launch_bounds__(wave_block_threads(K), wave_blocks_per_sm(K))
   uint32_t *slots_all = reinterpret_cast<uint32_t *>(smem_raw + ((p.prof_bytes + 15u) & ~15u));
   uint32_t *save_all = slots_all + (blockDim.x / p.G) * 32;
   __syncthreads();
-  wave_rows<K, MODE, PAIR>(p, smem_raw, slots_all, save_all, p.counter);
+  wave_rows<K, MODE, LAYOUT>(p, smem_raw, slots_all, save_all, p.counter);
 }
 
 // The batched launch: one persistent kernel for every query of a shape class
@@ -426,7 +450,7 @@ __global__ void __launch_bounds__(wave_block_threads(K), wave_blocks_per_sm(K))
 // the queries) and stays on a query until its counter runs dry; a barrier and
 // a profile reload happen only at a query switch, where the pairs left are the
 // shortest of the set.  Queries whose counter is already exhausted are skipped.
-template <int K, int MODE, bool PAIR>
+template <int K, int MODE, int LAYOUT>
 __global__ void __launch_bounds__(wave_block_threads(K), wave_blocks_per_sm(K))
     batch_kernel(const __grid_constant__ BatchParams b) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -466,7 +490,7 @@ __global__ void __launch_bounds__(wave_block_threads(K), wave_blocks_per_sm(K))
       for (uint32_t i = threadIdx.x; i < nvec; i += blockDim.x) dst[i] = src[i];
     }
     __syncthreads();
-    wave_rows<K, MODE, PAIR>(sp, smem_raw, slots_all, save_all, counter);
+    wave_rows<K, MODE, LAYOUT>(sp, smem_raw, slots_all, save_all, counter);
     __syncthreads();
   }
 }

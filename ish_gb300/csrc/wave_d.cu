@@ -5,63 +5,113 @@
 
 namespace ish {
 
-WaveFn wave_fn_d(int K, int mode, int pair) {
+WaveFn wave_fn_d(int K, int mode, int layout) {
+  if (layout < PROF_S16 || layout > PROF_S32) return nullptr;
   switch (K) {
-    case 25:
-      return mode == SG ? (pair ? (WaveFn)wave_kernel<25, SG, true> : (WaveFn)wave_kernel<25, SG, false>)
-                        : (pair ? (WaveFn)wave_kernel<25, SW, true> : (WaveFn)wave_kernel<25, SW, false>);
-    case 26:
-      return mode == SG ? (pair ? (WaveFn)wave_kernel<26, SG, true> : (WaveFn)wave_kernel<26, SG, false>)
-                        : (pair ? (WaveFn)wave_kernel<26, SW, true> : (WaveFn)wave_kernel<26, SW, false>);
-    case 27:
-      return mode == SG ? (pair ? (WaveFn)wave_kernel<27, SG, true> : (WaveFn)wave_kernel<27, SG, false>)
-                        : (pair ? (WaveFn)wave_kernel<27, SW, true> : (WaveFn)wave_kernel<27, SW, false>);
-    case 28:
-      return mode == SG ? (pair ? (WaveFn)wave_kernel<28, SG, true> : (WaveFn)wave_kernel<28, SG, false>)
-                        : (pair ? (WaveFn)wave_kernel<28, SW, true> : (WaveFn)wave_kernel<28, SW, false>);
-    case 29:
-      return mode == SG ? (pair ? (WaveFn)wave_kernel<29, SG, true> : (WaveFn)wave_kernel<29, SG, false>)
-                        : (pair ? (WaveFn)wave_kernel<29, SW, true> : (WaveFn)wave_kernel<29, SW, false>);
-    case 30:
-      return mode == SG ? (pair ? (WaveFn)wave_kernel<30, SG, true> : (WaveFn)wave_kernel<30, SG, false>)
-                        : (pair ? (WaveFn)wave_kernel<30, SW, true> : (WaveFn)wave_kernel<30, SW, false>);
-    case 31:
-      return mode == SG ? (pair ? (WaveFn)wave_kernel<31, SG, true> : (WaveFn)wave_kernel<31, SG, false>)
-                        : (pair ? (WaveFn)wave_kernel<31, SW, true> : (WaveFn)wave_kernel<31, SW, false>);
-    case 32:
-      return mode == SG ? (pair ? (WaveFn)wave_kernel<32, SG, true> : (WaveFn)wave_kernel<32, SG, false>)
-                        : (pair ? (WaveFn)wave_kernel<32, SW, true> : (WaveFn)wave_kernel<32, SW, false>);
+    case 25: {
+      static const WaveFn t[2][3] = {
+          {wave_kernel<25, SG, PROF_S16>, wave_kernel<25, SG, PROF_PAIR>, wave_kernel<25, SG, PROF_S32>},
+          {wave_kernel<25, SW, PROF_S16>, wave_kernel<25, SW, PROF_PAIR>, wave_kernel<25, SW, PROF_S32>}};
+      return t[mode == SW][layout];
+    }
+    case 26: {
+      static const WaveFn t[2][3] = {
+          {wave_kernel<26, SG, PROF_S16>, wave_kernel<26, SG, PROF_PAIR>, wave_kernel<26, SG, PROF_S32>},
+          {wave_kernel<26, SW, PROF_S16>, wave_kernel<26, SW, PROF_PAIR>, wave_kernel<26, SW, PROF_S32>}};
+      return t[mode == SW][layout];
+    }
+    case 27: {
+      static const WaveFn t[2][3] = {
+          {wave_kernel<27, SG, PROF_S16>, wave_kernel<27, SG, PROF_PAIR>, wave_kernel<27, SG, PROF_S32>},
+          {wave_kernel<27, SW, PROF_S16>, wave_kernel<27, SW, PROF_PAIR>, wave_kernel<27, SW, PROF_S32>}};
+      return t[mode == SW][layout];
+    }
+    case 28: {
+      static const WaveFn t[2][3] = {
+          {wave_kernel<28, SG, PROF_S16>, wave_kernel<28, SG, PROF_PAIR>, wave_kernel<28, SG, PROF_S32>},
+          {wave_kernel<28, SW, PROF_S16>, wave_kernel<28, SW, PROF_PAIR>, wave_kernel<28, SW, PROF_S32>}};
+      return t[mode == SW][layout];
+    }
+    case 29: {
+      static const WaveFn t[2][3] = {
+          {wave_kernel<29, SG, PROF_S16>, wave_kernel<29, SG, PROF_PAIR>, wave_kernel<29, SG, PROF_S32>},
+          {wave_kernel<29, SW, PROF_S16>, wave_kernel<29, SW, PROF_PAIR>, wave_kernel<29, SW, PROF_S32>}};
+      return t[mode == SW][layout];
+    }
+    case 30: {
+      static const WaveFn t[2][3] = {
+          {wave_kernel<30, SG, PROF_S16>, wave_kernel<30, SG, PROF_PAIR>, wave_kernel<30, SG, PROF_S32>},
+          {wave_kernel<30, SW, PROF_S16>, wave_kernel<30, SW, PROF_PAIR>, wave_kernel<30, SW, PROF_S32>}};
+      return t[mode == SW][layout];
+    }
+    case 31: {
+      static const WaveFn t[2][3] = {
+          {wave_kernel<31, SG, PROF_S16>, wave_kernel<31, SG, PROF_PAIR>, wave_kernel<31, SG, PROF_S32>},
+          {wave_kernel<31, SW, PROF_S16>, wave_kernel<31, SW, PROF_PAIR>, wave_kernel<31, SW, PROF_S32>}};
+      return t[mode == SW][layout];
+    }
+    case 32: {
+      static const WaveFn t[2][3] = {
+          {wave_kernel<32, SG, PROF_S16>, wave_kernel<32, SG, PROF_PAIR>, wave_kernel<32, SG, PROF_S32>},
+          {wave_kernel<32, SW, PROF_S16>, wave_kernel<32, SW, PROF_PAIR>, wave_kernel<32, SW, PROF_S32>}};
+      return t[mode == SW][layout];
+    }
     default:
       return nullptr;
   }
 }
 
-BatchFn batch_fn_d(int K, int mode, int pair) {
+BatchFn batch_fn_d(int K, int mode, int layout) {
+  if (layout < PROF_S16 || layout > PROF_S32) return nullptr;
   switch (K) {
-    case 25:
-      return mode == SG ? (pair ? (BatchFn)batch_kernel<25, SG, true> : (BatchFn)batch_kernel<25, SG, false>)
-                        : (pair ? (BatchFn)batch_kernel<25, SW, true> : (BatchFn)batch_kernel<25, SW, false>);
-    case 26:
-      return mode == SG ? (pair ? (BatchFn)batch_kernel<26, SG, true> : (BatchFn)batch_kernel<26, SG, false>)
-                        : (pair ? (BatchFn)batch_kernel<26, SW, true> : (BatchFn)batch_kernel<26, SW, false>);
-    case 27:
-      return mode == SG ? (pair ? (BatchFn)batch_kernel<27, SG, true> : (BatchFn)batch_kernel<27, SG, false>)
-                        : (pair ? (BatchFn)batch_kernel<27, SW, true> : (BatchFn)batch_kernel<27, SW, false>);
-    case 28:
-      return mode == SG ? (pair ? (BatchFn)batch_kernel<28, SG, true> : (BatchFn)batch_kernel<28, SG, false>)
-                        : (pair ? (BatchFn)batch_kernel<28, SW, true> : (BatchFn)batch_kernel<28, SW, false>);
-    case 29:
-      return mode == SG ? (pair ? (BatchFn)batch_kernel<29, SG, true> : (BatchFn)batch_kernel<29, SG, false>)
-                        : (pair ? (BatchFn)batch_kernel<29, SW, true> : (BatchFn)batch_kernel<29, SW, false>);
-    case 30:
-      return mode == SG ? (pair ? (BatchFn)batch_kernel<30, SG, true> : (BatchFn)batch_kernel<30, SG, false>)
-                        : (pair ? (BatchFn)batch_kernel<30, SW, true> : (BatchFn)batch_kernel<30, SW, false>);
-    case 31:
-      return mode == SG ? (pair ? (BatchFn)batch_kernel<31, SG, true> : (BatchFn)batch_kernel<31, SG, false>)
-                        : (pair ? (BatchFn)batch_kernel<31, SW, true> : (BatchFn)batch_kernel<31, SW, false>);
-    case 32:
-      return mode == SG ? (pair ? (BatchFn)batch_kernel<32, SG, true> : (BatchFn)batch_kernel<32, SG, false>)
-                        : (pair ? (BatchFn)batch_kernel<32, SW, true> : (BatchFn)batch_kernel<32, SW, false>);
+    case 25: {
+      static const BatchFn t[2][3] = {
+          {batch_kernel<25, SG, PROF_S16>, batch_kernel<25, SG, PROF_PAIR>, batch_kernel<25, SG, PROF_S32>},
+          {batch_kernel<25, SW, PROF_S16>, batch_kernel<25, SW, PROF_PAIR>, batch_kernel<25, SW, PROF_S32>}};
+      return t[mode == SW][layout];
+    }
+    case 26: {
+      static const BatchFn t[2][3] = {
+          {batch_kernel<26, SG, PROF_S16>, batch_kernel<26, SG, PROF_PAIR>, batch_kernel<26, SG, PROF_S32>},
+          {batch_kernel<26, SW, PROF_S16>, batch_kernel<26, SW, PROF_PAIR>, batch_kernel<26, SW, PROF_S32>}};
+      return t[mode == SW][layout];
+    }
+    case 27: {
+      static const BatchFn t[2][3] = {
+          {batch_kernel<27, SG, PROF_S16>, batch_kernel<27, SG, PROF_PAIR>, batch_kernel<27, SG, PROF_S32>},
+          {batch_kernel<27, SW, PROF_S16>, batch_kernel<27, SW, PROF_PAIR>, batch_kernel<27, SW, PROF_S32>}};
+      return t[mode == SW][layout];
+    }
+    case 28: {
+      static const BatchFn t[2][3] = {
+          {batch_kernel<28, SG, PROF_S16>, batch_kernel<28, SG, PROF_PAIR>, batch_kernel<28, SG, PROF_S32>},
+          {batch_kernel<28, SW, PROF_S16>, batch_kernel<28, SW, PROF_PAIR>, batch_kernel<28, SW, PROF_S32>}};
+      return t[mode == SW][layout];
+    }
+    case 29: {
+      static const BatchFn t[2][3] = {
+          {batch_kernel<29, SG, PROF_S16>, batch_kernel<29, SG, PROF_PAIR>, batch_kernel<29, SG, PROF_S32>},
+          {batch_kernel<29, SW, PROF_S16>, batch_kernel<29, SW, PROF_PAIR>, batch_kernel<29, SW, PROF_S32>}};
+      return t[mode == SW][layout];
+    }
+    case 30: {
+      static const BatchFn t[2][3] = {
+          {batch_kernel<30, SG, PROF_S16>, batch_kernel<30, SG, PROF_PAIR>, batch_kernel<30, SG, PROF_S32>},
+          {batch_kernel<30, SW, PROF_S16>, batch_kernel<30, SW, PROF_PAIR>, batch_kernel<30, SW, PROF_S32>}};
+      return t[mode == SW][layout];
+    }
+    case 31: {
+      static const BatchFn t[2][3] = {
+          {batch_kernel<31, SG, PROF_S16>, batch_kernel<31, SG, PROF_PAIR>, batch_kernel<31, SG, PROF_S32>},
+          {batch_kernel<31, SW, PROF_S16>, batch_kernel<31, SW, PROF_PAIR>, batch_kernel<31, SW, PROF_S32>}};
+      return t[mode == SW][layout];
+    }
+    case 32: {
+      static const BatchFn t[2][3] = {
+          {batch_kernel<32, SG, PROF_S16>, batch_kernel<32, SG, PROF_PAIR>, batch_kernel<32, SG, PROF_S32>},
+          {batch_kernel<32, SW, PROF_S16>, batch_kernel<32, SW, PROF_PAIR>, batch_kernel<32, SW, PROF_S32>}};
+      return t[mode == SW][layout];
+    }
     default:
       return nullptr;
   }

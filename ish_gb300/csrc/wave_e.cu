@@ -5,63 +5,113 @@
 
 namespace ish {
 
-WaveFn wave_fn_e(int K, int mode, int pair) {
+WaveFn wave_fn_e(int K, int mode, int layout) {
+  if (layout < PROF_S16 || layout > PROF_S32) return nullptr;
   switch (K) {
-    case 34:
-      return mode == SG ? (pair ? (WaveFn)wave_kernel<34, SG, true> : (WaveFn)wave_kernel<34, SG, false>)
-                        : (pair ? (WaveFn)wave_kernel<34, SW, true> : (WaveFn)wave_kernel<34, SW, false>);
-    case 36:
-      return mode == SG ? (pair ? (WaveFn)wave_kernel<36, SG, true> : (WaveFn)wave_kernel<36, SG, false>)
-                        : (pair ? (WaveFn)wave_kernel<36, SW, true> : (WaveFn)wave_kernel<36, SW, false>);
-    case 38:
-      return mode == SG ? (pair ? (WaveFn)wave_kernel<38, SG, true> : (WaveFn)wave_kernel<38, SG, false>)
-                        : (pair ? (WaveFn)wave_kernel<38, SW, true> : (WaveFn)wave_kernel<38, SW, false>);
-    case 40:
-      return mode == SG ? (pair ? (WaveFn)wave_kernel<40, SG, true> : (WaveFn)wave_kernel<40, SG, false>)
-                        : (pair ? (WaveFn)wave_kernel<40, SW, true> : (WaveFn)wave_kernel<40, SW, false>);
-    case 42:
-      return mode == SG ? (pair ? (WaveFn)wave_kernel<42, SG, true> : (WaveFn)wave_kernel<42, SG, false>)
-                        : (pair ? (WaveFn)wave_kernel<42, SW, true> : (WaveFn)wave_kernel<42, SW, false>);
-    case 44:
-      return mode == SG ? (pair ? (WaveFn)wave_kernel<44, SG, true> : (WaveFn)wave_kernel<44, SG, false>)
-                        : (pair ? (WaveFn)wave_kernel<44, SW, true> : (WaveFn)wave_kernel<44, SW, false>);
-    case 46:
-      return mode == SG ? (pair ? (WaveFn)wave_kernel<46, SG, true> : (WaveFn)wave_kernel<46, SG, false>)
-                        : (pair ? (WaveFn)wave_kernel<46, SW, true> : (WaveFn)wave_kernel<46, SW, false>);
-    case 48:
-      return mode == SG ? (pair ? (WaveFn)wave_kernel<48, SG, true> : (WaveFn)wave_kernel<48, SG, false>)
-                        : (pair ? (WaveFn)wave_kernel<48, SW, true> : (WaveFn)wave_kernel<48, SW, false>);
+    case 34: {
+      static const WaveFn t[2][3] = {
+          {wave_kernel<34, SG, PROF_S16>, wave_kernel<34, SG, PROF_PAIR>, wave_kernel<34, SG, PROF_S32>},
+          {wave_kernel<34, SW, PROF_S16>, wave_kernel<34, SW, PROF_PAIR>, wave_kernel<34, SW, PROF_S32>}};
+      return t[mode == SW][layout];
+    }
+    case 36: {
+      static const WaveFn t[2][3] = {
+          {wave_kernel<36, SG, PROF_S16>, wave_kernel<36, SG, PROF_PAIR>, wave_kernel<36, SG, PROF_S32>},
+          {wave_kernel<36, SW, PROF_S16>, wave_kernel<36, SW, PROF_PAIR>, wave_kernel<36, SW, PROF_S32>}};
+      return t[mode == SW][layout];
+    }
+    case 38: {
+      static const WaveFn t[2][3] = {
+          {wave_kernel<38, SG, PROF_S16>, wave_kernel<38, SG, PROF_PAIR>, wave_kernel<38, SG, PROF_S32>},
+          {wave_kernel<38, SW, PROF_S16>, wave_kernel<38, SW, PROF_PAIR>, wave_kernel<38, SW, PROF_S32>}};
+      return t[mode == SW][layout];
+    }
+    case 40: {
+      static const WaveFn t[2][3] = {
+          {wave_kernel<40, SG, PROF_S16>, wave_kernel<40, SG, PROF_PAIR>, wave_kernel<40, SG, PROF_S32>},
+          {wave_kernel<40, SW, PROF_S16>, wave_kernel<40, SW, PROF_PAIR>, wave_kernel<40, SW, PROF_S32>}};
+      return t[mode == SW][layout];
+    }
+    case 42: {
+      static const WaveFn t[2][3] = {
+          {wave_kernel<42, SG, PROF_S16>, wave_kernel<42, SG, PROF_PAIR>, wave_kernel<42, SG, PROF_S32>},
+          {wave_kernel<42, SW, PROF_S16>, wave_kernel<42, SW, PROF_PAIR>, wave_kernel<42, SW, PROF_S32>}};
+      return t[mode == SW][layout];
+    }
+    case 44: {
+      static const WaveFn t[2][3] = {
+          {wave_kernel<44, SG, PROF_S16>, wave_kernel<44, SG, PROF_PAIR>, wave_kernel<44, SG, PROF_S32>},
+          {wave_kernel<44, SW, PROF_S16>, wave_kernel<44, SW, PROF_PAIR>, wave_kernel<44, SW, PROF_S32>}};
+      return t[mode == SW][layout];
+    }
+    case 46: {
+      static const WaveFn t[2][3] = {
+          {wave_kernel<46, SG, PROF_S16>, wave_kernel<46, SG, PROF_PAIR>, wave_kernel<46, SG, PROF_S32>},
+          {wave_kernel<46, SW, PROF_S16>, wave_kernel<46, SW, PROF_PAIR>, wave_kernel<46, SW, PROF_S32>}};
+      return t[mode == SW][layout];
+    }
+    case 48: {
+      static const WaveFn t[2][3] = {
+          {wave_kernel<48, SG, PROF_S16>, wave_kernel<48, SG, PROF_PAIR>, wave_kernel<48, SG, PROF_S32>},
+          {wave_kernel<48, SW, PROF_S16>, wave_kernel<48, SW, PROF_PAIR>, wave_kernel<48, SW, PROF_S32>}};
+      return t[mode == SW][layout];
+    }
     default:
       return nullptr;
   }
 }
 
-BatchFn batch_fn_e(int K, int mode, int pair) {
+BatchFn batch_fn_e(int K, int mode, int layout) {
+  if (layout < PROF_S16 || layout > PROF_S32) return nullptr;
   switch (K) {
-    case 34:
-      return mode == SG ? (pair ? (BatchFn)batch_kernel<34, SG, true> : (BatchFn)batch_kernel<34, SG, false>)
-                        : (pair ? (BatchFn)batch_kernel<34, SW, true> : (BatchFn)batch_kernel<34, SW, false>);
-    case 36:
-      return mode == SG ? (pair ? (BatchFn)batch_kernel<36, SG, true> : (BatchFn)batch_kernel<36, SG, false>)
-                        : (pair ? (BatchFn)batch_kernel<36, SW, true> : (BatchFn)batch_kernel<36, SW, false>);
-    case 38:
-      return mode == SG ? (pair ? (BatchFn)batch_kernel<38, SG, true> : (BatchFn)batch_kernel<38, SG, false>)
-                        : (pair ? (BatchFn)batch_kernel<38, SW, true> : (BatchFn)batch_kernel<38, SW, false>);
-    case 40:
-      return mode == SG ? (pair ? (BatchFn)batch_kernel<40, SG, true> : (BatchFn)batch_kernel<40, SG, false>)
-                        : (pair ? (BatchFn)batch_kernel<40, SW, true> : (BatchFn)batch_kernel<40, SW, false>);
-    case 42:
-      return mode == SG ? (pair ? (BatchFn)batch_kernel<42, SG, true> : (BatchFn)batch_kernel<42, SG, false>)
-                        : (pair ? (BatchFn)batch_kernel<42, SW, true> : (BatchFn)batch_kernel<42, SW, false>);
-    case 44:
-      return mode == SG ? (pair ? (BatchFn)batch_kernel<44, SG, true> : (BatchFn)batch_kernel<44, SG, false>)
-                        : (pair ? (BatchFn)batch_kernel<44, SW, true> : (BatchFn)batch_kernel<44, SW, false>);
-    case 46:
-      return mode == SG ? (pair ? (BatchFn)batch_kernel<46, SG, true> : (BatchFn)batch_kernel<46, SG, false>)
-                        : (pair ? (BatchFn)batch_kernel<46, SW, true> : (BatchFn)batch_kernel<46, SW, false>);
-    case 48:
-      return mode == SG ? (pair ? (BatchFn)batch_kernel<48, SG, true> : (BatchFn)batch_kernel<48, SG, false>)
-                        : (pair ? (BatchFn)batch_kernel<48, SW, true> : (BatchFn)batch_kernel<48, SW, false>);
+    case 34: {
+      static const BatchFn t[2][3] = {
+          {batch_kernel<34, SG, PROF_S16>, batch_kernel<34, SG, PROF_PAIR>, batch_kernel<34, SG, PROF_S32>},
+          {batch_kernel<34, SW, PROF_S16>, batch_kernel<34, SW, PROF_PAIR>, batch_kernel<34, SW, PROF_S32>}};
+      return t[mode == SW][layout];
+    }
+    case 36: {
+      static const BatchFn t[2][3] = {
+          {batch_kernel<36, SG, PROF_S16>, batch_kernel<36, SG, PROF_PAIR>, batch_kernel<36, SG, PROF_S32>},
+          {batch_kernel<36, SW, PROF_S16>, batch_kernel<36, SW, PROF_PAIR>, batch_kernel<36, SW, PROF_S32>}};
+      return t[mode == SW][layout];
+    }
+    case 38: {
+      static const BatchFn t[2][3] = {
+          {batch_kernel<38, SG, PROF_S16>, batch_kernel<38, SG, PROF_PAIR>, batch_kernel<38, SG, PROF_S32>},
+          {batch_kernel<38, SW, PROF_S16>, batch_kernel<38, SW, PROF_PAIR>, batch_kernel<38, SW, PROF_S32>}};
+      return t[mode == SW][layout];
+    }
+    case 40: {
+      static const BatchFn t[2][3] = {
+          {batch_kernel<40, SG, PROF_S16>, batch_kernel<40, SG, PROF_PAIR>, batch_kernel<40, SG, PROF_S32>},
+          {batch_kernel<40, SW, PROF_S16>, batch_kernel<40, SW, PROF_PAIR>, batch_kernel<40, SW, PROF_S32>}};
+      return t[mode == SW][layout];
+    }
+    case 42: {
+      static const BatchFn t[2][3] = {
+          {batch_kernel<42, SG, PROF_S16>, batch_kernel<42, SG, PROF_PAIR>, batch_kernel<42, SG, PROF_S32>},
+          {batch_kernel<42, SW, PROF_S16>, batch_kernel<42, SW, PROF_PAIR>, batch_kernel<42, SW, PROF_S32>}};
+      return t[mode == SW][layout];
+    }
+    case 44: {
+      static const BatchFn t[2][3] = {
+          {batch_kernel<44, SG, PROF_S16>, batch_kernel<44, SG, PROF_PAIR>, batch_kernel<44, SG, PROF_S32>},
+          {batch_kernel<44, SW, PROF_S16>, batch_kernel<44, SW, PROF_PAIR>, batch_kernel<44, SW, PROF_S32>}};
+      return t[mode == SW][layout];
+    }
+    case 46: {
+      static const BatchFn t[2][3] = {
+          {batch_kernel<46, SG, PROF_S16>, batch_kernel<46, SG, PROF_PAIR>, batch_kernel<46, SG, PROF_S32>},
+          {batch_kernel<46, SW, PROF_S16>, batch_kernel<46, SW, PROF_PAIR>, batch_kernel<46, SW, PROF_S32>}};
+      return t[mode == SW][layout];
+    }
+    case 48: {
+      static const BatchFn t[2][3] = {
+          {batch_kernel<48, SG, PROF_S16>, batch_kernel<48, SG, PROF_PAIR>, batch_kernel<48, SG, PROF_S32>},
+          {batch_kernel<48, SW, PROF_S16>, batch_kernel<48, SW, PROF_PAIR>, batch_kernel<48, SW, PROF_S32>}};
+      return t[mode == SW][layout];
+    }
     default:
       return nullptr;
   }

@@ -5,63 +5,113 @@
 
 namespace ish {
 
-WaveFn wave_fn_f(int K, int mode, int pair) {
+WaveFn wave_fn_f(int K, int mode, int layout) {
+  if (layout < PROF_S16 || layout > PROF_S32) return nullptr;
   switch (K) {
-    case 50:
-      return mode == SG ? (pair ? (WaveFn)wave_kernel<50, SG, true> : (WaveFn)wave_kernel<50, SG, false>)
-                        : (pair ? (WaveFn)wave_kernel<50, SW, true> : (WaveFn)wave_kernel<50, SW, false>);
-    case 52:
-      return mode == SG ? (pair ? (WaveFn)wave_kernel<52, SG, true> : (WaveFn)wave_kernel<52, SG, false>)
-                        : (pair ? (WaveFn)wave_kernel<52, SW, true> : (WaveFn)wave_kernel<52, SW, false>);
-    case 54:
-      return mode == SG ? (pair ? (WaveFn)wave_kernel<54, SG, true> : (WaveFn)wave_kernel<54, SG, false>)
-                        : (pair ? (WaveFn)wave_kernel<54, SW, true> : (WaveFn)wave_kernel<54, SW, false>);
-    case 56:
-      return mode == SG ? (pair ? (WaveFn)wave_kernel<56, SG, true> : (WaveFn)wave_kernel<56, SG, false>)
-                        : (pair ? (WaveFn)wave_kernel<56, SW, true> : (WaveFn)wave_kernel<56, SW, false>);
-    case 58:
-      return mode == SG ? (pair ? (WaveFn)wave_kernel<58, SG, true> : (WaveFn)wave_kernel<58, SG, false>)
-                        : (pair ? (WaveFn)wave_kernel<58, SW, true> : (WaveFn)wave_kernel<58, SW, false>);
-    case 60:
-      return mode == SG ? (pair ? (WaveFn)wave_kernel<60, SG, true> : (WaveFn)wave_kernel<60, SG, false>)
-                        : (pair ? (WaveFn)wave_kernel<60, SW, true> : (WaveFn)wave_kernel<60, SW, false>);
-    case 62:
-      return mode == SG ? (pair ? (WaveFn)wave_kernel<62, SG, true> : (WaveFn)wave_kernel<62, SG, false>)
-                        : (pair ? (WaveFn)wave_kernel<62, SW, true> : (WaveFn)wave_kernel<62, SW, false>);
-    case 64:
-      return mode == SG ? (pair ? (WaveFn)wave_kernel<64, SG, true> : (WaveFn)wave_kernel<64, SG, false>)
-                        : (pair ? (WaveFn)wave_kernel<64, SW, true> : (WaveFn)wave_kernel<64, SW, false>);
+    case 50: {
+      static const WaveFn t[2][3] = {
+          {wave_kernel<50, SG, PROF_S16>, wave_kernel<50, SG, PROF_PAIR>, wave_kernel<50, SG, PROF_S32>},
+          {wave_kernel<50, SW, PROF_S16>, wave_kernel<50, SW, PROF_PAIR>, wave_kernel<50, SW, PROF_S32>}};
+      return t[mode == SW][layout];
+    }
+    case 52: {
+      static const WaveFn t[2][3] = {
+          {wave_kernel<52, SG, PROF_S16>, wave_kernel<52, SG, PROF_PAIR>, wave_kernel<52, SG, PROF_S32>},
+          {wave_kernel<52, SW, PROF_S16>, wave_kernel<52, SW, PROF_PAIR>, wave_kernel<52, SW, PROF_S32>}};
+      return t[mode == SW][layout];
+    }
+    case 54: {
+      static const WaveFn t[2][3] = {
+          {wave_kernel<54, SG, PROF_S16>, wave_kernel<54, SG, PROF_PAIR>, wave_kernel<54, SG, PROF_S32>},
+          {wave_kernel<54, SW, PROF_S16>, wave_kernel<54, SW, PROF_PAIR>, wave_kernel<54, SW, PROF_S32>}};
+      return t[mode == SW][layout];
+    }
+    case 56: {
+      static const WaveFn t[2][3] = {
+          {wave_kernel<56, SG, PROF_S16>, wave_kernel<56, SG, PROF_PAIR>, wave_kernel<56, SG, PROF_S32>},
+          {wave_kernel<56, SW, PROF_S16>, wave_kernel<56, SW, PROF_PAIR>, wave_kernel<56, SW, PROF_S32>}};
+      return t[mode == SW][layout];
+    }
+    case 58: {
+      static const WaveFn t[2][3] = {
+          {wave_kernel<58, SG, PROF_S16>, wave_kernel<58, SG, PROF_PAIR>, wave_kernel<58, SG, PROF_S32>},
+          {wave_kernel<58, SW, PROF_S16>, wave_kernel<58, SW, PROF_PAIR>, wave_kernel<58, SW, PROF_S32>}};
+      return t[mode == SW][layout];
+    }
+    case 60: {
+      static const WaveFn t[2][3] = {
+          {wave_kernel<60, SG, PROF_S16>, wave_kernel<60, SG, PROF_PAIR>, wave_kernel<60, SG, PROF_S32>},
+          {wave_kernel<60, SW, PROF_S16>, wave_kernel<60, SW, PROF_PAIR>, wave_kernel<60, SW, PROF_S32>}};
+      return t[mode == SW][layout];
+    }
+    case 62: {
+      static const WaveFn t[2][3] = {
+          {wave_kernel<62, SG, PROF_S16>, wave_kernel<62, SG, PROF_PAIR>, wave_kernel<62, SG, PROF_S32>},
+          {wave_kernel<62, SW, PROF_S16>, wave_kernel<62, SW, PROF_PAIR>, wave_kernel<62, SW, PROF_S32>}};
+      return t[mode == SW][layout];
+    }
+    case 64: {
+      static const WaveFn t[2][3] = {
+          {wave_kernel<64, SG, PROF_S16>, wave_kernel<64, SG, PROF_PAIR>, wave_kernel<64, SG, PROF_S32>},
+          {wave_kernel<64, SW, PROF_S16>, wave_kernel<64, SW, PROF_PAIR>, wave_kernel<64, SW, PROF_S32>}};
+      return t[mode == SW][layout];
+    }
     default:
       return nullptr;
   }
 }
 
-BatchFn batch_fn_f(int K, int mode, int pair) {
+BatchFn batch_fn_f(int K, int mode, int layout) {
+  if (layout < PROF_S16 || layout > PROF_S32) return nullptr;
   switch (K) {
-    case 50:
-      return mode == SG ? (pair ? (BatchFn)batch_kernel<50, SG, true> : (BatchFn)batch_kernel<50, SG, false>)
-                        : (pair ? (BatchFn)batch_kernel<50, SW, true> : (BatchFn)batch_kernel<50, SW, false>);
-    case 52:
-      return mode == SG ? (pair ? (BatchFn)batch_kernel<52, SG, true> : (BatchFn)batch_kernel<52, SG, false>)
-                        : (pair ? (BatchFn)batch_kernel<52, SW, true> : (BatchFn)batch_kernel<52, SW, false>);
-    case 54:
-      return mode == SG ? (pair ? (BatchFn)batch_kernel<54, SG, true> : (BatchFn)batch_kernel<54, SG, false>)
-                        : (pair ? (BatchFn)batch_kernel<54, SW, true> : (BatchFn)batch_kernel<54, SW, false>);
-    case 56:
-      return mode == SG ? (pair ? (BatchFn)batch_kernel<56, SG, true> : (BatchFn)batch_kernel<56, SG, false>)
-                        : (pair ? (BatchFn)batch_kernel<56, SW, true> : (BatchFn)batch_kernel<56, SW, false>);
-    case 58:
-      return mode == SG ? (pair ? (BatchFn)batch_kernel<58, SG, true> : (BatchFn)batch_kernel<58, SG, false>)
-                        : (pair ? (BatchFn)batch_kernel<58, SW, true> : (BatchFn)batch_kernel<58, SW, false>);
-    case 60:
-      return mode == SG ? (pair ? (BatchFn)batch_kernel<60, SG, true> : (BatchFn)batch_kernel<60, SG, false>)
-                        : (pair ? (BatchFn)batch_kernel<60, SW, true> : (BatchFn)batch_kernel<60, SW, false>);
-    case 62:
-      return mode == SG ? (pair ? (BatchFn)batch_kernel<62, SG, true> : (BatchFn)batch_kernel<62, SG, false>)
-                        : (pair ? (BatchFn)batch_kernel<62, SW, true> : (BatchFn)batch_kernel<62, SW, false>);
-    case 64:
-      return mode == SG ? (pair ? (BatchFn)batch_kernel<64, SG, true> : (BatchFn)batch_kernel<64, SG, false>)
-                        : (pair ? (BatchFn)batch_kernel<64, SW, true> : (BatchFn)batch_kernel<64, SW, false>);
+    case 50: {
+      static const BatchFn t[2][3] = {
+          {batch_kernel<50, SG, PROF_S16>, batch_kernel<50, SG, PROF_PAIR>, batch_kernel<50, SG, PROF_S32>},
+          {batch_kernel<50, SW, PROF_S16>, batch_kernel<50, SW, PROF_PAIR>, batch_kernel<50, SW, PROF_S32>}};
+      return t[mode == SW][layout];
+    }
+    case 52: {
+      static const BatchFn t[2][3] = {
+          {batch_kernel<52, SG, PROF_S16>, batch_kernel<52, SG, PROF_PAIR>, batch_kernel<52, SG, PROF_S32>},
+          {batch_kernel<52, SW, PROF_S16>, batch_kernel<52, SW, PROF_PAIR>, batch_kernel<52, SW, PROF_S32>}};
+      return t[mode == SW][layout];
+    }
+    case 54: {
+      static const BatchFn t[2][3] = {
+          {batch_kernel<54, SG, PROF_S16>, batch_kernel<54, SG, PROF_PAIR>, batch_kernel<54, SG, PROF_S32>},
+          {batch_kernel<54, SW, PROF_S16>, batch_kernel<54, SW, PROF_PAIR>, batch_kernel<54, SW, PROF_S32>}};
+      return t[mode == SW][layout];
+    }
+    case 56: {
+      static const BatchFn t[2][3] = {
+          {batch_kernel<56, SG, PROF_S16>, batch_kernel<56, SG, PROF_PAIR>, batch_kernel<56, SG, PROF_S32>},
+          {batch_kernel<56, SW, PROF_S16>, batch_kernel<56, SW, PROF_PAIR>, batch_kernel<56, SW, PROF_S32>}};
+      return t[mode == SW][layout];
+    }
+    case 58: {
+      static const BatchFn t[2][3] = {
+          {batch_kernel<58, SG, PROF_S16>, batch_kernel<58, SG, PROF_PAIR>, batch_kernel<58, SG, PROF_S32>},
+          {batch_kernel<58, SW, PROF_S16>, batch_kernel<58, SW, PROF_PAIR>, batch_kernel<58, SW, PROF_S32>}};
+      return t[mode == SW][layout];
+    }
+    case 60: {
+      static const BatchFn t[2][3] = {
+          {batch_kernel<60, SG, PROF_S16>, batch_kernel<60, SG, PROF_PAIR>, batch_kernel<60, SG, PROF_S32>},
+          {batch_kernel<60, SW, PROF_S16>, batch_kernel<60, SW, PROF_PAIR>, batch_kernel<60, SW, PROF_S32>}};
+      return t[mode == SW][layout];
+    }
+    case 62: {
+      static const BatchFn t[2][3] = {
+          {batch_kernel<62, SG, PROF_S16>, batch_kernel<62, SG, PROF_PAIR>, batch_kernel<62, SG, PROF_S32>},
+          {batch_kernel<62, SW, PROF_S16>, batch_kernel<62, SW, PROF_PAIR>, batch_kernel<62, SW, PROF_S32>}};
+      return t[mode == SW][layout];
+    }
+    case 64: {
+      static const BatchFn t[2][3] = {
+          {batch_kernel<64, SG, PROF_S16>, batch_kernel<64, SG, PROF_PAIR>, batch_kernel<64, SG, PROF_S32>},
+          {batch_kernel<64, SW, PROF_S16>, batch_kernel<64, SW, PROF_PAIR>, batch_kernel<64, SW, PROF_S32>}};
+      return t[mode == SW][layout];
+    }
     default:
       return nullptr;
   }

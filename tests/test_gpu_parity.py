@@ -215,3 +215,23 @@ def test_matchers_on_reference_searcher_fixtures(ctx):
             else:
                 assert got == exp, (case["line"], algo, ends)
             ctx.free_query(mt.query_id)
+
+
+@pytest.mark.parametrize("layout", [native.PROF_S16, native.PROF_PAIR, native.PROF_S32])
+@pytest.mark.parametrize("kind", [O.ACTGN, O.BLOSUM62])
+def test_every_profile_layout(ctx, layout, kind):
+    # the three shared-memory profile layouts give identical results
+    rng = np.random.default_rng(3000 + 10 * layout + kind)
+    alpha = 5 if kind == O.ACTGN else 20
+    # (the pair layout of a 24-letter alphabet holds 576 rows: short queries
+    # keep it within shared memory)
+    for qlen in ((13, 40, 97) if kind == O.ACTGN else (13, 40)):
+        q = rng.integers(0, alpha, qlen, dtype=np.uint8)
+        recs = random_records(rng, alpha, 150, 0, 2 * qlen + 30, q)
+        ctx.set_option(native.OPT_PROFILE_LAYOUT, layout)
+        try:
+            for algo, ends in ((native.ALGO_SEMI_GLOBAL, 12), (native.ALGO_SEMI_GLOBAL, 5), (native.ALGO_LOCAL, 0)):
+                g, o = run_both(ctx, algo, kind, q, recs, 10 if kind == O.BLOSUM62 else 3, 1, ends)
+                assert_same(g, o, f"layout={layout} kind={kind} Q={qlen} algo={algo} ends={ends}")
+        finally:
+            ctx.set_option(native.OPT_PROFILE_LAYOUT, native.PROF_AUTO)
