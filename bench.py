@@ -552,6 +552,25 @@ def run_workload(args):
             e2e.append(1e3 * (time.perf_counter() - t))
     e2e_ms = reduce_max(dist, float(np.mean(e2e)))
     d2h = 4 * nh + (0 if name == "batched" else 12 * wl.n) + 8 * (len(qids) + 1)
+    if name == "line":
+        # from raw text, as a line runner holds a file: upload, split into
+        # lines, encode and pack on the device, score, results back
+        from ish_gb300.scoring import ScoringMatrix as _SM
+
+        dec = _SM(wl.kind).code_to_ascii
+        text = b"\n".join(dec[wl.records[int(wl.offsets[i]):int(wl.offsets[i + 1])]].tobytes()
+                           for i in range(wl.n)) + b"\n"
+        tl = []
+        for s in range(args.warmup + args.steps):
+            t = time.perf_counter()
+            sid4, nl = ctx.records_load_lines(text, wl.kind)
+            r = ctx.score_set(qids[0], sid4, want=("score", "qend", "tend", "hit_idx"))
+            ctx.records_free(sid4)
+            if s >= args.warmup:
+                tl.append(1e3 * (time.perf_counter() - t))
+        extra["e2e_from_text"] = {"value": round(cells / (float(np.mean(tl)) * 1e-3) / 1e9, 2), "unit": "GCUPS",
+                                  "h2d_bytes_per_step": len(text), "lines": nl,
+                                  "hits_equal": bool(len(r["hit_idx"]) == nh)}
     cpu = None
     if rank == 0 and not args.no_cpu:
         cpu = _cpu_sample(wl, queries, gap_open, gap_ext, thr, args.cpu_seconds)

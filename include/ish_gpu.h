@@ -125,6 +125,23 @@ ISH_API int ish_gpu_records_free(ish_ctx *ctx, int32_t set_id);
 /* Number of records and total residue bytes of a resident set. */
 ISH_API int ish_gpu_records_info(ish_ctx *ctx, int32_t set_id, uint32_t *n, uint64_t *total_bytes);
 
+/* Load a resident set from RAW bytes: records as for ish_gpu_records_load, but
+ * not yet encoded; the device encodes them with ish's table for matrix_kind
+ * (convert_ascii_to_encoding: ishlib/matcher/alignment/scoring_matrix.mojo:
+ * 9-27 AA_TO_NUM, 131-149 NT_TO_NUM, identity for ascii) while packing,
+ * replacing the runners' per-byte host loop
+ * (ishlib/parallel_line_search_runner.mojo:90-94, 344-348). */
+ISH_API int ish_gpu_records_load_raw(ish_ctx *ctx, const uint8_t *raw, const uint64_t *offsets, uint32_t n,
+                                     int matrix_kind, int32_t *set_id);
+
+/* Load the LINES of a text buffer as a resident set: split at '\n' on the
+ * device exactly as ish's line reader does (ishlib/vendor/kseq.mojo:270-330:
+ * a trailing '\r' is dropped from lines longer than one byte, a last line
+ * without '\n' is a record, empty lines are records), encoded on the device as
+ * for ish_gpu_records_load_raw.  Record i is line i of the text. */
+ISH_API int ish_gpu_records_load_lines(ish_ctx *ctx, const uint8_t *text, uint64_t bytes, int matrix_kind,
+                                       int32_t *set_id, uint32_t *n_records);
+
 /* Score one query against a resident set; outputs as for ish_gpu_score. */
 ISH_API int ish_gpu_score_set(ish_ctx *ctx, int32_t query_id, int32_t set_id, int32_t *score,
                       int32_t *query_end, int32_t *target_end, uint8_t *hit, uint32_t *hit_idx,

@@ -65,7 +65,8 @@ struct WaveParams {
   const uint4 *prof;       // wavefront profile (see build_wave_profile)
   uint32_t prof_bytes;     // bytes copied into shared memory
   int Q, G, K, d, kp;      // query length, threads per group, columns per thread, front padding, profile stride
-  int alphabet;
+  int alphabet;            // profile rows (codes map to rows through the remap table when remap_off != 0)
+  uint32_t remap_off;      // byte offset of the 256-entry code -> row table in the profile, 0: none
   int layout;              // PROF_S16, PROF_PAIR or PROF_S32 (see below)
   uint32_t lane_mul;       // 65536: b * lane_mul + a packs two PROF_S32 words
   int open, ext, ends;

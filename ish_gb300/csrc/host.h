@@ -42,7 +42,8 @@ struct DevBuf {
 
 struct WaveLayout {
   int G = 0, K = 0, d = 0, kp = 0, layout = 0;
-  uint32_t prof_bytes = 0;
+  uint32_t prof_bytes = 0;  // profile rows, then (if remapped) the 256-byte code -> row table
+  uint32_t remap_off = 0;   // byte offset of that table, 0: codes are rows
   DevBuf prof, hinit;
 };
 
@@ -54,13 +55,20 @@ struct Query {
   std::vector<uint8_t> q;
   int mmin = 0, mmax = 0;
   int neg_limit = 0;
+  // Profile rows: codes whose matrix rows agree on every query column share
+  // one row (for ascii, every byte that is not in the query); rowmap[c] is the
+  // row of code c, rep[r] a code of row r.
+  int rows = 0;
+  std::vector<uint8_t> rowmap, rep;
   DevBuf plain_prof, plain_hinit;
   bool plain_ready = false;
   std::map<long, WaveLayout> layouts;
   std::unique_ptr<Query> reverse;  // reversed query with swapped free ends (start finding)
+  std::map<long, DevBuf> exact_prof;  // striped profiles of the exact kernels (exact.cu)
 };
 
 // Parameters and sequence of a query without its device state.
+void compute_rows(Query &q);
 inline void clone_params(const Query &src, Query &dst) {
   dst.algo = src.algo;
   dst.kind = src.kind;
@@ -76,6 +84,9 @@ inline void clone_params(const Query &src, Query &dst) {
   dst.mmin = src.mmin;
   dst.mmax = src.mmax;
   dst.neg_limit = src.neg_limit;
+  dst.rows = src.rows;
+  dst.rowmap = src.rowmap;
+  dst.rep = src.rep;
 }
 
 struct RecordSet {
@@ -120,6 +131,8 @@ struct ish_ctx {
   ish::host::DevBuf raw, off_in, len_tmp, slot_tmp, poff_tmp, hist, scan_tmp, max_code;
   ish::host::DevBuf counter, error, out_score, out_qend, out_tend, out_hit, hit_idx, block_counts, nhits;
   ish::host::DevBuf plain_scratch;
+  ish::host::DevBuf enc_tables, nl_pos, line_end;  // encoding tables; line splitting scratch
+  ish::host::DevBuf exact_scratch, exact_redo;      // exact kernels (exact.cu)
   float last_ms = 0.f;
   // batched launches (multi.cu): plans cached per (queries, set, outputs)
   std::map<std::string, ish::host::MultiPlan *> plans;
@@ -139,12 +152,16 @@ namespace host {
 int fail(ish_ctx *c, int code, const char *fmt, ...);
 extern thread_local std::string g_open_error;
 
+// A failed runtime call also leaves the runtime's last-error state set;
+// it is cleared here so that the next call does not report it again.
 #define CU(call)                                                                                   \
   do {                                                                                             \
     cudaError_t _e = (call);                                                                       \
-    if (_e != cudaSuccess)                                                                         \
+    if (_e != cudaSuccess) {                                                                       \
+      (void)cudaGetLastError();                                                                    \
       return ::ish::host::fail(ctx, _e == cudaErrorMemoryAllocation ? ISH_ENOMEM : ISH_EDEVICE,     \
                                "%s: %s (%s:%d)", #call, cudaGetErrorString(_e), __FILE__, __LINE__); \
+    }                                                                                              \
   } while (0)
 
 inline uint32_t ceil_div(uint64_t a, uint64_t b) { return (uint32_t)((a + b - 1) / b); }
@@ -162,7 +179,11 @@ int layout_stride(int layout, int K);
 size_t layout_bytes(int layout, int alphabet, int G, int K);
 int choose_layout(int alphabet, int G, int K, int mode);
 int build_wave_layout(ish_ctx *ctx, Query &q, int G, int K, int layout, WaveLayout **out);
-int load_records(ish_ctx *ctx, const uint8_t *records, const uint64_t *offsets, uint32_t n, RecordSet &rs);
+int load_records(ish_ctx *ctx, const uint8_t *records, const uint64_t *offsets, uint32_t n, RecordSet &rs,
+                 const uint8_t *enc);
+int load_lines(ish_ctx *ctx, const uint8_t *text, uint64_t bytes, RecordSet &rs, const uint8_t *enc, uint32_t *n_out);
+int device_encoding(ish_ctx *ctx, int kind, const uint8_t **out);
+void encoding_table(int kind, uint8_t t[256]);
 uint32_t count_longer(const RecordSet &rs, uint64_t len);
 // Checks that query q may run on the wavefront kernels against set rs with
 // shape (G, K): 0 or a status with the reason in msg.  check_fast picks the
@@ -173,6 +194,12 @@ int check_fast(ish_ctx *ctx, const Query &q, const RecordSet &rs);
 void wave_params(const Query &q, const WaveLayout &L, const RecordSet &rs, OutDev out, int *error, WaveParams *p);
 int launch_wave_range(ish_ctx *ctx, Query &q, RecordSet &rs, uint32_t first, uint32_t count, OutDev out, int G, int K,
                       int layout, cudaStream_t s);
+bool wave_fits(const Query &q, int G, int K, int layout);
+// Whether the wavefront kernels compute the reference's exact results for q on
+// rs (the safe regime); the exact kernels (exact.cu) take the rest.
+bool fast_regime(ish_ctx *ctx, const Query &q, const RecordSet &rs);
+int launch_exact(ish_ctx *ctx, Query &q, RecordSet &rs, uint32_t first, uint32_t count, OutDev out, cudaStream_t s);
+int launch_range(ish_ctx *ctx, Query &q, RecordSet &rs, uint32_t first, uint32_t count, OutDev out, cudaStream_t s);
 void drop_plans(ish_ctx *ctx, int32_t query_id, int32_t set_id);  // multi.cu
 void free_plans(ish_ctx *ctx);                                   // multi.cu
 void stop_server(ish_ctx *ctx);                                  // serve.cu

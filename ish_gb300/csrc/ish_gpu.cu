@@ -43,6 +43,8 @@ void release_query(Query &q) {
     l.second.hinit.release();
   }
   q.layouts.clear();
+  for (auto &kv : q.exact_prof) kv.second.release();
+  q.exact_prof.clear();
   if (q.reverse) release_query(*q.reverse);
   q.reverse.reset();
 }
@@ -50,6 +52,24 @@ void release_query(Query &q) {
 void release_set(RecordSet &rs) {
   DevBuf *b[] = {&rs.codes, &rs.off_s, &rs.len_s, &rs.orig_s, &rs.inv};
   for (DevBuf *x : b) x->release();
+}
+
+void compute_rows(Query &q) {
+  const int A = q.alphabet;
+  q.rowmap.assign(256, 0);
+  q.rep.clear();
+  std::map<std::vector<int8_t>, int> seen;
+  std::vector<int8_t> key(q.Q);
+  for (int c = 0; c < A; ++c) {
+    for (int j = 0; j < q.Q; ++j) key[j] = q.M[(size_t)c * A + q.q[j]];
+    auto it = seen.find(key);
+    if (it == seen.end()) {
+      it = seen.emplace(key, (int)q.rep.size()).first;
+      q.rep.push_back((uint8_t)c);
+    }
+    q.rowmap[c] = (uint8_t)it->second;
+  }
+  q.rows = (int)q.rep.size();
 }
 
 int matrix_alphabet_ok(uint32_t alphabet) { return alphabet >= 1 && alphabet <= 256; }
@@ -119,7 +139,8 @@ void choose_shape(int Q, int force_G, int force_K, int *G, int *K) {
   *K = bk;
 }
 
-uint64_t tune_key(int mode, int alphabet, int Q) { return ((uint64_t)mode << 48) | ((uint64_t)alphabet << 32) | (uint32_t)Q; }
+// Autotuner key: mode, profile rows (the profile's size) and query length.
+uint64_t tune_key(int mode, int rows, int Q) { return ((uint64_t)mode << 48) | ((uint64_t)rows << 32) | (uint32_t)Q; }
 
 // Row stride (in words) of a profile layout.  Strides are an odd number of
 // 16-byte units: the eight threads of a quarter-warp read consecutive rows
@@ -145,22 +166,22 @@ size_t layout_bytes(int layout, int alphabet, int G, int K) {
 // when a block still fits twice on an SM; else 16-bit words (one PRMT).
 int choose_layout(int alphabet, int G, int K, int mode) {
   if (layout_bytes(PROF_PAIR, alphabet, G, K) <= 64 * 1024) return PROF_PAIR;
-  if (wave_smem((uint32_t)layout_bytes(PROF_S32, alphabet, G, K), wave_block_threads(K), G, K, mode) <= 112 * 1024)
+  if (wave_smem((uint32_t)layout_bytes(PROF_S32, alphabet, G, K), wave_block_threads(K, mode), G, K, mode) <= 112 * 1024)
     return PROF_S32;
   return PROF_S16;
 }
 
 void pick_shape(ish_ctx *ctx, const Query &q, int *G, int *K, int *layout) {
   const int mode = q.algo == ISH_ALGO_LOCAL ? SW : SG;
-  auto it = ctx->tuned.find(tune_key(mode, q.alphabet, q.Q));
+  auto it = ctx->tuned.find(tune_key(mode, q.rows, q.Q));
   if (!ctx->force_G && !ctx->force_K && ctx->force_layout < 0 && it != ctx->tuned.end()) {
     *G = it->second.G;
     *K = it->second.K;
-    *layout = it->second.layout >= 0 ? it->second.layout : choose_layout(q.alphabet, *G, *K, mode);
+    *layout = it->second.layout >= 0 ? it->second.layout : choose_layout(q.rows, *G, *K, mode);
     return;
   }
   choose_shape(q.Q, ctx->force_G, ctx->force_K, G, K);
-  *layout = ctx->force_layout >= 0 ? ctx->force_layout : (*G ? choose_layout(q.alphabet, *G, *K, mode) : PROF_S16);
+  *layout = ctx->force_layout >= 0 ? ctx->force_layout : (*G ? choose_layout(q.rows, *G, *K, mode) : PROF_S16);
 }
 
 int build_wave_layout(ish_ctx *ctx, Query &q, int G, int K, int layout, WaveLayout **out) {
@@ -176,12 +197,14 @@ int build_wave_layout(ish_ctx *ctx, Query &q, int G, int K, int layout, WaveLayo
   L.d = G * K - q.Q;
   L.layout = layout;
   L.kp = layout_stride(layout, K);
-  const int A = q.alphabet;
+  // profile rows: one per class of codes with equal scores against the
+  // query (q.rep), addressed through q.rowmap when the classes merge codes
+  const int A = q.rows;
   const bool sg = q.algo == ISH_ALGO_SEMI_GLOBAL;
   const int ppad = (sg && !(q.ends & ISH_FREE_TARGET_START)) ? -(q.open + q.ext) : 0;
-  auto P = [&](int c, int col) -> int {
+  auto P = [&](int r, int col) -> int {
     if (col < 0) return ppad;
-    return q.M[(size_t)c * A + q.q[col]];
+    return q.M[(size_t)q.rep[r] * q.alphabet + q.q[col]];
   };
   std::vector<uint8_t> host;
   if (layout == PROF_PAIR) {
@@ -213,6 +236,11 @@ int build_wave_layout(ish_ctx *ctx, Query &q, int G, int K, int layout, WaveLayo
   }
   L.prof_bytes = (uint32_t)((host.size() + 15) & ~(size_t)15);
   host.resize(L.prof_bytes, 0);
+  if (q.rows < q.alphabet) {
+    L.remap_off = L.prof_bytes;
+    host.insert(host.end(), q.rowmap.begin(), q.rowmap.end());
+    L.prof_bytes += 256;
+  }
   std::vector<int16_t> hin((size_t)G * K, 0);
   for (int c = 0; c < G * K; ++c) {
     const int col = c - L.d;
@@ -246,51 +274,71 @@ int build_plain(ish_ctx *ctx, Query &q) {
   return ISH_OK;
 }
 
-// Upload and pack a record set (see k_lengths .. k_pack in kernels.cu).
-int load_records(ish_ctx *ctx, const uint8_t *records, const uint64_t *offsets, uint32_t n, RecordSet &rs) {
-  if (n == 0) {
-    rs.n = 0;
-    rs.total = 0;
-    return ISH_OK;
-  }
-  if (!offsets) return fail(ctx, ISH_EINVAL, "offsets is NULL");
-  const uint64_t base = offsets[0], end = offsets[n];
-  if (end < base) return fail(ctx, ISH_EINVAL, "offsets are not monotone");
-  const uint64_t bytes = end - base;
-  if (bytes && !records) return fail(ctx, ISH_EINVAL, "records is NULL");
-  rs.n = n;
-  rs.total = bytes;
-  cudaStream_t s = ctx->stream;
-  // raw bytes (+16 slack for the realigning pack loads)
-  CU(ctx->raw.ensure(bytes + 32));
-  if (bytes) CU(cudaMemcpyAsync(ctx->raw.p, records + base, bytes, cudaMemcpyHostToDevice, s));
-  CU(ctx->off_in.ensure((size_t)(n + 1) * 8));
-  if (base == 0) {
-    CU(cudaMemcpyAsync(ctx->off_in.p, offsets, (size_t)(n + 1) * 8, cudaMemcpyHostToDevice, s));
+// Byte -> code tables of ish's encodings (convert_ascii_to_encoding,
+// ishlib/matcher/alignment/scoring_matrix.mojo:9-27 AA_TO_NUM, 131-149
+// NT_TO_NUM): ascii is the identity; actgn / actgn0 map A/a C/c G/g T/t/U/u to
+// 0-3 and everything else to 4 (N); blosum62 maps the 23 letters of its
+// residue order (either case) to their index and everything else to 23 ('*').
+void encoding_table(int kind, uint8_t t[256]) {
+  if (kind == ISH_MATRIX_ASCII) {
+    for (int i = 0; i < 256; ++i) t[i] = (uint8_t)i;
+  } else if (kind == ISH_MATRIX_ACTGN || kind == ISH_MATRIX_ACTGN0) {
+    memset(t, 4, 256);
+    const char *groups[4] = {"Aa", "Cc", "Gg", "TtUu"};
+    for (int code = 0; code < 4; ++code)
+      for (const char *c = groups[code]; *c; ++c) t[(uint8_t)*c] = (uint8_t)code;
   } else {
-    std::vector<uint64_t> rebased(offsets, offsets + n + 1);
-    for (auto &v : rebased) v -= base;
-    CU(cudaMemcpyAsync(ctx->off_in.p, rebased.data(), (size_t)(n + 1) * 8, cudaMemcpyHostToDevice, s));
-    CU(cudaStreamSynchronize(s));
+    memset(t, 23, 256);
+    const char *order = "ARNDCQEGHILKMFPSTWYVBZX*";
+    for (int code = 0; order[code]; ++code) {
+      const uint8_t c = (uint8_t)order[code];
+      if (c >= 'A' && c <= 'Z') {
+        t[c] = (uint8_t)code;
+        t[c + 32] = (uint8_t)code;
+      }
+    }
   }
+}
+
+// Device copy of the encoding table of a matrix kind (nullptr: records are
+// already encoded).
+int device_encoding(ish_ctx *ctx, int kind, const uint8_t **out) {
+  if (kind < ISH_MATRIX_ASCII || kind > ISH_MATRIX_BLOSUM62) return fail(ctx, ISH_EINVAL, "unknown matrix kind %d", kind);
+  if (!ctx->enc_tables.p) {
+    uint8_t t[4 * 256];
+    for (int k = 0; k < 4; ++k) encoding_table(k, t + 256 * k);
+    CU(ctx->enc_tables.ensure(sizeof t));
+    CU(cudaMemcpy(ctx->enc_tables.p, t, sizeof t, cudaMemcpyHostToDevice));
+  }
+  *out = ctx->enc_tables.as<uint8_t>() + 256 * kind;
+  return ISH_OK;
+}
+
+// Sort and pack n records held in ctx->raw (raw_bytes bytes): record i is
+// raw[off_in[i] .. end[i]) with `end` on the device, or raw[off_in[i] ..
+// off_in[i + 1]) without; `enc` (device, may be null) encodes bytes on the way
+// (see k_lengths .. k_pack in kernels.cu).  rs.total must hold the residue count.
+int pack_set(ish_ctx *ctx, uint32_t n, uint64_t raw_bytes, const uint64_t *end, const uint8_t *enc, RecordSet &rs) {
+  cudaStream_t s = ctx->stream;
+  rs.n = n;
   CU(ctx->len_tmp.ensure((size_t)n * 4));
   CU(ctx->slot_tmp.ensure((size_t)n * 8));
   CU(ctx->poff_tmp.ensure((size_t)n * 8));
   CU(ctx->hist.ensure((size_t)NBUCKETS * 4 * 2));
   CU(cudaMemsetAsync(ctx->hist.p, 0, (size_t)NBUCKETS * 4, s));
   const uint32_t nb = std::min<uint32_t>(ceil_div(n, 256), (uint32_t)ctx->num_sms * 16);
-  k_lengths<<<nb, 256, 0, s>>>(ctx->off_in.as<uint64_t>(), n, ctx->len_tmp.as<uint32_t>(), ctx->slot_tmp.as<uint64_t>(),
-                                ctx->hist.as<uint32_t>());
+  k_lengths<<<nb, 256, 0, s>>>(ctx->off_in.as<uint64_t>(), end, n, ctx->len_tmp.as<uint32_t>(),
+                                ctx->slot_tmp.as<uint64_t>(), ctx->hist.as<uint32_t>());
   ++ctx->launches;
   // exclusive scan of slot sizes -> packed offsets
   const uint32_t tiles = ceil_div(n, SCAN_TILE);
+  if (tiles > SCAN_TILE) return fail(ctx, ISH_EINVAL, "too many records in one set (%u)", n);
   CU(ctx->scan_tmp.ensure((size_t)(tiles + 1) * 8 * 2));
   uint64_t *bsum = ctx->scan_tmp.as<uint64_t>();
   uint64_t *boff = bsum + tiles + 1;
   k_scan64_block<<<tiles, 1024, 0, s>>>(ctx->slot_tmp.as<uint64_t>(), ctx->poff_tmp.as<uint64_t>(), n, bsum);
   ++ctx->launches;
   if (tiles > 1) {
-    if (tiles > SCAN_TILE) return fail(ctx, ISH_EINVAL, "too many records in one set (%u)", n);
     k_scan64_block<<<1, 1024, 0, s>>>(bsum, boff, tiles, nullptr);
     ++ctx->launches;
     k_scan64_add<<<tiles, 1024, 0, s>>>(ctx->poff_tmp.as<uint64_t>(), n, boff);
@@ -307,13 +355,13 @@ int load_records(ish_ctx *ctx, const uint8_t *records, const uint64_t *offsets, 
   k_scatter<<<nb, 256, 0, s>>>(ctx->len_tmp.as<uint32_t>(), ctx->poff_tmp.as<uint64_t>(), n, ctx->hist.as<uint32_t>(),
                                rs.len_s.as<uint32_t>(), rs.off_s.as<uint64_t>(), rs.orig_s.as<uint32_t>());
   ++ctx->launches;
-  const uint64_t packed = bytes + 16ull * n + 16;
+  const uint64_t packed = rs.total + 16ull * n + 16;
   CU(rs.codes.ensure(packed));
   const uint32_t pb = std::min<uint32_t>(ceil_div((uint64_t)n * 32, 256), (uint32_t)ctx->num_sms * 32);
   CU(ctx->max_code.ensure(16));
   CU(cudaMemsetAsync(ctx->max_code.p, 0, 4, s));
-  k_pack<<<pb, 256, 0, s>>>(ctx->raw.as<uint8_t>(), bytes, ctx->off_in.as<uint64_t>(), ctx->poff_tmp.as<uint64_t>(), n,
-                            rs.codes.as<uint8_t>(), ctx->max_code.as<uint32_t>());
+  k_pack<<<pb, 256, 0, s>>>(ctx->raw.as<uint8_t>(), raw_bytes, ctx->off_in.as<uint64_t>(), end,
+                            ctx->poff_tmp.as<uint64_t>(), n, enc, rs.codes.as<uint8_t>(), ctx->max_code.as<uint32_t>());
   ++ctx->launches;
   CU(cudaGetLastError());
   CU(cudaMemcpyAsync(&rs.max_code, ctx->max_code.p, 4, cudaMemcpyDeviceToHost, s));
@@ -326,6 +374,85 @@ int load_records(ish_ctx *ctx, const uint8_t *records, const uint64_t *offsets, 
       break;
     }
   return ISH_OK;
+}
+
+// Upload and pack a record set given as concatenated records + n+1 offsets.
+int load_records(ish_ctx *ctx, const uint8_t *records, const uint64_t *offsets, uint32_t n, RecordSet &rs,
+                 const uint8_t *enc) {
+  if (n == 0) {
+    rs.n = 0;
+    rs.total = 0;
+    return ISH_OK;
+  }
+  if (!offsets) return fail(ctx, ISH_EINVAL, "offsets is NULL");
+  const uint64_t base = offsets[0], end = offsets[n];
+  if (end < base) return fail(ctx, ISH_EINVAL, "offsets are not monotone");
+  const uint64_t bytes = end - base;
+  if (bytes && !records) return fail(ctx, ISH_EINVAL, "records is NULL");
+  rs.total = bytes;
+  cudaStream_t s = ctx->stream;
+  // raw bytes (+16 slack for the realigning pack loads)
+  CU(ctx->raw.ensure(bytes + 32));
+  if (bytes) CU(cudaMemcpyAsync(ctx->raw.p, records + base, bytes, cudaMemcpyHostToDevice, s));
+  CU(ctx->off_in.ensure((size_t)(n + 1) * 8));
+  if (base == 0) {
+    CU(cudaMemcpyAsync(ctx->off_in.p, offsets, (size_t)(n + 1) * 8, cudaMemcpyHostToDevice, s));
+  } else {
+    std::vector<uint64_t> rebased(offsets, offsets + n + 1);
+    for (auto &v : rebased) v -= base;
+    CU(cudaMemcpyAsync(ctx->off_in.p, rebased.data(), (size_t)(n + 1) * 8, cudaMemcpyHostToDevice, s));
+    CU(cudaStreamSynchronize(s));
+  }
+  return pack_set(ctx, n, bytes, nullptr, enc, rs);
+}
+
+// Upload a text buffer, split it into lines on the device and pack the lines
+// as records (see k_count_newlines .. k_line_bounds in kernels.cu).
+int load_lines(ish_ctx *ctx, const uint8_t *text, uint64_t bytes, RecordSet &rs, const uint8_t *enc, uint32_t *n_out) {
+  *n_out = 0;
+  rs.n = 0;
+  rs.total = 0;
+  if (bytes == 0) return ISH_OK;
+  if (!text) return fail(ctx, ISH_EINVAL, "text is NULL");
+  cudaStream_t s = ctx->stream;
+  CU(ctx->raw.ensure(bytes + 32));
+  CU(cudaMemcpyAsync(ctx->raw.p, text, bytes, cudaMemcpyHostToDevice, s));
+  const uint64_t tiles64 = (bytes + LINE_TILE - 1) / LINE_TILE;
+  if (tiles64 > 0x7fffffffull) return fail(ctx, ISH_EINVAL, "text too large");
+  const uint32_t tiles = (uint32_t)tiles64;
+  CU(ctx->block_counts.ensure((size_t)tiles * 4 + 8));
+  CU(ctx->nhits.ensure(16));
+  k_count_newlines<<<tiles, 1024, 0, s>>>(ctx->raw.as<uint8_t>(), bytes, ctx->block_counts.as<uint32_t>());
+  ++ctx->launches;
+  k_scan_counts<<<1, 1024, 0, s>>>(ctx->block_counts.as<uint32_t>(), tiles, ctx->nhits.as<uint32_t>());
+  ++ctx->launches;
+  uint32_t n_nl = 0;
+  uint8_t last = 0;
+  CU(cudaMemcpyAsync(&n_nl, ctx->nhits.p, 4, cudaMemcpyDeviceToHost, s));
+  CU(cudaStreamSynchronize(s));
+  last = text[bytes - 1];
+  const uint64_t lines = (uint64_t)n_nl + (last != '\n' ? 1 : 0);
+  if (lines >= 0xffffffffull) return fail(ctx, ISH_EINVAL, "too many lines (%llu)", (unsigned long long)lines);
+  const uint32_t n = (uint32_t)lines;
+  CU(ctx->nl_pos.ensure((size_t)n_nl * 8 + 8));
+  CU(ctx->off_in.ensure((size_t)(n + 1) * 8));
+  CU(ctx->line_end.ensure((size_t)n * 8 + 8));
+  k_write_newlines<<<tiles, 1024, 0, s>>>(ctx->raw.as<uint8_t>(), bytes, ctx->block_counts.as<uint32_t>(),
+                                          ctx->nl_pos.as<uint64_t>());
+  ++ctx->launches;
+  CU(cudaMemsetAsync(ctx->nhits.p, 0, 16, s));
+  k_line_bounds<<<std::max<uint32_t>(1, std::min<uint32_t>(ceil_div(n, 256), (uint32_t)ctx->num_sms * 16)), 256, 0,
+                  s>>>(ctx->raw.as<uint8_t>(), bytes, ctx->nl_pos.as<uint64_t>(), n_nl, n, ctx->off_in.as<uint64_t>(),
+                       ctx->line_end.as<uint64_t>(), reinterpret_cast<unsigned long long *>(ctx->nhits.p));
+  ++ctx->launches;
+  CU(cudaGetLastError());
+  // residues: the text minus the newlines and the dropped carriage returns
+  unsigned long long total = 0;
+  CU(cudaMemcpyAsync(&total, ctx->nhits.p, 8, cudaMemcpyDeviceToHost, s));
+  CU(cudaStreamSynchronize(s));
+  rs.total = total;
+  *n_out = n;
+  return pack_set(ctx, n, bytes, ctx->line_end.as<uint64_t>(), enc, rs);
 }
 
 // Number of records (a prefix of the descending order) whose length bucket
@@ -363,7 +490,8 @@ void wave_params(const Query &q, const WaveLayout &L, const RecordSet &rs, OutDe
   p.K = L.K;
   p.d = L.d;
   p.kp = L.kp;
-  p.alphabet = q.alphabet;
+  p.alphabet = q.rows;
+  p.remap_off = L.remap_off;
   p.layout = L.layout;
   p.lane_mul = 65536u;
   p.open = q.open;
@@ -382,9 +510,9 @@ void wave_params(const Query &q, const WaveLayout &L, const RecordSet &rs, OutDe
 }
 
 // Shared memory of a wavefront block: the profile, 32 slot words per group,
-// and (local alignment) 2 * KP4 save words per thread (see wave.cuh).
+// and (local alignment) wave_save_words(K) save words per thread (see wave.cuh).
 size_t wave_smem(uint32_t prof_area, int threads, int G, int K, int mode) {
-  const size_t save = mode == SW ? (size_t)threads * 2 * ((K + 3) & ~3) * 4 : 0;
+  const size_t save = mode == SW ? (size_t)threads * wave_save_words(K) * 4 : 0;
   return prof_area + (size_t)(threads / G) * 32 * 4 + save;
 }
 
@@ -398,10 +526,23 @@ int launch_wave_range(ish_ctx *ctx, Query &q, RecordSet &rs, uint32_t first, uin
   const int mode = q.algo == ISH_ALGO_LOCAL ? SW : SG;
   WaveFn fn = wave_fn(K, mode, L->layout);
   if (!fn) return fail(ctx, ISH_EOVERFLOW, "no wavefront kernel for K=%d", K);
-  const int threads = wave_block_threads(K);
+  const int threads = wave_block_threads(K, mode);
   const int groups = threads / G;
   const size_t smem = wave_smem((L->prof_bytes + 15) & ~15u, threads, G, K, mode);
-  CU(cudaFuncSetAttribute((const void *)fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  {
+    const cudaError_t e = cudaFuncSetAttribute((const void *)fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) {
+      (void)cudaGetLastError();
+      cudaFuncAttributes a{};
+      const cudaError_t ea = cudaFuncGetAttributes(&a, (const void *)fn);
+      (void)cudaGetLastError();
+      return fail(ctx, ISH_EDEVICE,
+                  "wavefront kernel K=%d mode=%d layout=%d: dynamic shared memory %zu bytes refused (%s); kernel "
+                  "attributes (%s): static %zu, max dynamic %d, %d registers",
+                  K, mode, L->layout, smem, cudaGetErrorString(e), cudaGetErrorString(ea), a.sharedSizeBytes,
+                  a.maxDynamicSharedSizeBytes, a.numRegs);
+    }
+  }
   int per_sm = 0;
   CU(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, (const void *)fn, threads, smem));
   if (per_sm < 1) return fail(ctx, ISH_EOVERFLOW, "wavefront kernel K=%d does not fit (smem %zu)", K, smem);
@@ -484,12 +625,42 @@ int fast_check(const Query &q, const RecordSet &rs, int G, int K, char *msg, siz
   return ISH_OK;
 }
 
+bool fast_regime(ish_ctx *ctx, const Query &q, const RecordSet &rs) {
+  int G, K, layout;
+  pick_shape(ctx, q, &G, &K, &layout);
+  char msg[256];
+  return fast_check(q, rs, G, K, msg, sizeof msg) == ISH_OK;
+}
+
 int check_fast(ish_ctx *ctx, const Query &q, const RecordSet &rs) {
   int G, K, layout;
   pick_shape(ctx, q, &G, &K, &layout);
   char msg[256];
   const int rc = fast_check(q, rs, G, K, msg, sizeof msg);
   return rc ? fail(ctx, rc, "%s", msg) : ISH_OK;
+}
+
+// Whether the wavefront kernel's shared memory (profile, code -> row table,
+// slots, saved rows) fits in a block for this shape and layout.
+bool wave_fits(const Query &q, int G, int K, int layout) {
+  if (!G) return false;
+  const int mode = q.algo == ISH_ALGO_LOCAL ? SW : SG;
+  size_t prof = (layout_bytes(layout, q.rows, G, K) + 15) & ~(size_t)15;
+  if (q.rows < q.alphabet) prof += 256;
+  return wave_smem((uint32_t)prof, wave_block_threads(K, mode), G, K, mode) <= 227 * 1024;
+}
+
+// The wavefront kernel, or the plain kernel when the wavefront profile does
+// not fit in shared memory (long queries over large alphabets) or the plain
+// kernel was asked for.
+int launch_range(ish_ctx *ctx, Query &q, RecordSet &rs, uint32_t first, uint32_t count, OutDev out, cudaStream_t s) {
+  int G, K, layout;
+  pick_shape(ctx, q, &G, &K, &layout);
+  if (ctx->kernel == ISH_KERNEL_PLAIN || !wave_fits(q, G, K, layout)) {
+    if (s != ctx->stream) return fail(ctx, ISH_EINVAL, "the plain kernel runs on the context stream only");
+    return launch_plain(ctx, q, rs, first, count, out);
+  }
+  return launch_wave_range(ctx, q, rs, first, count, out, G, K, layout, s);
 }
 
 // Score query q against set rs into the context's device output buffers.
@@ -514,15 +685,13 @@ int run_scoring(ish_ctx *ctx, Query &q, RecordSet &rs) {
     CU(cudaGetLastError());
   }
   if (nonempty) {
-    rc = check_fast(ctx, q, rs);
-    if (rc) return rc;
-    if (ctx->kernel == ISH_KERNEL_PLAIN) {
-      rc = launch_plain(ctx, q, rs, 0, nonempty, out);
-    } else {
-      int G, K, layout;
-      pick_shape(ctx, q, &G, &K, &layout);
-      rc = launch_wave_range(ctx, q, rs, 0, nonempty, out, G, K, layout, s);
-    }
+    if (rs.max_code >= (uint32_t)q.alphabet)
+      return fail(ctx, ISH_EINVAL, "a record contains code %u >= the alphabet size %d of the query", rs.max_code,
+                  q.alphabet);
+    if (ctx->kernel == ISH_KERNEL_EXACT || !fast_regime(ctx, q, rs))
+      rc = launch_exact(ctx, q, rs, 0, nonempty, out, s);
+    else
+      rc = launch_range(ctx, q, rs, 0, nonempty, out, s);
     if (rc) return rc;
   }
   return ISH_OK;
@@ -611,7 +780,8 @@ void ish_gpu_close(ish_ctx *ctx) {
   for (auto &kv : ctx->sets) release_set(kv.second);
   DevBuf *bufs[] = {&ctx->raw, &ctx->off_in, &ctx->len_tmp, &ctx->slot_tmp, &ctx->poff_tmp, &ctx->hist, &ctx->max_code,
                     &ctx->scan_tmp, &ctx->counter, &ctx->error, &ctx->out_score, &ctx->out_qend, &ctx->out_tend,
-                    &ctx->out_hit, &ctx->hit_idx, &ctx->block_counts, &ctx->nhits, &ctx->plain_scratch};
+                    &ctx->out_hit, &ctx->hit_idx, &ctx->block_counts, &ctx->nhits, &ctx->plain_scratch,
+                    &ctx->enc_tables, &ctx->nl_pos, &ctx->line_end, &ctx->exact_scratch, &ctx->exact_redo};
   for (DevBuf *b : bufs) b->release();
   cudaEventDestroy(ctx->ev0);
   cudaEventDestroy(ctx->ev1);
@@ -697,6 +867,7 @@ int ish_gpu_set_query(ish_ctx *ctx, const uint8_t *enc_query, uint32_t qlen, int
     q.mmax = std::max<int>(q.mmax, v);
   }
   q.neg_limit = neg_limit_of(q.open, q.mmin);
+  compute_rows(q);
   cudaSetDevice(ctx->device);
   const int32_t id = ctx->next_query++;
   ctx->queries.emplace(id, std::move(q));
@@ -719,7 +890,7 @@ int ish_gpu_records_load(ish_ctx *ctx, const uint8_t *records, const uint64_t *o
   if (!ctx || !set_id) return ctx ? fail(ctx, ISH_EINVAL, "set_id is NULL") : ISH_EINVAL;
   cudaSetDevice(ctx->device);
   RecordSet rs;
-  int rc = load_records(ctx, records, offsets, n, rs);
+  int rc = load_records(ctx, records, offsets, n, rs, nullptr);
   if (rc) {
     release_set(rs);
     return rc;
@@ -727,6 +898,46 @@ int ish_gpu_records_load(ish_ctx *ctx, const uint8_t *records, const uint64_t *o
   const int32_t id = ctx->next_set++;
   ctx->sets.emplace(id, std::move(rs));
   *set_id = id;
+  return ISH_OK;
+}
+
+int ish_gpu_records_load_raw(ish_ctx *ctx, const uint8_t *raw, const uint64_t *offsets, uint32_t n, int matrix_kind,
+                             int32_t *set_id) {
+  if (!ctx || !set_id) return ctx ? fail(ctx, ISH_EINVAL, "set_id is NULL") : ISH_EINVAL;
+  cudaSetDevice(ctx->device);
+  const uint8_t *enc = nullptr;
+  int rc = device_encoding(ctx, matrix_kind, &enc);
+  if (rc) return rc;
+  RecordSet rs;
+  rc = load_records(ctx, raw, offsets, n, rs, enc);
+  if (rc) {
+    release_set(rs);
+    return rc;
+  }
+  const int32_t id = ctx->next_set++;
+  ctx->sets.emplace(id, std::move(rs));
+  *set_id = id;
+  return ISH_OK;
+}
+
+int ish_gpu_records_load_lines(ish_ctx *ctx, const uint8_t *text, uint64_t bytes, int matrix_kind, int32_t *set_id,
+                               uint32_t *n_records) {
+  if (!ctx || !set_id) return ctx ? fail(ctx, ISH_EINVAL, "set_id is NULL") : ISH_EINVAL;
+  cudaSetDevice(ctx->device);
+  const uint8_t *enc = nullptr;
+  int rc = device_encoding(ctx, matrix_kind, &enc);
+  if (rc) return rc;
+  RecordSet rs;
+  uint32_t n = 0;
+  rc = load_lines(ctx, text, bytes, rs, enc, &n);
+  if (rc) {
+    release_set(rs);
+    return rc;
+  }
+  const int32_t id = ctx->next_set++;
+  ctx->sets.emplace(id, std::move(rs));
+  *set_id = id;
+  if (n_records) *n_records = n;
   return ISH_OK;
 }
 
@@ -775,7 +986,7 @@ int ish_gpu_score(ish_ctx *ctx, int32_t query_id, const uint8_t *records, const 
   if (qi == ctx->queries.end()) return fail(ctx, ISH_EINVAL, "unknown query %d", query_id);
   cudaSetDevice(ctx->device);
   RecordSet rs;
-  int rc = load_records(ctx, records, offsets, n, rs);
+  int rc = load_records(ctx, records, offsets, n, rs, nullptr);
   if (!rc) rc = run_scoring(ctx, qi->second, rs);
   if (!rc) rc = fetch_outputs(ctx, n, score, query_end, target_end, hit, hit_idx, n_hits);
   cudaStreamSynchronize(ctx->stream);

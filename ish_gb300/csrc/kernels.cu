@@ -21,10 +21,16 @@ __device__ __forceinline__ uint32_t len_bucket(uint64_t len) {
   return b > NBUCKETS - 1 ? NBUCKETS - 1 : (uint32_t)b;
 }
 
-__global__ void k_lengths(const uint64_t *off, uint32_t n, uint32_t *len, uint64_t *slot_bytes,
+// Record i is src[off[i] .. end[i]) when `end` is given, else
+// src[off[i] .. off[i + 1]) (one concatenated array).
+__device__ __forceinline__ uint64_t rec_len(const uint64_t *off, const uint64_t *end, uint32_t i) {
+  return (end ? end[i] : off[i + 1]) - off[i];
+}
+
+__global__ void k_lengths(const uint64_t *off, const uint64_t *end, uint32_t n, uint32_t *len, uint64_t *slot_bytes,
                           uint32_t *hist) {
   for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-    const uint64_t l = off[i + 1] - off[i];
+    const uint64_t l = rec_len(off, end, i);
     len[i] = (uint32_t)l;
     slot_bytes[i] = (l + 15) & ~(uint64_t)15;
     atomicAdd(&hist[len_bucket(l)], 1u);
@@ -67,12 +73,19 @@ __global__ void k_scatter(const uint32_t *len, const uint64_t *poff, uint32_t n,
   }
 }
 
-// One warp per record: copy src[off[i] .. off[i+1]) to dst[poff[i] ..) with
-// 16-byte stores, realigning 4-byte words with funnel shifts; the tail of the
-// 16-byte slot is zero-filled.  The largest code of the set is reduced into
+// One warp per record: the record is copied to dst[poff[i] ..) in 16-byte
+// chunks realigned with funnel shifts, optionally encoded through a 256-entry
+// byte table (ish's convert_ascii_to_encoding, done per byte on the host by
+// the runners, ishlib/parallel_line_search_runner.mojo:90-94); the tail of the
+// 16-byte slot is zero-filled, and the largest code of the set is reduced into
 // *max_code, so a query's alphabet can be checked once per set.
-__global__ void k_pack(const uint8_t *src, uint64_t src_bytes, const uint64_t *off, const uint64_t *poff,
-                       uint32_t n, uint8_t *dst, uint32_t *max_code) {
+__global__ void k_pack(const uint8_t *src, uint64_t src_bytes, const uint64_t *off, const uint64_t *end,
+                       const uint64_t *poff, uint32_t n, const uint8_t *enc, uint8_t *dst, uint32_t *max_code) {
+  __shared__ uint8_t table[256];
+  if (enc) {
+    for (int i = threadIdx.x; i < 256; i += blockDim.x) table[i] = enc[i];
+    __syncthreads();
+  }
   const uint32_t warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const uint32_t lane = threadIdx.x & 31;
   const uint32_t nwarps = (gridDim.x * blockDim.x) >> 5;
@@ -80,7 +93,7 @@ __global__ void k_pack(const uint8_t *src, uint64_t src_bytes, const uint64_t *o
   const uint64_t nwords = (src_bytes + 3) >> 2;
   uint32_t mx = 0;
   for (uint32_t r = warp; r < n; r += nwarps) {
-    const uint64_t s0 = off[r], len = off[r + 1] - off[r];
+    const uint64_t s0 = off[r], len = rec_len(off, end, r);
     uint4 *d = reinterpret_cast<uint4 *>(dst + poff[r]);
     const uint64_t nchunks = (len + 15) >> 4;
     for (uint64_t c = lane; c < nchunks; c += 32) {
@@ -93,6 +106,14 @@ __global__ void k_pack(const uint8_t *src, uint64_t src_bytes, const uint64_t *o
       uint32_t o[4];
 #pragma unroll
       for (int k = 0; k < 4; ++k) o[k] = __funnelshift_r(w[k], w[k + 1], sh);
+      if (enc) {
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+          const uint32_t x = o[k];
+          o[k] = (uint32_t)table[x & 0xffu] | ((uint32_t)table[(x >> 8) & 0xffu] << 8) |
+                 ((uint32_t)table[(x >> 16) & 0xffu] << 16) | ((uint32_t)table[x >> 24] << 24);
+        }
+      }
       // zero bytes past the record end
       const uint64_t rem = len - c * 16;
       if (rem < 16) {
@@ -110,6 +131,71 @@ __global__ void k_pack(const uint8_t *src, uint64_t src_bytes, const uint64_t *o
   uint32_t m = max(max(mx & 0xffu, (mx >> 8) & 0xffu), max((mx >> 16) & 0xffu, mx >> 24));
   for (int o = 16; o > 0; o >>= 1) m = max(m, __shfl_xor_sync(0xffffffffu, m, o));
   if (lane == 0 && m) atomicMax(max_code, m);
+}
+
+// ---------------------------------------------------------------------------
+// Line splitting: the records of a text buffer are its lines, as ish's line
+// reader cuts them (ishlib/vendor/kseq.mojo:270-330, read_until with the
+// newline delimiter): lines end at '\n', a trailing '\r' is dropped from lines
+// longer than one byte, a final line without '\n' is a record, and a final
+// '\n' does not start another one.
+// ---------------------------------------------------------------------------
+__global__ void k_count_newlines(const uint8_t *text, uint64_t bytes, uint32_t *block_counts) {
+  __shared__ uint32_t wsum[32];
+  const uint64_t base = (uint64_t)blockIdx.x * LINE_TILE;
+  uint32_t c = 0;
+  for (uint64_t i = base + threadIdx.x; i < bytes && i < base + LINE_TILE; i += blockDim.x) c += text[i] == '\n';
+  for (int o = 16; o > 0; o >>= 1) c += __shfl_down_sync(0xffffffffu, c, o);
+  if ((threadIdx.x & 31) == 0) wsum[threadIdx.x >> 5] = c;
+  __syncthreads();
+  if (threadIdx.x < 32) {
+    uint32_t v = threadIdx.x < (blockDim.x >> 5) ? wsum[threadIdx.x] : 0;
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+    if (threadIdx.x == 0) block_counts[blockIdx.x] = v;
+  }
+}
+
+// Positions of the newlines, in order (block_offsets: exclusive scan of the
+// per-block counts).
+__global__ void k_write_newlines(const uint8_t *text, uint64_t bytes, const uint32_t *block_offsets, uint64_t *pos) {
+  __shared__ uint32_t wsum[32];
+  __shared__ uint32_t run;
+  const uint64_t base = (uint64_t)blockIdx.x * LINE_TILE;
+  if (threadIdx.x == 0) run = block_offsets[blockIdx.x];
+  __syncthreads();
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  for (uint64_t b = base; b < bytes && b < base + LINE_TILE; b += blockDim.x) {
+    const uint64_t i = b + threadIdx.x;
+    const bool h = i < bytes && i < base + LINE_TILE && text[i] == '\n';
+    const uint32_t m = __ballot_sync(0xffffffffu, h);
+    if (lane == 0) wsum[wid] = __popc(m);
+    __syncthreads();
+    uint32_t before = 0, total = 0;
+    for (int w = 0; w < nw; ++w) {
+      if (w < wid) before += wsum[w];
+      total += wsum[w];
+    }
+    if (h) pos[run + before + __popc(m & ((1u << lane) - 1u))] = i;
+    __syncthreads();
+    if (threadIdx.x == 0) run += total;
+    __syncthreads();
+  }
+}
+
+// Line i's bounds; *total accumulates the residues of all lines.
+__global__ void k_line_bounds(const uint8_t *text, uint64_t bytes, const uint64_t *nl, uint32_t n_nl, uint32_t n_lines,
+                              uint64_t *start, uint64_t *end, unsigned long long *total) {
+  unsigned long long sum = 0;
+  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n_lines; i += gridDim.x * blockDim.x) {
+    const uint64_t s = i == 0 ? 0 : nl[i - 1] + 1;
+    uint64_t e = i < n_nl ? nl[i] : bytes;
+    if (e - s > 1 && text[e - 1] == '\r') --e;
+    start[i] = s;
+    end[i] = e;
+    sum += e - s;
+  }
+  for (int o = 16; o > 0; o >>= 1) sum += __shfl_down_sync(0xffffffffu, sum, o);
+  if ((threadIdx.x & 31) == 0 && sum) atomicAdd(total, sum);
 }
 
 // Exclusive scan of uint64 values (n <= 1024 * 1024 * 16 per call level).

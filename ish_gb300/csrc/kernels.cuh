@@ -10,12 +10,18 @@ constexpr uint32_t NBUCKETS = 65536;     // length buckets of the record sort
 constexpr uint32_t SCAN_TILE = 4096;     // values per block of k_scan64_block (1024 threads)
 constexpr uint32_t HIT_TILE = 8192;      // records per block of the hit compaction
 
-__global__ void k_lengths(const uint64_t *off, uint32_t n, uint32_t *len, uint64_t *slot_bytes, uint32_t *hist);
+constexpr uint32_t LINE_TILE = 65536;    // text bytes per block of the line splitter
+__global__ void k_lengths(const uint64_t *off, const uint64_t *end, uint32_t n, uint32_t *len, uint64_t *slot_bytes,
+                          uint32_t *hist);
 __global__ void k_bucket_scan(uint32_t *hist);
 __global__ void k_scatter(const uint32_t *len, const uint64_t *poff, uint32_t n, uint32_t *cursor, uint32_t *len_s,
                           uint64_t *off_s, uint32_t *orig_s);
-__global__ void k_pack(const uint8_t *src, uint64_t src_bytes, const uint64_t *off, const uint64_t *poff, uint32_t n,
-                       uint8_t *dst, uint32_t *max_code);
+__global__ void k_pack(const uint8_t *src, uint64_t src_bytes, const uint64_t *off, const uint64_t *end,
+                       const uint64_t *poff, uint32_t n, const uint8_t *enc, uint8_t *dst, uint32_t *max_code);
+__global__ void k_count_newlines(const uint8_t *text, uint64_t bytes, uint32_t *block_counts);
+__global__ void k_write_newlines(const uint8_t *text, uint64_t bytes, const uint32_t *block_offsets, uint64_t *pos);
+__global__ void k_line_bounds(const uint8_t *text, uint64_t bytes, const uint64_t *nl, uint32_t n_nl, uint32_t n_lines,
+                              uint64_t *start, uint64_t *end, unsigned long long *total);
 __global__ void k_scan64_block(const uint64_t *in, uint64_t *out, uint32_t n, uint64_t *block_sums);
 __global__ void k_scan64_add(uint64_t *out, uint32_t n, const uint64_t *block_offsets);
 __global__ void k_trivial(RecordsDev rec, uint32_t first, uint32_t count, int mode, int qlen, OutDev out, Decision dec);
@@ -33,9 +39,19 @@ __global__ void k_gather_hits(const uint32_t *idx, const uint32_t *count, const 
 constexpr int WAVE_KMAX = 64;
 // Threads per block and blocks per SM (the register budget): 256 x 2 up to
 // K = 32 columns per thread, 128 x 3 up to K = 48 (12 warps per SM for wide
-// rows), 128 x 2 above.
-__host__ __device__ constexpr int wave_block_threads(int K) { return K <= 32 ? 256 : 128; }
-__host__ __device__ constexpr int wave_blocks_per_sm(int K) { return K <= 32 ? 2 : (K <= 48 ? 3 : 2); }
+// rows), above that 128 x 2 for semi-global and 256 x 1 for local alignment
+// (whose long-query profiles and saved rows would otherwise fit only one
+// 128-thread block per SM: +46 % at Q = 1900).
+__host__ __device__ constexpr int wave_block_threads(int K, int mode) {
+  return K <= 32 ? 256 : (K <= 48 ? 128 : (mode == 1 ? 256 : 128));
+}
+__host__ __device__ constexpr int wave_blocks_per_sm(int K, int mode) {
+  return K <= 32 ? 2 : (K <= 48 ? 3 : (mode == 1 ? 1 : 2));
+}
+// Local alignment keeps, per thread, the H row of each lane's last
+// improvement as 16-bit values: two arrays of K (rounded up to 8) halves,
+// strided by an odd number of 16-byte units.
+__host__ __device__ constexpr int wave_save_words(int K) { return ((((K + 7) & ~7) / 4) | 1) * 4; }
 typedef void (*WaveFn)(const WaveParams);
 // Returns the kernel for (K, mode, profile layout) or nullptr.
 WaveFn wave_fn(int K, int mode, int layout);

@@ -125,6 +125,10 @@ int build_plan(ish_ctx *ctx, const int32_t *qids, uint32_t nq, int32_t set_id, R
     if (!m.G || m.G * m.K < q.Q + 1)
       return fail(ctx, ISH_EOVERFLOW, "no wavefront shape for a query of %d residues", q.Q);
     m.mode = q.algo == ISH_ALGO_LOCAL ? SW : SG;
+    if (!wave_fits(q, m.G, m.K, m.layout))
+      return fail(ctx, ISH_EOVERFLOW,
+                  "query %d (%d residues, %d profile rows) does not fit a batched launch; score it with "
+                  "ish_gpu_score_set", qids[i], q.Q, q.rows);
     rc = build_wave_layout(ctx, q, m.G, m.K, m.layout, &m.L);
     if (rc) return rc;
     m.layout = m.L->layout;
@@ -152,9 +156,9 @@ int build_plan(ish_ctx *ctx, const int32_t *qids, uint32_t nq, int32_t set_id, R
   for (MultiClass &c : P.classes) {
     c.fn = batch_fn(c.K, c.mode, c.layout);
     if (!c.fn) return fail(ctx, ISH_EOVERFLOW, "no batch kernel for K=%d", c.K);
-    c.threads = wave_block_threads(c.K);
+    c.threads = wave_block_threads(c.K, c.mode);
     const size_t slot_words = (size_t)(c.threads / c.Gmin) * 32;
-    const size_t save = c.mode == SW ? (size_t)c.threads * 2 * ((c.K + 3) & ~3) * 4 : 0;
+    const size_t save = c.mode == SW ? (size_t)c.threads * wave_save_words(c.K) * 4 : 0;
     c.smem = c.prof_area + slot_words * 4 + save;
     CU(cudaFuncSetAttribute((const void *)c.fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)c.smem));
     int per_sm = 0;
@@ -417,7 +421,7 @@ int ish_gpu_autotune(ish_ctx *ctx, int32_t set_id, const int32_t *query_ids, uin
     }
     Query &q = qi->second;
     const int mode = q.algo == ISH_ALGO_LOCAL ? SW : SG;
-    const uint64_t key = tune_key(mode, q.alphabet, q.Q);
+    const uint64_t key = tune_key(mode, q.rows, q.Q);
     if (q.Q > 0 && nonempty > 0 && !ctx->tuned.count(key)) {
       if ((rc = check_fast(ctx, q, rs))) break;
       // candidates: every group size whose modelled cost is within 1.6x of
@@ -437,11 +441,11 @@ int ish_gpu_autotune(ish_ctx *ctx, int32_t set_id, const int32_t *query_ids, uin
         // the layout rule's pick, and the 16/32-bit alternative to it (the
         // 32-bit profile saves an ALU instruction per column but can cost
         // occupancy)
-        const int pick = choose_layout(q.alphabet, g, k, mode);
+        const int pick = choose_layout(q.rows, g, k, mode);
         cands.push_back({g, k, pick, m});
         const int other = pick == PROF_S32 ? PROF_S16 : (pick == PROF_S16 ? PROF_S32 : -1);
         if (other >= 0 &&
-            wave_smem((uint32_t)layout_bytes(other, q.alphabet, g, k), wave_block_threads(k), g, k, mode) <= 227 * 1024)
+            wave_smem((uint32_t)layout_bytes(other, q.rows, g, k), wave_block_threads(k, mode), g, k, mode) <= 227 * 1024)
           cands.push_back({g, k, other, m});
       }
       cands.erase(std::remove_if(cands.begin(), cands.end(), [&](const Cand &c) { return c.model > 1.6 * best_model; }),

@@ -171,6 +171,7 @@ void finish(Server &S, Request *r) {
   do {                                                                             \
     cudaError_t _e = (call);                                                       \
     if (_e != cudaSuccess) {                                                       \
+      (void)cudaGetLastError();                                                    \
       snprintf(msg, 256, "%s: %s", #call, cudaGetErrorString(_e));                 \
       return _e == cudaErrorMemoryAllocation ? ISH_ENOMEM : ISH_EDEVICE;           \
     }                                                                              \
@@ -183,6 +184,10 @@ int admit(Server &S, Request *r, char *msg, size_t) {
   if (r->q.Q > 0 && rs.n > rs.n_empty) {
     int rc = fast_check(r->q, rs, r->G, r->K, msg, 256);
     if (rc) return rc;
+    if (!wave_fits(r->q, r->G, r->K, r->layout)) {
+      snprintf(msg, 256, "query of %d residues (%d profile rows) does not fit the serving kernels", r->q.Q, r->q.rows);
+      return ISH_EOVERFLOW;
+    }
     rc = build_wave_layout(S.ctx, r->q, r->G, r->K, r->layout, &r->L);
     if (rc) {
       snprintf(msg, 256, "profile upload failed");
@@ -285,9 +290,9 @@ int step(Server &S, char *msg) {
         snprintf(msg, 256, "no batch kernel for K=%d", C.K);
         return ISH_EOVERFLOW;
       }
-      const int threads = wave_block_threads(C.K);
+      const int threads = wave_block_threads(C.K, C.mode);
       const size_t slot_words = (size_t)(threads / C.Gmin) * 32;
-      const size_t save = C.mode == SW ? (size_t)threads * 2 * ((C.K + 3) & ~3) * 4 : 0;
+      const size_t save = C.mode == SW ? (size_t)threads * wave_save_words(C.K) * 4 : 0;
       const size_t smem = C.prof_area + slot_words * 4 + save;
       SCU(cudaFuncSetAttribute((const void *)fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
       int per_sm = 0;

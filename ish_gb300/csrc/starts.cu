@@ -112,19 +112,18 @@ extern "C" int ish_gpu_match_starts(ish_ctx *ctx, int32_t query_id, int32_t set_
   for (uint32_t i = 0; i < n_hits; ++i)
     if (hit_idx[i] >= n) return fail(ctx, ISH_EINVAL, "hit index %u >= %u records", hit_idx[i], n);
   Query &rq = reverse_of(q);
-  int G = 0, K = 0, layout = 0;
-  if (rq.Q > 0) {  // an empty query scores nothing: reverse end 0, start = len(prefix) - 1
+  // the reverse pass runs where the forward pass ran: the wavefront kernels
+  // in their exact regime, else the lane-exact emulation (exact.cu)
+  bool fast = rq.Q > 0 && ctx->kernel != ISH_KERNEL_EXACT;
+  if (fast) {
+    int G, K, layout;
     pick_shape(ctx, rq, &G, &K, &layout);
     Regime r = regime(rq, G ? G * K : rq.Q + 64);
-    if (!r.fast || !G || G * K < rq.Q + 1)
-      return fail(ctx, ISH_EINVAL, "start finding: parameters outside the exact-integer fast regime");
-    if (r.max_safe_len != ~0ull && rs.max_len > r.max_safe_len)
-      return fail(ctx, ISH_EINVAL, "start finding: records longer than %llu residues with a non-free target end",
-                  (unsigned long long)r.max_safe_len);
-    if (rs.max_code >= (uint32_t)rq.alphabet)
-      return fail(ctx, ISH_EINVAL, "a record contains code %u >= the alphabet size %d of the query", rs.max_code,
-                  rq.alphabet);
+    fast = r.fast && G && G * K >= rq.Q + 1 && (r.max_safe_len == ~0ull || rs.max_len <= r.max_safe_len);
   }
+  if (rq.Q > 0 && rs.max_code >= (uint32_t)rq.alphabet)
+    return fail(ctx, ISH_EINVAL, "a record contains code %u >= the alphabet size %d of the query", rs.max_code,
+                rq.alphabet);
   cudaStream_t s = ctx->stream;
   const uint32_t nb = std::max<uint32_t>(1, std::min<uint32_t>(ceil_div(n, 256), (uint32_t)ctx->num_sms * 8));
   if (!rs.inv.p) {
@@ -152,6 +151,7 @@ extern "C" int ish_gpu_match_starts(ish_ctx *ctx, int32_t query_id, int32_t set_
   {                                                                                                \
     cudaError_t _e = (call);                                                                       \
     if (_e != cudaSuccess) {                                                                       \
+      (void)cudaGetLastError();                                                                    \
       rc = fail(ctx, _e == cudaErrorMemoryAllocation ? ISH_ENOMEM : ISH_EDEVICE, "%s: %s", #call,  \
                 cudaGetErrorString(_e));                                                           \
       break;                                                                                       \
@@ -209,7 +209,7 @@ extern "C" int ish_gpu_match_starts(ish_ctx *ctx, int32_t query_id, int32_t set_
     rev.orig_s.p = orig.p;
     SCU(cudaMemsetAsync(rev_end.p, 0, (size_t)n_hits * 4, s));
     OutDev out{nullptr, nullptr, rev_end.as<int32_t>(), nullptr};
-    if (rq.Q > 0) rc = launch_wave_range(ctx, rq, rev, 0, n_hits, out, G, K, layout, s);
+    if (rq.Q > 0) rc = fast ? launch_range(ctx, rq, rev, 0, n_hits, out, s) : launch_exact(ctx, rq, rev, 0, n_hits, out, s);
     rev.off_s.p = rev.len_s.p = rev.orig_s.p = nullptr;  // owned by poff / rlen / orig
     if (rc) break;
     k_starts<<<hb, 256, 0, s>>>(rlen.as<uint32_t>(), rev_end.as<int32_t>(), n_hits, d_start.as<int64_t>());

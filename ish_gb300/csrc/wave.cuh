@@ -41,7 +41,7 @@ namespace ish {
 // Scores sorted entries [p.first, p.first + p.count) of the record set: the
 // groups of the calling block take record pairs from *counter until none are
 // left.  `prof` is the profile in shared memory; `slots_all` holds 32 words per
-// group (pair indices in flight), `save_all` 2 * KP4 words per thread (local
+// group (pair indices in flight), `save_all` wave_save_words(K) words per thread (local
 // alignment only).
 template <int K, int MODE, int LAYOUT>
 __device__ __forceinline__ void wave_rows(const WaveParams &p, const unsigned char *prof, uint32_t *slots_all,
@@ -52,9 +52,9 @@ __device__ __forceinline__ void wave_rows(const WaveParams &p, const unsigned ch
   const int t = lane & (G - 1);
   uint32_t *slots = slots_all + (tid / G) * 32;
   // local alignment: per thread, the H row of the last improvement of each lane
-  constexpr int KP4 = (K + 3) & ~3;
-  uint32_t *saveA = save_all + tid * 2 * KP4;
-  uint32_t *saveB = saveA + KP4;
+  constexpr int KP8 = (K + 7) & ~7;
+  uint16_t *saveA = reinterpret_cast<uint16_t *>(save_all + tid * wave_save_words(K));
+  uint16_t *saveB = saveA + KP8;
 
   const unsigned FULL = 0xffffffffu;
   const uint32_t NOPEN = dup16(-p.open);
@@ -170,7 +170,11 @@ __device__ __forceinline__ void wave_rows(const WaveParams &p, const unsigned ch
           if (row + 256 < lenB) asm volatile("prefetch.global.L1 [%0];" ::"l"(pb + row + 256));
         }
       }
-      const uint32_t cA = wA & 0xffu, cB = wB & 0xffu;
+      uint32_t cA = wA & 0xffu, cB = wB & 0xffu;
+      if (p.remap_off) {  // codes that score alike share a profile row
+        cA = prof[p.remap_off + cA];
+        cB = prof[p.remap_off + cB];
+      }
       wA >>= 8;
       wB >>= 8;
 
@@ -259,17 +263,27 @@ __device__ __forceinline__ void wave_rows(const WaveParams &p, const unsigned ch
           // keep this row (shared-memory stores only); the column of the
           // maximum is looked up once, at the record's last row
           const bool upA = lo16(cm) > lo16(best), upB = hi16(cm) > hi16(best);
-          uint32_t *dst = upA ? saveA : saveB;
+          // the improving lane's halves of the row: one PRMT per two columns
+#define ISH_H(j) ((j) < K ? H[(j) < K ? (j) : 0] : 0u)
+          if (upA) {
 #pragma unroll
-          for (int v = 0; v < KP4 / 4; ++v)
-            reinterpret_cast<uint4 *>(dst)[v] =
-                make_uint4(H[4 * v], 4 * v + 1 < K ? H[4 * v + 1] : 0u, 4 * v + 2 < K ? H[4 * v + 2] : 0u,
-                           4 * v + 3 < K ? H[4 * v + 3] : 0u);
-          if (upA && upB) {
-#pragma unroll
-            for (int v = 0; v < KP4 / 4; ++v)
-              reinterpret_cast<uint4 *>(saveB)[v] = reinterpret_cast<const uint4 *>(saveA)[v];
+            for (int v = 0; v < KP8 / 8; ++v)
+              reinterpret_cast<uint4 *>(saveA)[v] =
+                  make_uint4(__byte_perm(ISH_H(8 * v), ISH_H(8 * v + 1), 0x5410),
+                             __byte_perm(ISH_H(8 * v + 2), ISH_H(8 * v + 3), 0x5410),
+                             __byte_perm(ISH_H(8 * v + 4), ISH_H(8 * v + 5), 0x5410),
+                             __byte_perm(ISH_H(8 * v + 6), ISH_H(8 * v + 7), 0x5410));
           }
+          if (upB) {
+#pragma unroll
+            for (int v = 0; v < KP8 / 8; ++v)
+              reinterpret_cast<uint4 *>(saveB)[v] =
+                  make_uint4(__byte_perm(ISH_H(8 * v), ISH_H(8 * v + 1), 0x7632),
+                             __byte_perm(ISH_H(8 * v + 2), ISH_H(8 * v + 3), 0x7632),
+                             __byte_perm(ISH_H(8 * v + 4), ISH_H(8 * v + 5), 0x7632),
+                             __byte_perm(ISH_H(8 * v + 6), ISH_H(8 * v + 7), 0x7632));
+          }
+#undef ISH_H
           if (upA) rowA = row;
           if (upB) rowB = row;
           best = nb;
@@ -366,8 +380,8 @@ __device__ __forceinline__ void wave_rows(const WaveParams &p, const unsigned ch
           // smallest column of this thread's maximum in its first row
 #pragma unroll 1
           for (int j = K - 1; j >= 0; --j) {
-            if (bA > 0 && lo16(saveA[j]) == bA) qA = col0 + j;
-            if (bB > 0 && hi16(saveB[j]) == bB) qB = col0 + j;
+            if (bA > 0 && (int)(int16_t)saveA[j] == bA) qA = col0 + j;
+            if (bB > 0 && (int)(int16_t)saveB[j] == bB) qB = col0 + j;
           }
           if (t > 0) {
             const int ia = lo16(iR0), ib = hi16(iR0), ira = (int)iR2, irb = (int)iR3;
@@ -425,9 +439,9 @@ __device__ __forceinline__ void wave_rows(const WaveParams &p, const unsigned ch
 }
 
 // Shared memory of a block: the profile, then 32 slot words per group, then
-// (local alignment) 2 * KP4 save words per thread.
+// (local alignment) wave_save_words(K) save words per thread.
 template <int K, int MODE, int LAYOUT>
-__global__ void __launch_bounds__(wave_block_threads(K), wave_blocks_per_sm(K))
+__global__ void __launch_bounds__(wave_block_threads(K, MODE), wave_blocks_per_sm(K, MODE))
     wave_kernel(const __grid_constant__ WaveParams p) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   {
@@ -451,7 +465,7 @@ __global__ void __launch_bounds__(wave_block_threads(K), wave_blocks_per_sm(K))
 // a profile reload happen only at a query switch, where the pairs left are the
 // shortest of the set.  Queries whose counter is already exhausted are skipped.
 template <int K, int MODE, int LAYOUT>
-__global__ void __launch_bounds__(wave_block_threads(K), wave_blocks_per_sm(K))
+__global__ void __launch_bounds__(wave_block_threads(K, MODE), wave_blocks_per_sm(K, MODE))
     batch_kernel(const __grid_constant__ BatchParams b) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   __shared__ WaveParams sp;

@@ -27,7 +27,7 @@ EXPORTS = (
     "ish_gpu_records_info", "ish_gpu_score_set", "ish_gpu_last_kernel_ms", "ish_gpu_calibrate",
     "ish_gpu_score_noalloc", "ish_gpu_score_multi", "ish_gpu_autotune", "ish_gpu_serve_start", "ish_gpu_submit",
     "ish_gpu_poll", "ish_gpu_serve_stop", "ish_gpu_serve_stats", "ish_gpu_match_starts",
-    "ish_gpu_launch_count",
+    "ish_gpu_launch_count", "ish_gpu_records_load_raw", "ish_gpu_records_load_lines",
 )
 
 
@@ -89,6 +89,8 @@ def load(build_if_missing: bool = False):
     L.ish_gpu_score_multi.argtypes = [vp, i32p, C.c_uint32, C.c_int32, i32p, i32p, i32p, u8p, u32p, C.c_uint64, u64p]
     L.ish_gpu_autotune.argtypes = [vp, C.c_int32, i32p, C.c_uint32, i32p, i32p]
     L.ish_gpu_launch_count.argtypes = [vp, u64p]
+    L.ish_gpu_records_load_raw.argtypes = [vp, u8p, u64p, C.c_uint32, C.c_int, i32p]
+    L.ish_gpu_records_load_lines.argtypes = [vp, u8p, C.c_uint64, C.c_int, i32p, u32p]
     L.ish_gpu_match_starts.argtypes = [vp, C.c_int32, C.c_int32, u32p, i32p, C.c_uint32, C.POINTER(C.c_int64)]
     L.ish_gpu_serve_start.argtypes = [vp, C.c_int32, C.c_uint32, C.c_uint64, C.c_uint32]
     L.ish_gpu_submit.argtypes = [vp, C.c_int32, u64p]
@@ -208,6 +210,26 @@ class Context:
         self._check(self._L.ish_gpu_records_load(self._h, _p(records, C.c_uint8), _p(offsets, C.c_uint64),
                                                  len(offsets) - 1, C.byref(sid)))
         return sid.value
+
+    def records_load_raw(self, raw: np.ndarray, offsets: np.ndarray, matrix_kind: int) -> int:
+        """Resident set from raw bytes, encoded on the device for `matrix_kind`."""
+        raw = np.ascontiguousarray(raw, np.uint8)
+        offsets = np.ascontiguousarray(offsets, np.uint64)
+        sid = C.c_int32()
+        self._check(self._L.ish_gpu_records_load_raw(self._h, _p(raw, C.c_uint8), _p(offsets, C.c_uint64),
+                                                     len(offsets) - 1, matrix_kind, C.byref(sid)))
+        return sid.value
+
+    def records_load_lines(self, text, matrix_kind: int):
+        """Resident set of the lines of `text` (split and encoded on the device);
+        returns (set id, number of lines)."""
+        buf = np.frombuffer(bytes(text), np.uint8) if not isinstance(text, np.ndarray) else \
+            np.ascontiguousarray(text, np.uint8)
+        sid = C.c_int32()
+        n = C.c_uint32()
+        self._check(self._L.ish_gpu_records_load_lines(self._h, _p(buf, C.c_uint8) if len(buf) else None, len(buf),
+                                                       matrix_kind, C.byref(sid), C.byref(n)))
+        return sid.value, n.value
 
     def records_free(self, sid: int):
         self._check(self._L.ish_gpu_records_free(self._h, sid))

@@ -17,12 +17,24 @@ def cases():
     return json.load(open(os.path.join(HERE, "golden", "searcher_cases.json")))["cases"]
 
 
+def kseq_lines(data: bytes):
+    """Lines as ish's reader returns them (ishlib/vendor/kseq.mojo:270-330,
+    read_until with the newline delimiter): split at '\\n'; a trailing '\\r' is
+    dropped from a line longer than one byte; a last line without '\\n' is a
+    record; a final '\\n' does not start another one."""
+    out, pos, n = [], 0, len(data)
+    while pos < n:
+        r = data.find(b"\n", pos)
+        line = data[pos:] if r < 0 else data[pos:r]
+        pos = n if r < 0 else r + 1
+        if len(line) > 1 and line[-1] == 13:
+            line = line[:-1]
+        out.append(line)
+    return out
+
+
 def line_records(text: str):
-    data = text.encode()
-    parts = data.split(b"\n")
-    if parts and parts[-1] == b"":
-        parts = parts[:-1]
-    return [(None, p.rstrip(b"\r")) for p in parts]
+    return [(None, line) for line in kseq_lines(text.encode())]
 
 
 def fasta_records(text: str):

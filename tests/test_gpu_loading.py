@@ -1,0 +1,125 @@
+"""Records prepared on the device: raw bytes encoded while packing
+(ish_gpu_records_load_raw) and text split into line records
+(ish_gpu_records_load_lines).  Both must give exactly the set the host path
+gives -- records encoded and split as ish's runners do -- and therefore
+identical scores."""
+import numpy as np
+import pytest
+
+import oracle as O
+from ish_gb300 import native
+from ish_gb300.scoring import ScoringMatrix
+from searcher_fixtures import kseq_lines
+
+pytestmark = pytest.mark.gpu
+
+KINDS = [O.ASCII, O.ACTGN, O.ACTGN0, O.BLOSUM62]
+
+
+@pytest.fixture(scope="module")
+def ctx():
+    native.load(build_if_missing=True)
+    c = native.Context(0)
+    yield c
+    c.close()
+
+
+def query_for(ctx, kind, rng, qlen=30, algo=native.ALGO_SEMI_GLOBAL, ends=12):
+    m = ScoringMatrix(kind)
+    q = m.encode(rng.choice(np.frombuffer(b"ACGTNacgtnRDEQHKLMxyz*#", np.uint8), qlen).tobytes())
+    return ctx.set_query(q, kind, m.values, algo, 3, 1, ends, int(m.values[q, q].sum()), 0.3), m
+
+
+def same_results(ctx, qid, a, b):
+    ra, rb = ctx.score_set(qid, a), ctx.score_set(qid, b)
+    for k in ("score", "qend", "tend", "hit"):
+        assert np.array_equal(ra[k], rb[k]), k
+    assert np.array_equal(ra["hit_idx"], rb["hit_idx"])
+
+
+def random_text(rng, nlines):
+    parts = []
+    for i in range(nlines):
+        L = int(rng.integers(0, 90))
+        line = bytes(rng.choice(list(b"ACGTacgtNRDEQ \t*xyz"), L))
+        end = [b"\n", b"\r\n", b"\n", b"\r\r\n"][int(rng.integers(0, 4))]
+        if rng.random() < 0.05:
+            line = b"\r"  # a lone carriage return is kept
+        parts.append(line + end)
+    text = b"".join(parts)
+    if rng.random() < 0.5:
+        text += b"tail without newline\r"
+    return text
+
+
+@pytest.mark.parametrize("kind", KINDS)
+def test_lines_split_and_encoded_on_device(ctx, kind):
+    rng = np.random.default_rng(40 + kind)
+    for trial in range(4):
+        text = random_text(rng, int(rng.integers(1, 3000)))
+        lines = kseq_lines(text)
+        m = ScoringMatrix(kind)
+        enc = [m.encode(l) for l in lines]
+        buf, off = native.pack_records(enc)
+        sid_d, n = ctx.records_load_lines(text, kind)
+        sid_h = ctx.records_load(buf, off)
+        try:
+            assert n == len(lines)
+            assert ctx.records_info(sid_d) == (len(lines), int(off[-1]))
+            qid, _ = query_for(ctx, kind, rng)
+            same_results(ctx, qid, sid_d, sid_h)
+            ctx.free_query(qid)
+        finally:
+            ctx.records_free(sid_d)
+            ctx.records_free(sid_h)
+
+
+@pytest.mark.parametrize("kind", KINDS)
+def test_raw_bytes_encoded_on_device(ctx, kind):
+    rng = np.random.default_rng(60 + kind)
+    recs = [rng.integers(0, 256, int(rng.integers(0, 300)), dtype=np.uint8) for _ in range(2000)]
+    raw, off = native.pack_records(recs)
+    m = ScoringMatrix(kind)
+    enc = m.encode(raw)
+    sid_d = ctx.records_load_raw(raw, off, kind)
+    sid_h = ctx.records_load(enc, off)
+    try:
+        for algo, ends in ((native.ALGO_SEMI_GLOBAL, 12), (native.ALGO_LOCAL, 0)):
+            qid, _ = query_for(ctx, kind, rng, 40, algo, ends)
+            same_results(ctx, qid, sid_d, sid_h)
+            ctx.free_query(qid)
+    finally:
+        ctx.records_free(sid_d)
+        ctx.records_free(sid_h)
+
+
+def test_line_edge_cases(ctx):
+    for text in (b"", b"\n", b"\n\n", b"a", b"a\n", b"\r\n", b"\r", b"ab\r", b"x\r\r\n\ny"):
+        lines = kseq_lines(text)
+        sid, n = ctx.records_load_lines(text, O.ASCII)
+        try:
+            assert n == len(lines), text
+            assert ctx.records_info(sid) == (len(lines), sum(len(l) for l in lines)), text
+        finally:
+            ctx.records_free(sid)
+
+
+def test_lines_against_oracle(ctx):
+    # end to end: text in, hits out, compared with the oracle on host-split lines
+    rng = np.random.default_rng(77)
+    pat = b"GATTACAGATTACA"
+    lines = [bytes(rng.choice(list(b"ACGT"), int(rng.integers(5, 120)))) for _ in range(3000)]
+    lines = [l[:7] + pat + l[7:] if i % 9 == 0 else l for i, l in enumerate(lines)]
+    text = b"\r\n".join(lines) + b"\n"
+    om = O.Matcher.from_ascii(O.SEMI_GLOBAL, O.ACTGN, pat, 0.8, ends=O.TS | O.TE)
+    m = ScoringMatrix(O.ACTGN)
+    q, mx = m.encode_and_score(pat)
+    qid = ctx.set_query(q, O.ACTGN, m.values, native.ALGO_SEMI_GLOBAL, 3, 1, 12, mx, 0.8)
+    sid, n = ctx.records_load_lines(text, O.ACTGN)
+    try:
+        r = ctx.score_set(qid, sid)
+        want = [i for i, l in enumerate(kseq_lines(text)) if om.first_match(m.encode(l)) is not None]
+        assert list(r["hit_idx"]) == want and len(want) >= 300
+    finally:
+        ctx.records_free(sid)
+        ctx.free_query(qid)

@@ -235,3 +235,20 @@ def test_every_profile_layout(ctx, layout, kind):
                 assert_same(g, o, f"layout={layout} kind={kind} Q={qlen} algo={algo} ends={ends}")
         finally:
             ctx.set_option(native.OPT_PROFILE_LAYOUT, native.PROF_AUTO)
+
+
+@pytest.mark.parametrize("qlen", [120, 300, 1000])
+def test_ascii_long_queries(ctx, qlen):
+    # 256-code ascii profiles: codes absent from the query share one profile
+    # row, which keeps long ascii queries within shared memory
+    rng = np.random.default_rng(4000 + qlen)
+    printable = np.arange(0x20, 0x7F, dtype=np.uint8)
+    q = rng.choice(printable, qlen)
+    recs = [rng.choice(printable, int(rng.integers(0, 2 * qlen))) for _ in range(120)]
+    for r in recs[::5]:
+        if len(r) >= qlen:
+            pos = int(rng.integers(0, len(r) - qlen + 1))
+            r[pos:pos + qlen] = q
+    for algo, ends in ((native.ALGO_SEMI_GLOBAL, 12), (native.ALGO_SEMI_GLOBAL, 3), (native.ALGO_LOCAL, 0)):
+        g, o = run_both(ctx, algo, O.ASCII, q, recs, 3, 1, ends, thr=0.6)
+        assert_same(g, o, f"ascii Q={qlen} algo={algo} ends={ends}")
