@@ -75,6 +75,7 @@ __device__ __forceinline__ void wave_rows(const WaveParams &p, const unsigned ch
     E[j] = 0;
   }
   uint32_t prevH = 0, outH = 0, outF = 0, outC = CTL_IDLE;
+  uint32_t outBest = 0;  // local alignment: best cell so far in this thread's and all earlier columns
   int row = 0, lenA = 0, lenB = 0, lastA_row = -1, lastB_row = -1;
   uint32_t pr = 0;
   // this thread's record streams: 4 codes per 32-bit word, one word ahead
@@ -96,6 +97,7 @@ __device__ __forceinline__ void wave_rows(const WaveParams &p, const unsigned ch
     const uint32_t msgH = __shfl_up_sync(FULL, outH, 1, G);
     const uint32_t msgF = __shfl_up_sync(FULL, outF, 1, G);
     uint32_t msgC = __shfl_up_sync(FULL, outC, 1, G);
+    const uint32_t msgBest = (MODE == SW) ? __shfl_up_sync(FULL, outBest, 1, G) : 0u;
 
     if (t == 0) {
       if (!f_active && !f_done) {
@@ -258,11 +260,20 @@ __device__ __forceinline__ void wave_rows(const WaveParams &p, const unsigned ch
 #pragma unroll
         for (int j = 1; j + 1 < K; j += 2) cm = __vimax3_s16x2(cm, H[j], H[j + 1]);
         if ((K & 1) == 0 && K > 1) cm = __viaddmax_s16x2(cm, 0u, H[K - 1]);
-        const uint32_t nb = __viaddmax_s16x2(best, 0u, cm);
-        if (nb != best) {
+        // Only a row maximum above every cell so far in this thread AND in
+        // all columns to its left (`left`, the running best passed along the
+        // pipeline for this row) can be the first row of the record's
+        // maximum at its smallest column; anything else is dominated
+        // (smaller, or equal in an earlier row or a smaller column), so only
+        // those improvements are recorded.
+        const uint32_t left = (t == 0) ? 0u : msgBest;
+        const uint32_t thr = __viaddmax_s16x2(best, 0u, left);
+        const uint32_t nb = __viaddmax_s16x2(thr, 0u, cm);
+        outBest = nb;
+        if (nb != thr) {
           // keep this row (shared-memory stores only); the column of the
           // maximum is looked up once, at the record's last row
-          const bool upA = lo16(cm) > lo16(best), upB = hi16(cm) > hi16(best);
+          const bool upA = lo16(cm) > lo16(thr), upB = hi16(cm) > hi16(thr);
           // the improving lane's halves of the row: one PRMT per two columns
 #define ISH_H(j) ((j) < K ? H[(j) < K ? (j) : 0] : 0u)
           if (upA) {
@@ -286,7 +297,7 @@ __device__ __forceinline__ void wave_rows(const WaveParams &p, const unsigned ch
 #undef ISH_H
           if (upA) rowA = row;
           if (upB) rowB = row;
-          best = nb;
+          best = ((upA ? cm : best) & 0xffffu) | ((upB ? cm : best) & 0xffff0000u);
         }
       }
     } else {
