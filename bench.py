@@ -602,7 +602,9 @@ def run_serving(args, rank, world, local, dist):
     residues = int(wl.offsets[-1])
     m = ScoringMatrix(wl.kind)
     count = max(args.steps, 4)
-    rates = (10.0, 100.0, 2000.0)
+    # 0.5/s is below the set's capacity (~0.85 queries/s at 4 GB), the
+    # configuration's own rates (10-2000/s) are far above it
+    rates = (0.5, 10.0, 100.0, 2000.0)
     config = {"workload": f"serving: {gb:g} GB resident blosum62 protein set ({wl.n} records, lognormal median "
                           f"350), Poisson arrivals at {', '.join(f'{r:g}' for r in rates)} queries/s, {count} "
                           "queries per rate, Q ~ U[20,2000], striped-local / semi-global FFTT mix, gap 10/1, "
