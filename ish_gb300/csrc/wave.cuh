@@ -86,11 +86,17 @@ __device__ __forceinline__ void wave_rows(const WaveParams &p, const unsigned ch
   int rowA = -1, rowB = -1;  // first row of the lane's maximum
   uint32_t oR0 = 0, oR1 = 0, oR2 = 0, oR3 = 0;  // last-row partials for thread t+1
   bool has_out = false;
-  // thread 0 of the group grabs record pairs
-  bool f_active = false, f_done = false;
-  int f_row = 0, f_rows = 0;
+  // thread 0 of the group grabs record pairs: f_left rows of the current pair
+  // are still to start, f_ctl is the control word of the next row
+  bool f_done = false;
+  int f_left = 0;
+  uint32_t f_ctl = CTL_IDLE;
   uint32_t f_seq = 31;
+  // the next row at which one of this thread's records ends (-3: none)
+  int ev_row = -3;
+  const bool remap = p.remap_off != 0;
   uint64_t steps = 0;
+  int chk = 8;
 
   while (true) {
     __syncwarp();
@@ -100,27 +106,23 @@ __device__ __forceinline__ void wave_rows(const WaveParams &p, const unsigned ch
     const uint32_t msgBest = (MODE == SW) ? __shfl_up_sync(FULL, outBest, 1, G) : 0u;
 
     if (t == 0) {
-      if (!f_active && !f_done) {
+      if (f_left <= 0 && !f_done) {
         const uint32_t np = atomicAdd(counter, 1u);
         if (np < npairs) {
-          f_active = true;
           f_seq = (f_seq + 1) & 31;
           slots[f_seq] = np;
           const uint32_t sA = p.first + 2 * np;
           const int la = (int)p.rec.len[sA];
           const int lb = (2 * np + 1 < p.count) ? (int)p.rec.len[sA + 1] : 0;
-          f_rows = max(max(la, lb), 1);
-          f_row = 0;
+          f_left = max(max(la, lb), 1);
+          f_ctl = CTL_NEW | (f_seq << CTL_SEQ_SHIFT);
         } else {
           f_done = true;
         }
       }
-      if (f_active) {
-        msgC = (f_row == 0 ? CTL_NEW : 0u) | (f_seq << CTL_SEQ_SHIFT);
-        if (++f_row >= f_rows) f_active = false;
-      } else {
-        msgC = CTL_IDLE;
-      }
+      msgC = f_ctl;
+      f_ctl &= ~CTL_NEW;
+      if (--f_left <= 0) f_ctl = CTL_IDLE;
     }
 
     const bool busy = !(msgC & CTL_IDLE);
@@ -139,6 +141,9 @@ __device__ __forceinline__ void wave_rows(const WaveParams &p, const unsigned ch
         }
         lastA_row = lenA - 1;
         lastB_row = lenB > 0 ? lenB - 1 : -2;
+        // the earlier of the two records' last rows (either may be empty)
+        ev_row = lastA_row >= 0 ? lastA_row : -3;
+        if (lastB_row >= 0 && (ev_row < 0 || lastB_row < ev_row)) ev_row = lastB_row;
         nA = __ldg(reinterpret_cast<const uint32_t *>(pa));
         nB = lenB ? __ldg(reinterpret_cast<const uint32_t *>(pb)) : 0u;
         const int16_t *hi = p.hinit + t * K;
@@ -173,7 +178,7 @@ __device__ __forceinline__ void wave_rows(const WaveParams &p, const unsigned ch
         }
       }
       uint32_t cA = wA & 0xffu, cB = wB & 0xffu;
-      if (p.remap_off) {  // codes that score alike share a profile row
+      if (remap) {  // codes that score alike share a profile row
         cA = prof[p.remap_off + cA];
         cB = prof[p.remap_off + cB];
       }
@@ -305,8 +310,15 @@ __device__ __forceinline__ void wave_rows(const WaveParams &p, const unsigned ch
     }
 
     // ---- last row of a record: fold partial results left to right ----
-    const bool lastA = busy && row == lastA_row, lastB = busy && row == lastB_row;
-    if (__any_sync(FULL, lastA || lastB || has_out)) {
+    // (a handled end moves ev_row on, so an idle thread never sees it again)
+    const bool ev = row == ev_row;
+    if (__any_sync(FULL, ev || has_out)) {
+      const bool lastA = ev && row == lastA_row, lastB = ev && row == lastB_row;
+      if (ev) {  // the other record's end, if it is still ahead
+        int nxt = lastA_row > row ? lastA_row : -3;
+        if (lastB_row > row && (nxt < 0 || lastB_row < nxt)) nxt = lastB_row;
+        ev_row = nxt;
+      }
       const uint32_t iR0 = __shfl_up_sync(FULL, oR0, 1, G);
       const uint32_t iR1 = __shfl_up_sync(FULL, oR1, 1, G);
       uint32_t iR2 = 0, iR3 = 0;
@@ -438,7 +450,9 @@ __device__ __forceinline__ void wave_rows(const WaveParams &p, const unsigned ch
     // group is done once thread 0 is and no row is in flight.  The step budget
     // (all rows of the range plus the pipeline depth) is a hard stop.
     // (checked every 8 steps; idle extra steps do nothing)
-    if ((++steps & 7) == 0) {
+    if (--chk == 0) {
+      chk = 8;
+      steps += 8;
       const bool more = busy || (t == 0 && !f_done);
       if (!__any_sync(FULL, more)) break;
       if (steps > p.max_steps) {
