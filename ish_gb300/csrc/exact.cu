@@ -339,80 +339,121 @@ std::vector<TY> striped_profile(const Query &q, int W, bool local, int bias) {
   return out;
 }
 
-int exact_pass(ish_ctx *ctx, Query &q, RecordSet &rs, uint32_t first, uint32_t count, OutDev out, cudaStream_t s,
-               int mode, int W, int word, const uint8_t *redo, uint8_t *redo_out) {
-  ExactFn fn = exact_fn(mode, W, word);
-  if (!fn) return fail(ctx, ISH_EINVAL, "exact kernel: %d lanes are not supported (8, 16 or 32)", W);
-  const int seg = std::max(1, (q.Q + W - 1) / W);
-  const int bias = mode == SW ? -std::min(0, q.mmin) : 0;
-  // profile (cached per query, lane count and lane type)
-  const long key = ((long)mode << 16) | ((long)word << 8) | W;
-  DevBuf &prof = q.exact_prof[key];
-  if (!prof.p) {
-    if (mode == SG) {
-      auto v = striped_profile<int16_t>(q, W, false, 0);
-      CU(prof.ensure(v.size() * 2));
-      CU(cudaMemcpy(prof.p, v.data(), v.size() * 2, cudaMemcpyHostToDevice));
-    } else if (!word) {
-      auto v = striped_profile<uint8_t>(q, W, true, bias);
-      CU(prof.ensure(v.size()));
-      CU(cudaMemcpy(prof.p, v.data(), v.size(), cudaMemcpyHostToDevice));
-    } else {
-      auto v = striped_profile<uint16_t>(q, W, true, bias);
-      CU(prof.ensure(v.size() * 2));
-      CU(cudaMemcpy(prof.p, v.data(), v.size() * 2, cudaMemcpyHostToDevice));
-    }
-  }
-  // one tile per record in flight; scratch of 4 * seg * W lane values each,
-  // at most ~1 GB in all
+// Lanes, lane type and grid of one pass: one tile per record in flight, each
+// with a scratch slice of 4 * seg * W lane values; at most ~1 GB in all.
+struct PassShape {
+  int mode, W, word, seg;
+  size_t tile_stride, tile_bytes;
+  uint64_t blocks;
+};
+
+PassShape pass_shape(const ish_ctx *ctx, const Query &q, int mode, int W, int word, uint32_t count) {
+  PassShape ps;
+  ps.mode = mode;
+  ps.W = W;
+  ps.word = word;
+  ps.seg = std::max(1, (q.Q + W - 1) / W);
   const size_t lane_bytes = (mode == SW && !word) ? 1 : 2;
-  const size_t tile_stride = (size_t)4 * seg * W;
-  const size_t tile_bytes = tile_stride * lane_bytes;
+  ps.tile_stride = (size_t)4 * ps.seg * W;
+  ps.tile_bytes = ps.tile_stride * lane_bytes;
   const uint32_t tiles_per_block = 256 / W;
   uint64_t blocks = std::min<uint64_t>((uint64_t)ctx->num_sms * 8, ((uint64_t)count + tiles_per_block - 1) / tiles_per_block);
-  blocks = std::min<uint64_t>(blocks, std::max<uint64_t>(1, (1ull << 30) / (tile_bytes * tiles_per_block)));
-  blocks = std::max<uint64_t>(blocks, 1);
-  CU(ctx->exact_scratch.ensure(blocks * tiles_per_block * tile_bytes + 16));
+  blocks = std::min<uint64_t>(blocks, std::max<uint64_t>(1, (1ull << 30) / (ps.tile_bytes * tiles_per_block)));
+  ps.blocks = std::max<uint64_t>(blocks, 1);
+  return ps;
+}
+
+std::vector<PassShape> passes_of(const ish_ctx *ctx, const Query &q, uint32_t count) {
+  if (q.algo == ISH_ALGO_SEMI_GLOBAL) return {pass_shape(ctx, q, SG, ctx->sg_lanes, 0, count)};
+  return {pass_shape(ctx, q, SW, ctx->sw_u8_lanes, 0, count), pass_shape(ctx, q, SW, ctx->sw_u16_lanes, 1, count)};
+}
+
+long prof_key(const PassShape &ps) { return ((long)ps.mode << 16) | ((long)ps.word << 8) | ps.W; }
+
+int enqueue_pass(ish_ctx *ctx, Query &q, RecordSet &rs, uint32_t first, uint32_t count, OutDev out, cudaStream_t s,
+                 const PassShape &ps, ExactRes &res, const uint8_t *redo, uint8_t *redo_out, uint32_t *launches) {
+  ExactFn fn = exact_fn(ps.mode, ps.W, ps.word);
   ExactParams p{};
-  p.prof = prof.p;
+  p.prof = q.exact_prof.at(prof_key(ps)).p;
   p.Q = q.Q;
-  p.seg = seg;
-  p.open = mode == SG ? q.open : (uint8_t)q.open;
-  p.ext = mode == SG ? q.ext : (uint8_t)q.ext;
+  p.seg = ps.seg;
+  p.open = ps.mode == SG ? q.open : (uint8_t)q.open;
+  p.ext = ps.mode == SG ? q.ext : (uint8_t)q.ext;
   p.ends = q.ends;
   p.min_s = q.mmin;
-  p.bias = bias;
+  p.bias = ps.mode == SW ? -std::min(0, q.mmin) : 0;
   p.rec = RecordsDev{rs.codes.as<const uint8_t>(), rs.off_s.as<const uint64_t>(), rs.len_s.as<const uint32_t>(),
                      rs.orig_s.as<const uint32_t>(), rs.n};
   p.first = first;
   p.count = count;
-  p.counter = ctx->counter.as<uint32_t>();
-  p.scratch = ctx->exact_scratch.p;
-  p.tile_stride = tile_stride;
+  p.counter = res.counter.as<uint32_t>();
+  p.scratch = res.scratch.p;
+  p.tile_stride = ps.tile_stride;
   p.redo = redo;
   p.redo_out = redo_out;
   p.out = out;
   p.dec = Decision{q.max_score, q.thr};
-  CU(cudaMemsetAsync(ctx->counter.p, 0, 4, s));
-  fn<<<(uint32_t)blocks, 256, 0, s>>>(p);
-  ++ctx->launches;
+  CU(cudaMemsetAsync(res.counter.p, 0, 4, s));
+  fn<<<(uint32_t)ps.blocks, 256, 0, s>>>(p);
+  ++*launches;
   CU(cudaGetLastError());
   return ISH_OK;
 }
 
 }  // namespace
 
+// Uploads the striped profiles q needs and sizes res for passes over up to
+// `count` records (no launch; call before a CUDA graph capture).
+int exact_prepare(ish_ctx *ctx, Query &q, uint32_t count, ExactRes &res) {
+  for (const PassShape &ps : passes_of(ctx, q, count)) {
+    if (!exact_fn(ps.mode, ps.W, ps.word))
+      return fail(ctx, ISH_EINVAL, "exact kernel: %d lanes are not supported (8, 16 or 32)", ps.W);
+    DevBuf &prof = q.exact_prof[prof_key(ps)];
+    if (!prof.p) {
+      const int bias = ps.mode == SW ? -std::min(0, q.mmin) : 0;
+      if (ps.mode == SG) {
+        auto v = striped_profile<int16_t>(q, ps.W, false, 0);
+        CU(prof.ensure(v.size() * 2));
+        CU(cudaMemcpy(prof.p, v.data(), v.size() * 2, cudaMemcpyHostToDevice));
+      } else if (!ps.word) {
+        auto v = striped_profile<uint8_t>(q, ps.W, true, bias);
+        CU(prof.ensure(v.size()));
+        CU(cudaMemcpy(prof.p, v.data(), v.size(), cudaMemcpyHostToDevice));
+      } else {
+        auto v = striped_profile<uint16_t>(q, ps.W, true, bias);
+        CU(prof.ensure(v.size() * 2));
+        CU(cudaMemcpy(prof.p, v.data(), v.size() * 2, cudaMemcpyHostToDevice));
+      }
+    }
+    CU(res.scratch.ensure(ps.blocks * (256 / ps.W) * ps.tile_bytes + 16));
+  }
+  CU(res.counter.ensure(64));
+  CU(res.redo.ensure((size_t)count + 16));
+  return ISH_OK;
+}
+
 // The reference's striped passes emulated lane by lane, for sorted entries
-// [first, first + count) of rs.  Local alignment runs the uint8 pass and
+// [first, first + count) of rs, with resources from exact_prepare (no
+// allocation, graph-capturable).  Local alignment runs the uint8 pass and
 // reruns the entries that saturated it with uint16 lanes, as ssw_align does.
+int exact_enqueue(ish_ctx *ctx, Query &q, RecordSet &rs, uint32_t first, uint32_t count, OutDev out, cudaStream_t s,
+                  ExactRes &res, uint32_t *launches) {
+  if (count == 0) return ISH_OK;
+  const std::vector<PassShape> ps = passes_of(ctx, q, count);
+  if (ps.size() == 1) return enqueue_pass(ctx, q, rs, first, count, out, s, ps[0], res, nullptr, nullptr, launches);
+  int rc = enqueue_pass(ctx, q, rs, first, count, out, s, ps[0], res, nullptr, res.redo.as<uint8_t>(), launches);
+  if (rc) return rc;
+  return enqueue_pass(ctx, q, rs, first, count, out, s, ps[1], res, res.redo.as<uint8_t>(), nullptr, launches);
+}
+
 int launch_exact(ish_ctx *ctx, Query &q, RecordSet &rs, uint32_t first, uint32_t count, OutDev out, cudaStream_t s) {
   if (count == 0) return ISH_OK;
-  CU(ctx->counter.ensure(64));
-  if (q.algo == ISH_ALGO_SEMI_GLOBAL) return exact_pass(ctx, q, rs, first, count, out, s, SG, ctx->sg_lanes, 0, nullptr, nullptr);
-  CU(ctx->exact_redo.ensure((size_t)count + 16));
-  int rc = exact_pass(ctx, q, rs, first, count, out, s, SW, ctx->sw_u8_lanes, 0, nullptr, ctx->exact_redo.as<uint8_t>());
+  int rc = exact_prepare(ctx, q, count, ctx->exact);
   if (rc) return rc;
-  return exact_pass(ctx, q, rs, first, count, out, s, SW, ctx->sw_u16_lanes, 1, ctx->exact_redo.as<uint8_t>(), nullptr);
+  uint32_t n = 0;
+  rc = exact_enqueue(ctx, q, rs, first, count, out, s, ctx->exact, &n);
+  ctx->launches += n;
+  return rc;
 }
 
 }  // namespace host

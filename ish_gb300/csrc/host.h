@@ -105,6 +105,18 @@ struct Regime {
   uint64_t max_safe_len = 0;  // records longer than this need the exact path
 };
 
+// Scratch, rerun flags and work counter of the exact kernels (exact.cu); a
+// batched plan and the serving loop own theirs, so captured graphs and
+// concurrent steps never share them.
+struct ExactRes {
+  DevBuf scratch, redo, counter;
+  void release() {
+    scratch.release();
+    redo.release();
+    counter.release();
+  }
+};
+
 struct MultiPlan;  // multi.cu
 struct Server;     // serve.cu
 struct Tuned {
@@ -132,7 +144,7 @@ struct ish_ctx {
   ish::host::DevBuf counter, error, out_score, out_qend, out_tend, out_hit, hit_idx, block_counts, nhits;
   ish::host::DevBuf plain_scratch;
   ish::host::DevBuf enc_tables, nl_pos, line_end;  // encoding tables; line splitting scratch
-  ish::host::DevBuf exact_scratch, exact_redo;      // exact kernels (exact.cu)
+  ish::host::ExactRes exact;                        // exact kernels (exact.cu)
   float last_ms = 0.f;
   // batched launches (multi.cu): plans cached per (queries, set, outputs)
   std::map<std::string, ish::host::MultiPlan *> plans;
@@ -199,6 +211,9 @@ bool wave_fits(const Query &q, int G, int K, int layout);
 // rs (the safe regime); the exact kernels (exact.cu) take the rest.
 bool fast_regime(ish_ctx *ctx, const Query &q, const RecordSet &rs);
 int launch_exact(ish_ctx *ctx, Query &q, RecordSet &rs, uint32_t first, uint32_t count, OutDev out, cudaStream_t s);
+int exact_prepare(ish_ctx *ctx, Query &q, uint32_t count, ExactRes &res);
+int exact_enqueue(ish_ctx *ctx, Query &q, RecordSet &rs, uint32_t first, uint32_t count, OutDev out, cudaStream_t s,
+                  ExactRes &res, uint32_t *launches);
 int launch_range(ish_ctx *ctx, Query &q, RecordSet &rs, uint32_t first, uint32_t count, OutDev out, cudaStream_t s);
 void drop_plans(ish_ctx *ctx, int32_t query_id, int32_t set_id);  // multi.cu
 void free_plans(ish_ctx *ctx);                                   // multi.cu

@@ -781,8 +781,9 @@ void ish_gpu_close(ish_ctx *ctx) {
   DevBuf *bufs[] = {&ctx->raw, &ctx->off_in, &ctx->len_tmp, &ctx->slot_tmp, &ctx->poff_tmp, &ctx->hist, &ctx->max_code,
                     &ctx->scan_tmp, &ctx->counter, &ctx->error, &ctx->out_score, &ctx->out_qend, &ctx->out_tend,
                     &ctx->out_hit, &ctx->hit_idx, &ctx->block_counts, &ctx->nhits, &ctx->plain_scratch,
-                    &ctx->enc_tables, &ctx->nl_pos, &ctx->line_end, &ctx->exact_scratch, &ctx->exact_redo};
+                    &ctx->enc_tables, &ctx->nl_pos, &ctx->line_end};
   for (DevBuf *b : bufs) b->release();
+  ctx->exact.release();
   cudaEventDestroy(ctx->ev0);
   cudaEventDestroy(ctx->ev1);
   cudaStreamDestroy(ctx->stream);

@@ -36,6 +36,8 @@ struct MultiPlan {
   uint32_t kernels = 0;  // kernel nodes of the graph
   std::vector<MultiClass> classes;
   DevBuf counters, score, qend, tend, hit, block_counts, hit_idx, nhits;
+  std::vector<uint32_t> exact_q;  // positions of the queries the exact kernels score
+  ExactRes exact;
   std::vector<cudaStream_t> side;
   std::vector<cudaEvent_t> events;
   cudaGraph_t graph = nullptr;
@@ -57,6 +59,7 @@ struct MultiPlan {
     }
     DevBuf *bufs[] = {&counters, &score, &qend, &tend, &hit, &block_counts, &hit_idx, &nhits};
     for (DevBuf *b : bufs) b->release();
+    exact.release();
   }
 };
 
@@ -117,19 +120,22 @@ int build_plan(ish_ctx *ctx, const int32_t *qids, uint32_t nq, int32_t set_id, R
   for (uint32_t i = 0; i < nq; ++i) {
     Query &q = ctx->queries.at(qids[i]);
     if (q.Q == 0 || nonempty == 0) continue;
-    int rc = check_fast(ctx, q, rs);
-    if (rc) return rc;
+    if (rs.max_code >= (uint32_t)q.alphabet)
+      return fail(ctx, ISH_EINVAL, "a record contains code %u >= the alphabet size %d of query %d", rs.max_code,
+                  q.alphabet, qids[i]);
     Member m;
     m.pos = i;
     pick_shape(ctx, q, &m.G, &m.K, &m.layout);
-    if (!m.G || m.G * m.K < q.Q + 1)
-      return fail(ctx, ISH_EOVERFLOW, "no wavefront shape for a query of %d residues", q.Q);
     m.mode = q.algo == ISH_ALGO_LOCAL ? SW : SG;
-    if (!wave_fits(q, m.G, m.K, m.layout))
-      return fail(ctx, ISH_EOVERFLOW,
-                  "query %d (%d residues, %d profile rows) does not fit a batched launch; score it with "
-                  "ish_gpu_score_set", qids[i], q.Q, q.rows);
-    rc = build_wave_layout(ctx, q, m.G, m.K, m.layout, &m.L);
+    if (!fast_regime(ctx, q, rs) || !wave_fits(q, m.G, m.K, m.layout)) {
+      // outside the wavefront kernels' exact regime, or a profile that fits
+      // no layout: the lane-exact kernels score this query in the same graph
+      int rc = exact_prepare(ctx, q, nonempty, P.exact);
+      if (rc) return rc;
+      P.exact_q.push_back(i);
+      continue;
+    }
+    int rc = build_wave_layout(ctx, q, m.G, m.K, m.layout, &m.L);
     if (rc) return rc;
     m.layout = m.L->layout;
     members.push_back(m);
@@ -235,6 +241,16 @@ int enqueue_plan(ish_ctx *ctx, MultiPlan &P, RecordSet &rs, cudaStream_t s) {
       CU(cudaEventRecord(P.events[i], cs));
       CU(cudaStreamWaitEvent(s, P.events[i], 0));
     }
+  }
+  // queries the lane-exact kernels score
+  for (uint32_t i : P.exact_q) {
+    Query &q = ctx->queries.at(P.qids[i]);
+    OutDev out{(P.want & W_SCORE) ? P.score.as<int32_t>() + (size_t)i * n : nullptr,
+               (P.want & W_QEND) ? P.qend.as<int32_t>() + (size_t)i * n : nullptr,
+               (P.want & W_TEND) ? P.tend.as<int32_t>() + (size_t)i * n : nullptr,
+               (P.want & (W_HIT | W_COMPACT)) ? P.hit.as<uint8_t>() + (size_t)i * n : nullptr};
+    int rc = exact_enqueue(ctx, q, rs, 0, n - rs.n_empty, out, s, P.exact, &P.kernels);
+    if (rc) return rc;
   }
   // empty records and empty queries
   const RecordsDev rec{rs.codes.as<const uint8_t>(), rs.off_s.as<const uint64_t>(), rs.len_s.as<const uint32_t>(),
@@ -422,8 +438,9 @@ int ish_gpu_autotune(ish_ctx *ctx, int32_t set_id, const int32_t *query_ids, uin
     Query &q = qi->second;
     const int mode = q.algo == ISH_ALGO_LOCAL ? SW : SG;
     const uint64_t key = tune_key(mode, q.rows, q.Q);
-    if (q.Q > 0 && nonempty > 0 && !ctx->tuned.count(key)) {
-      if ((rc = check_fast(ctx, q, rs))) break;
+    // (queries outside the wavefront kernels' exact regime run on the exact
+    // kernels, which have no shapes to tune)
+    if (q.Q > 0 && nonempty > 0 && !ctx->tuned.count(key) && fast_regime(ctx, q, rs)) {
       // candidates: every group size whose modelled cost is within 1.6x of
       // the best, each with its profile layout and the alternative one
       struct Cand {

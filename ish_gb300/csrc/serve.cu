@@ -47,6 +47,7 @@ struct Request {
   Query q;  // private copy: parameters and sequence (its layouts belong to the scheduler)
   int G = 0, K = 0, layout = 0, mode = 0;
   WaveLayout *L = nullptr;
+  bool exact = false;  // scored by the lane-exact kernels (outside the wavefront kernels' regime)
   Bundle *b = nullptr;
   WaveParams params{};
   uint32_t next_chunk = 0;
@@ -87,6 +88,8 @@ struct Server {
   uint32_t bundles = 0;
   size_t bundle_bytes = 0;
   DevBuf step_params, step_tiles, step_counters, error;
+  ExactRes exact;         // exact kernels' resources, shared by the exact requests (one stream)
+  uint32_t max_chunk = 0;  // records in the largest chunk
   WaveParams *h_params = nullptr;  // pinned staging
   BatchTile *h_tiles = nullptr;
   uint32_t *h_nhits = nullptr;
@@ -95,14 +98,6 @@ struct Server {
 namespace {
 
 inline uint64_t bucket_len(uint32_t b) { return b < 32768 ? b : 32768 + ((uint64_t)(b - 32768) << 5) + 31; }
-
-void free_layouts(Query &q) {
-  for (auto &l : q.layouts) {
-    l.second.prof.release();
-    l.second.hinit.release();
-  }
-  q.layouts.clear();
-}
 
 // Splits the set's non-empty sorted entries into `n` chunks of about equal
 // residue count.
@@ -154,7 +149,7 @@ void make_chunks(Server &S, uint32_t n) {
 
 void finish(Server &S, Request *r) {
   r->t_done = Clock::now();
-  if (r->L) free_layouts(r->q);
+  release_query(r->q);
   r->L = nullptr;
   if (r->b) {
     S.pool.push_back(r->b);
@@ -182,18 +177,28 @@ int admit(Server &S, Request *r, char *msg, size_t) {
   const RecordSet &rs = *S.rs;
   const uint32_t n = rs.n;
   if (r->q.Q > 0 && rs.n > rs.n_empty) {
-    int rc = fast_check(r->q, rs, r->G, r->K, msg, 256);
-    if (rc) return rc;
-    if (!wave_fits(r->q, r->G, r->K, r->layout)) {
-      snprintf(msg, 256, "query of %d residues (%d profile rows) does not fit the serving kernels", r->q.Q, r->q.rows);
-      return ISH_EOVERFLOW;
+    if (rs.max_code >= (uint32_t)r->q.alphabet) {
+      snprintf(msg, 256, "a record contains code %u >= the alphabet size %d of the query", rs.max_code, r->q.alphabet);
+      return ISH_EINVAL;
     }
-    rc = build_wave_layout(S.ctx, r->q, r->G, r->K, r->layout, &r->L);
-    if (rc) {
-      snprintf(msg, 256, "profile upload failed");
-      return rc;
+    char why[256];
+    if (fast_check(r->q, rs, r->G, r->K, why, sizeof why) == ISH_OK && wave_fits(r->q, r->G, r->K, r->layout)) {
+      int rc = build_wave_layout(S.ctx, r->q, r->G, r->K, r->layout, &r->L);
+      if (rc) {
+        snprintf(msg, 256, "profile upload failed");
+        return rc;
+      }
+      r->layout = r->L->layout;
+    } else {
+      // outside the wavefront kernels' exact regime, or a profile that fits
+      // no layout: the lane-exact kernels score its chunks
+      int rc = exact_prepare(S.ctx, r->q, S.max_chunk, S.exact);
+      if (rc) {
+        snprintf(msg, 256, "exact kernel resources: %s", ish_gpu_last_error(S.ctx));
+        return rc;
+      }
+      r->exact = true;
     }
-    r->layout = r->L->layout;
   }
   if (S.pool.empty()) {
     Bundle *b = new Bundle();
@@ -228,7 +233,7 @@ int admit(Server &S, Request *r, char *msg, size_t) {
                r->b->hit.as<uint8_t>()};
     wave_params(r->q, *r->L, rs, out, S.error.as<int>(), &r->params);
   }
-  r->next_chunk = r->L ? 0 : (uint32_t)S.chunks.size();
+  r->next_chunk = (r->L || r->exact) ? 0 : (uint32_t)S.chunks.size();
   return ISH_OK;
 }
 
@@ -246,7 +251,7 @@ int step(Server &S, char *msg) {
   std::vector<Cls> cls;
   std::vector<std::vector<Request *>> members;
   for (Request *r : S.active) {
-    if (r->next_chunk >= S.chunks.size()) continue;
+    if (r->next_chunk >= S.chunks.size() || r->exact) continue;
     size_t c = 0;
     for (; c < cls.size(); ++c)
       if (cls[c].K == r->K && cls[c].mode == r->mode && cls[c].layout == r->layout) break;
@@ -318,6 +323,18 @@ int step(Server &S, char *msg) {
         SCU(cudaStreamWaitEvent(s, S.join[c - 1], 0));
       }
     }
+  }
+  // ---- requests on the exact kernels: their chunk, after the batched launch ----
+  for (Request *r : S.active) {
+    if (!r->exact || r->next_chunk >= S.chunks.size()) continue;
+    const auto &ch = S.chunks[r->next_chunk];
+    OutDev out{r->b->score.as<int32_t>(), r->b->qend.as<int32_t>(), r->b->tend.as<int32_t>(), r->b->hit.as<uint8_t>()};
+    uint32_t nl = 0;
+    if (exact_enqueue(S.ctx, r->q, *S.rs, ch.first, ch.second, out, s, S.exact, &nl)) {
+      snprintf(msg, 256, "exact kernel launch failed");
+      return ISH_EDEVICE;
+    }
+    S.ctx->launches += nl;
   }
   // ---- completion of requests past their last chunk ----
   std::vector<Request *> done;
@@ -481,6 +498,7 @@ void stop_server(ish_ctx *ctx) {
   S->step_tiles.release();
   S->step_counters.release();
   S->error.release();
+  S->exact.release();
   cudaFreeHost(S->h_params);
   cudaFreeHost(S->h_tiles);
   cudaFreeHost(S->h_nhits);
@@ -519,6 +537,7 @@ int ish_gpu_serve_start(ish_ctx *ctx, int32_t set_id, uint32_t max_active, uint6
   }
   S->mem_budget = mem_budget;
   make_chunks(*S, chunks);
+  for (const auto &ch : S->chunks) S->max_chunk = std::max(S->max_chunk, ch.second);
   auto bail = [&](cudaError_t e) {
     ctx->server = S;
     stop_server(ctx);

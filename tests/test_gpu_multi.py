@@ -201,3 +201,32 @@ def test_autotune_changes_shapes_not_results(ctx):
         ctx.records_free(sid)
         for qid in ids:
             ctx.free_query(qid)
+
+
+def test_multi_with_exact_kernel_queries(ctx):
+    # queries outside the wavefront kernels' regime (gap_open <= gap_extend)
+    # run on the lane-exact kernels inside the same batched launch
+    rng = np.random.default_rng(36)
+    m = ScoringMatrix(O.BLOSUM62)
+    specs = [(80, native.ALGO_SEMI_GLOBAL, 12), (120, native.ALGO_LOCAL, 0)]
+    qs, ids = make_queries(ctx, O.BLOSUM62, specs, rng, 20, 10, 1)
+    qx = rng.integers(0, 20, 60, dtype=np.uint8)
+    mx = int(m.values[qx, qx].sum())
+    ex = [ctx.set_query(qx, O.BLOSUM62, m.values, algo, g, g, ends, mx, 0.5)
+          for algo, ends, g in ((native.ALGO_SEMI_GLOBAL, 15, 1), (native.ALGO_LOCAL, 0, 2))]
+    recs = records(rng, 20, 600, 0, 400, plants=[q for q, *_ in qs] + [qx])
+    buf, off = native.pack_records(recs)
+    sid = ctx.records_load(buf, off)
+    try:
+        order = [ids[0], ex[0], ids[1], ex[1]]
+        res = ctx.score_multi(order, sid)
+        check_against_single(ctx, order, sid, res)
+        exq = [(qx, native.ALGO_SEMI_GLOBAL, 15, mx)]
+        check_against_oracle(O.BLOSUM62, exq, buf, off, {k: (v[[1]] if k != "hit_idx" else [v[1]])
+                                                           for k, v in res.items()}, 1, 1, thr=0.5)
+        again = ctx.score_multi(order, sid)  # graph replay
+        assert np.array_equal(again["score"], res["score"])
+    finally:
+        ctx.records_free(sid)
+        for qid in ids + ex:
+            ctx.free_query(qid)

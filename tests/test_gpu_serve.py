@@ -148,9 +148,11 @@ def test_serving_memory_budget_admits_one_at_a_time(ctx):
 def test_serving_errors_stay_with_their_request(ctx):
     rng = np.random.default_rng(53)
     seqs, ids = make_queries(ctx, rng, [80, 0])
-    m = ScoringMatrix(BLOSUM62)
-    q = rng.integers(0, 20, 50, dtype=np.uint8)
-    bad = ctx.set_query(q, BLOSUM62, m.values, native.ALGO_SEMI_GLOBAL, 1, 1, 12, int(m.values[q, q].sum()), 0.5)
+    # a nucleotide query (5-letter alphabet) against protein records (codes up
+    # to 19) cannot run: its request fails alone
+    dna = ScoringMatrix(1)
+    qd = rng.integers(0, 5, 50, dtype=np.uint8)
+    bad = ctx.set_query(qd, 1, dna.values, native.ALGO_SEMI_GLOBAL, 3, 1, 12, int(dna.values[qd, qd].sum()), 0.5)
     buf, off = protein_set(rng, 1500, seqs[:1])
     sid = ctx.records_load(buf, off)
     try:
@@ -159,7 +161,7 @@ def test_serving_errors_stay_with_their_request(ctx):
         try:
             with pytest.raises(native.IshGpuError):
                 ctx.records_free(sid)  # in use by the serving loop
-            tb = ctx.submit(bad)  # gap_open == gap_extend: outside the exact fast regime
+            tb = ctx.submit(bad)
             t0, t1 = ctx.submit(ids[0]), ctx.submit(ids[1])
             with pytest.raises(native.IshGpuError) as ei:
                 wait(ctx, tb)
@@ -173,4 +175,31 @@ def test_serving_errors_stay_with_their_request(ctx):
     finally:
         ctx.records_free(sid)
         for qid in ids + [bad]:
+            ctx.free_query(qid)
+
+
+def test_serving_exact_kernel_requests(ctx):
+    # gap_open == gap_extend puts a query outside the wavefront kernels'
+    # regime: the serving loop scores its chunks with the lane-exact kernels,
+    # next to wavefront requests, and results still equal the query alone
+    rng = np.random.default_rng(54)
+    m = ScoringMatrix(BLOSUM62)
+    seqs, ids = make_queries(ctx, rng, [70, 140])
+    q = rng.integers(0, 20, 90, dtype=np.uint8)
+    ex = [ctx.set_query(q, BLOSUM62, m.values, algo, 2, 2, ends, int(m.values[q, q].sum()), 0.3)
+          for algo, ends in ((native.ALGO_SEMI_GLOBAL, 12), (native.ALGO_LOCAL, 0))]
+    buf, off = protein_set(rng, 1200, seqs + [q])
+    sid = ctx.records_load(buf, off)
+    try:
+        expect = [alone(ctx, qid, sid) for qid in ids + ex]
+        ctx.serve_start(sid, max_active=8, chunks=3)
+        try:
+            ts = [ctx.submit(qid) for qid in ids + ex]
+            for t, e, i in zip(ts, expect, range(4)):
+                same(wait(ctx, t), e, f"request {i}")
+        finally:
+            ctx.serve_stop()
+    finally:
+        ctx.records_free(sid)
+        for qid in ids + ex:
             ctx.free_query(qid)
