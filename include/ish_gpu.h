@@ -78,6 +78,7 @@ extern "C" {
 #define ISH_OPT_WAVE_GROUP 5  /* force threads per record pair (0 = autotuned) */
 #define ISH_OPT_WAVE_K 6      /* force query columns per thread (0 = autotuned) */
 #define ISH_OPT_PROFILE_LAYOUT 7 /* force the profile layout: -1 auto, 0 16-bit, 1 pair, 2 32-bit */
+#define ISH_OPT_WAVE_BLOCKS 8 /* cap wavefront blocks per SM (0 = as many as fit) */
 
 typedef struct ish_ctx ish_ctx;
 

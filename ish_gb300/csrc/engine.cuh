@@ -72,6 +72,7 @@ struct WaveParams {
   int open, ext, ends;
   int neg_limit;           // v_neg_limit of the reference (semi_global_aln/striped.mojo:329-334)
   int hleft, fin;          // left boundary value and F entering the padding
+  int frame_mask;          // semi-global: R - 1, rows between frame resets (R * ext <= 2048)
   const int16_t *hinit;    // H(-1, q) for q in [-d, Q), index q + d
   uint32_t first, count;   // sorted entries [first, first + count) are scored
   uint32_t *counter;       // work counter (record pairs), zeroed before launch

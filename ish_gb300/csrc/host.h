@@ -135,9 +135,13 @@ struct ish_ctx {
   int kernel = ISH_KERNEL_AUTO;
   int sg_lanes = 8, sw_u8_lanes = 16, sw_u16_lanes = 8;
   int force_G = 0, force_K = 0, force_layout = -1;
+  int force_blocks = 0;  // cap on wavefront blocks per SM (0: occupancy limit)
   std::map<int32_t, ish::host::Query> queries;
   int32_t next_query = 1;
   std::map<int32_t, ish::host::RecordSet> sets;
+  // device buffers of recently freed record sets, reused by the next load
+  // (a load/score/free cycle per batch then allocates nothing)
+  std::vector<ish::host::RecordSet> spare_sets;
   int32_t next_set = 1;
   // scratch
   ish::host::DevBuf raw, off_in, len_tmp, slot_tmp, poff_tmp, hist, scan_tmp, max_code;
@@ -178,9 +182,12 @@ extern thread_local std::string g_open_error;
 
 inline uint32_t ceil_div(uint64_t a, uint64_t b) { return (uint32_t)((a + b - 1) / b); }
 
+int frame_rows(int ext);
 Regime regime(const Query &q, int qpad);
 void release_query(Query &q);
 void release_set(RecordSet &rs);
+void recycle_set(ish_ctx *ctx, RecordSet &rs);
+void take_spare_set(ish_ctx *ctx, RecordSet &rs, size_t codes_bytes);
 int wave_k_available(int k);
 // Shape of the wavefront kernel for a query: the autotuner's choice when one
 // exists, else the cost model; forced options override both.

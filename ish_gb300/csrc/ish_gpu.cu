@@ -54,6 +54,47 @@ void release_set(RecordSet &rs) {
   for (DevBuf *x : b) x->release();
 }
 
+// Freed sets keep their device buffers for the next load: at most two sets,
+// each under 1 GiB of packed codes, so the cache stays small next to HBM.
+static constexpr size_t kSpareSets = 2, kSpareCodesMax = size_t(1) << 30;
+
+void recycle_set(ish_ctx *ctx, RecordSet &rs) {
+  rs.inv.release();  // rebuilt on first use by the next set
+  if (!rs.codes.p || rs.codes.cap > kSpareCodesMax) {
+    release_set(rs);
+    return;
+  }
+  if (ctx->spare_sets.size() >= kSpareSets) {
+    release_set(ctx->spare_sets.front());
+    ctx->spare_sets.erase(ctx->spare_sets.begin());
+  }
+  RecordSet keep;
+  keep.codes = rs.codes;
+  keep.off_s = rs.off_s;
+  keep.len_s = rs.len_s;
+  keep.orig_s = rs.orig_s;
+  ctx->spare_sets.push_back(keep);
+  rs.codes = rs.off_s = rs.len_s = rs.orig_s = DevBuf{};
+}
+
+// Hands `rs` the spare buffers with the smallest code area that holds
+// codes_bytes (buffers that are still too small grow in DevBuf::ensure).
+void take_spare_set(ish_ctx *ctx, RecordSet &rs, size_t codes_bytes) {
+  if (rs.codes.p || ctx->spare_sets.empty()) return;
+  size_t pick = ctx->spare_sets.size();
+  for (size_t i = 0; i < ctx->spare_sets.size(); ++i) {
+    const size_t cap = ctx->spare_sets[i].codes.cap;
+    if (cap >= codes_bytes && (pick == ctx->spare_sets.size() || cap < ctx->spare_sets[pick].codes.cap)) pick = i;
+  }
+  if (pick == ctx->spare_sets.size()) return;
+  RecordSet &sp = ctx->spare_sets[pick];
+  rs.codes = sp.codes;
+  rs.off_s = sp.off_s;
+  rs.len_s = sp.len_s;
+  rs.orig_s = sp.orig_s;
+  ctx->spare_sets.erase(ctx->spare_sets.begin() + pick);
+}
+
 void compute_rows(Query &q) {
   const int A = q.alphabet;
   q.rowmap.assign(256, 0);
@@ -79,6 +120,15 @@ int matrix_alphabet_ok(uint32_t alphabet) { return alphabet >= 1 && alphabet <= 
 // gap_open > gap_extend and no lane value of the reference can saturate or
 // wrap.  Bounds are conservative.
 
+// Semi-global rows are held in frames that rise by ext per row and drop back
+// to 0 every R rows, R a power of two with R * ext <= 2048 (the headroom the
+// regime keeps above the largest score).
+int frame_rows(int ext) {
+  int R = 1;
+  while (R < (1 << 20) && (long)2 * R * std::max(ext, 1) <= 2048) R *= 2;
+  return R;
+}
+
 Regime regime(const Query &q, int qpad) {
   Regime r;
   if (q.Q == 0) return r;
@@ -91,7 +141,8 @@ Regime regime(const Query &q, int qpad) {
     return r;
   }
   if (q.open + q.ext > 10000) return r;
-  const long base = 2L * q.open + (long)q.ext * (qpad + 2) + std::abs(q.mmin) + 64;
+  if (q.ext > 2048) return r;  // row frames (see frame_rows)
+  const long base = 2L * q.open + (long)q.ext * (qpad + 3) + std::abs(q.mmin) + 64;
   if (base > 30000) return r;
   r.fast = true;
   if (q.ends & ISH_FREE_TARGET_START) {
@@ -202,9 +253,12 @@ int build_wave_layout(ish_ctx *ctx, Query &q, int G, int K, int layout, WaveLayo
   const int A = q.rows;
   const bool sg = q.algo == ISH_ALGO_SEMI_GLOBAL;
   const int ppad = (sg && !(q.ends & ISH_FREE_TARGET_START)) ? -(q.open + q.ext) : 0;
+  // semi-global scores carry +ext: with row frames rising by ext per row,
+  // H(i-1) in frame(i-1) plus P + ext lands in frame(i)
+  const int pext = sg ? q.ext : 0;
   auto P = [&](int r, int col) -> int {
-    if (col < 0) return ppad;
-    return q.M[(size_t)q.rep[r] * q.alphabet + q.q[col]];
+    if (col < 0) return ppad + pext;
+    return q.M[(size_t)q.rep[r] * q.alphabet + q.q[col]] + pext;
   };
   std::vector<uint8_t> host;
   if (layout == PROF_PAIR) {
@@ -349,14 +403,24 @@ int pack_set(ish_ctx *ctx, uint32_t n, uint64_t raw_bytes, const uint64_t *end, 
   CU(cudaMemcpyAsync(rs.hist.data(), ctx->hist.p, (size_t)NBUCKETS * 4, cudaMemcpyDeviceToHost, s));
   k_bucket_scan<<<1, 1024, 0, s>>>(ctx->hist.as<uint32_t>());
   ++ctx->launches;
+  const uint64_t packed = rs.total + 16ull * n + 16;
+  take_spare_set(ctx, rs, packed);
   CU(rs.len_s.ensure((size_t)n * 4));
   CU(rs.off_s.ensure((size_t)n * 8));
   CU(rs.orig_s.ensure((size_t)n * 4));
   k_scatter<<<nb, 256, 0, s>>>(ctx->len_tmp.as<uint32_t>(), ctx->poff_tmp.as<uint64_t>(), n, ctx->hist.as<uint32_t>(),
                                rs.len_s.as<uint32_t>(), rs.off_s.as<uint64_t>(), rs.orig_s.as<uint32_t>());
   ++ctx->launches;
-  const uint64_t packed = rs.total + 16ull * n + 16;
-  CU(rs.codes.ensure(packed));
+  {
+    cudaError_t e = rs.codes.ensure(packed);
+    if (e == cudaErrorMemoryAllocation && !ctx->spare_sets.empty()) {  // give the cached buffers back first
+      (void)cudaGetLastError();
+      for (RecordSet &sp : ctx->spare_sets) release_set(sp);
+      ctx->spare_sets.clear();
+      e = rs.codes.ensure(packed);
+    }
+    CU(e);
+  }
   const uint32_t pb = std::min<uint32_t>(ceil_div((uint64_t)n * 32, 256), (uint32_t)ctx->num_sms * 32);
   CU(ctx->max_code.ensure(16));
   CU(cudaMemsetAsync(ctx->max_code.p, 0, 4, s));
@@ -501,6 +565,7 @@ void wave_params(const Query &q, const WaveLayout &L, const RecordSet &rs, OutDe
   const bool sg = mode == SG;
   p.hleft = (sg && !(q.ends & ISH_FREE_TARGET_START)) ? NEG_BIG : 0;
   p.fin = sg ? NEG_BIG : 0;
+  p.frame_mask = sg ? frame_rows(q.ext) - 1 : 0x3fffffff;
   p.hinit = L.hinit.as<const int16_t>();
   p.error = error;
   p.rec = RecordsDev{rs.codes.as<const uint8_t>(), rs.off_s.as<const uint64_t>(), rs.len_s.as<const uint32_t>(),
@@ -546,6 +611,7 @@ int launch_wave_range(ish_ctx *ctx, Query &q, RecordSet &rs, uint32_t first, uin
   int per_sm = 0;
   CU(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, (const void *)fn, threads, smem));
   if (per_sm < 1) return fail(ctx, ISH_EOVERFLOW, "wavefront kernel K=%d does not fit (smem %zu)", K, smem);
+  if (ctx->force_blocks) per_sm = std::min(per_sm, ctx->force_blocks);
   const uint32_t pairs = (count + 1) / 2;
   const uint32_t want = ceil_div(pairs, groups);
   const uint32_t grid = std::max<uint32_t>(1, std::min<uint32_t>(want, (uint32_t)(per_sm * ctx->num_sms)));
@@ -778,6 +844,7 @@ void ish_gpu_close(ish_ctx *ctx) {
   free_plans(ctx);
   for (auto &kv : ctx->queries) release_query(kv.second);
   for (auto &kv : ctx->sets) release_set(kv.second);
+  for (RecordSet &sp : ctx->spare_sets) release_set(sp);
   DevBuf *bufs[] = {&ctx->raw, &ctx->off_in, &ctx->len_tmp, &ctx->slot_tmp, &ctx->poff_tmp, &ctx->hist, &ctx->max_code,
                     &ctx->scan_tmp, &ctx->counter, &ctx->error, &ctx->out_score, &ctx->out_qend, &ctx->out_tend,
                     &ctx->out_hit, &ctx->hit_idx, &ctx->block_counts, &ctx->nhits, &ctx->plain_scratch,
@@ -821,6 +888,11 @@ int ish_gpu_set_option(ish_ctx *ctx, int option, int64_t value) {
     if (value != 0 && !wave_k_available((int)value))
       return fail(ctx, ISH_EINVAL, "K must be 0, 1..32 or even up to %d", WAVE_KMAX);
     ctx->force_K = (int)value;
+    drop_plans(ctx, 0, 0);
+    return ISH_OK;
+  case ISH_OPT_WAVE_BLOCKS:
+    if (value < 0 || value > 32) return fail(ctx, ISH_EINVAL, "blocks per SM must be in 0..32");
+    ctx->force_blocks = (int)value;
     drop_plans(ctx, 0, 0);
     return ISH_OK;
   default:
@@ -949,7 +1021,7 @@ int ish_gpu_records_free(ish_ctx *ctx, int32_t set_id) {
   if (server_uses_set(ctx, set_id)) return fail(ctx, ISH_EINVAL, "record set %d is used by the serving loop", set_id);
   cudaStreamSynchronize(ctx->stream);
   drop_plans(ctx, 0, set_id);
-  release_set(it->second);
+  recycle_set(ctx, it->second);
   ctx->sets.erase(it);
   return ISH_OK;
 }

@@ -170,6 +170,7 @@ int build_plan(ish_ctx *ctx, const int32_t *qids, uint32_t nq, int32_t set_id, R
     int per_sm = 0;
     CU(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, (const void *)c.fn, c.threads, c.smem));
     if (per_sm < 1) return fail(ctx, ISH_EOVERFLOW, "batch kernel K=%d does not fit (smem %zu)", c.K, c.smem);
+    if (ctx->force_blocks) per_sm = std::min(per_sm, ctx->force_blocks);
     c.grid = (uint32_t)(per_sm * ctx->num_sms);
 
     std::vector<WaveParams> params(c.members.size());

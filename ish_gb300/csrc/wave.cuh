@@ -14,7 +14,8 @@
 // long queries.
 //
 // Per cell and record pair (two cells) the recurrence costs five DPX
-// instructions, in two in-place passes over the thread's columns:
+// instructions (four for semi-global, below), in two in-place passes over the
+// thread's columns:
 //   backward:  T = max(Hdiag + P, E);  u = T - open;  E = max(E - ext, u);  H := T
 //   forward:   H = max(Fs - open, T);  Fs = max(Fs - ext, T)
 // with Fs = F + open carried along the row (local alignment floors u at 0,
@@ -23,6 +24,15 @@
 // which this recurrence keeps, so H is exactly the Gotoh H.  The serial
 // dependency along a row is the single Fs instruction per cell, and both passes
 // update H and E in place (no register rotation between rows).
+//
+// Semi-global alignment needs only four: row r is held raised by a frame
+// f(r) = (r mod R) * ext, and the profile carries +ext, so H(r-1) + P lands in
+// f(r) and the E update E' = max(E - ext, T - open) becomes
+// E'(framed) = max(T(framed) + ext - open, E(framed)), one add-max.  Every R
+// rows (R * ext <= 2048, headroom the fast regime keeps above the largest
+// score) the carried row drops back to frame 0; scores leave the kernel with
+// their frame taken off.  Local alignment keeps five: its floor at 0 would
+// move with the frame.
 //
 // End coordinates follow the reference exactly:
 //   semi-global, target end free: first row where H(i, Q-1) strictly beats the
@@ -61,6 +71,11 @@ __device__ __forceinline__ void wave_rows(const WaveParams &p, const unsigned ch
   const uint32_t NEXT = dup16(-p.ext);
   const uint32_t VFLOOR = (MODE == SW) ? 0u : dup16(-32768);
   const uint32_t FS_IN = dup16(p.fin + p.open);  // F + open entering the padding
+  // semi-global row frames: row r is held raised by frame = (r mod R) * ext
+  const uint32_t EOPEN = dup16(p.ext - p.open);                   // E' = max(T + ext - open, E)
+  const uint32_t FRAME_DROP = dup16(-(p.frame_mask + 1) * p.ext);  // back to frame 0 every R rows
+  const uint32_t NEGMIN = dup16(-32768);
+  const int f0 = (MODE == SG) ? p.ext : 0;  // row -1 sits in frame -ext
   const bool te = (MODE == SG) && (p.ends & 8);
   const bool qe = (MODE == SG) && (p.ends & 2);
   const uint32_t npairs = (p.count + 1) >> 1;
@@ -92,6 +107,7 @@ __device__ __forceinline__ void wave_rows(const WaveParams &p, const unsigned ch
   int f_left = 0;
   uint32_t f_ctl = CTL_IDLE;
   uint32_t f_seq = 31;
+  int frame = 0;    // semi-global: frame of the current row
   // the next row at which one of this thread's records ends (-3: none)
   int ev_row = -3;
   const bool remap = p.remap_off != 0;
@@ -112,9 +128,9 @@ __device__ __forceinline__ void wave_rows(const WaveParams &p, const unsigned ch
           f_seq = (f_seq + 1) & 31;
           slots[f_seq] = np;
           const uint32_t sA = p.first + 2 * np;
-          const int la = (int)p.rec.len[sA];
-          const int lb = (2 * np + 1 < p.count) ? (int)p.rec.len[sA + 1] : 0;
-          f_left = max(max(la, lb), 1);
+          const int na = (int)p.rec.len[sA];
+          const int nb = (2 * np + 1 < p.count) ? (int)p.rec.len[sA + 1] : 0;
+          f_left = max(max(na, nb), 1);
           f_ctl = CTL_NEW | (f_seq << CTL_SEQ_SHIFT);
         } else {
           f_done = true;
@@ -150,82 +166,98 @@ __device__ __forceinline__ void wave_rows(const WaveParams &p, const unsigned ch
 #pragma unroll
         for (int j = 0; j < K; ++j) {
           const int h0 = hi[j];
-          H[j] = dup16(h0);
+          H[j] = dup16(h0 - f0);
           E[j] = (MODE == SW) ? 0u : dup16(h0 - p.open);
         }
-        prevH = (t == 0) ? dup16(p.hleft) : dup16(p.hinit[t * K - 1]);
+        prevH = (t == 0) ? dup16(p.hleft - f0) : dup16(p.hinit[t * K - 1] - f0);
+        frame = 0;
         best = (MODE == SW) ? 0u : dup16(p.neg_limit);
         rowA = rowB = -1;
         row = 0;
       } else {
         ++row;
+        if (MODE == SG) {
+          if ((row & p.frame_mask) == 0) {
+            // frame R*ext -> 0: lower what this row takes from the row above
+#pragma unroll
+            for (int j = 0; j < K; ++j) {
+              H[j] = __viaddmax_s16x2(H[j], FRAME_DROP, NEGMIN);
+              E[j] = __viaddmax_s16x2(E[j], FRAME_DROP, NEGMIN);
+            }
+            prevH = __viaddmax_s16x2(prevH, FRAME_DROP, NEGMIN);
+            frame = 0;
+          } else {
+            frame += p.ext;
+          }
+        }
       }
 
       // ---- record codes of this row ----
       // Codes were checked against the alphabet when the set was loaded and
       // every record slot is zero-padded to 16 bytes.  Past a record's end the
       // last word repeats: those rows only feed a lane whose result is final.
-      if ((row & 3) == 0) {
-        wA = nA;
-        wB = nB;
-        if (row + 4 < lenA) nA = __ldg(reinterpret_cast<const uint32_t *>(pa + row + 4));
-        if (row + 4 < lenB) nB = __ldg(reinterpret_cast<const uint32_t *>(pb + row + 4));
-        // long records: pull the codes 256 rows ahead into L1, so the group's
-        // loads above hit L1 even when few warps are left to hide latency
-        if ((row & 127) == 0) {
-          if (row + 256 < lenA) asm volatile("prefetch.global.L1 [%0];" ::"l"(pa + row + 256));
-          if (row + 256 < lenB) asm volatile("prefetch.global.L1 [%0];" ::"l"(pb + row + 256));
-        }
-      }
-      uint32_t cA = wA & 0xffu, cB = wB & 0xffu;
-      if (remap) {  // codes that score alike share a profile row
-        cA = prof[p.remap_off + cA];
-        cB = prof[p.remap_off + cB];
-      }
-      wA >>= 8;
-      wB >>= 8;
-
-      // ---- profile words of this row ----
       uint32_t P[K];
-      if (LAYOUT == PROF_PAIR) {
-        const uint4 *r4 = reinterpret_cast<const uint4 *>(prof32 + ((cA * p.alphabet + cB) * G + t) * p.kp);
-#pragma unroll
-        for (int v = 0; v < (K + 3) / 4; ++v) {
-          const uint4 w = r4[v];
-          if (4 * v + 0 < K) P[4 * v + 0] = w.x;
-          if (4 * v + 1 < K) P[4 * v + 1] = w.y;
-          if (4 * v + 2 < K) P[4 * v + 2] = w.z;
-          if (4 * v + 3 < K) P[4 * v + 3] = w.w;
+      {
+        if ((row & 3) == 0) {
+          wA = nA;
+          wB = nB;
+          if (row + 4 < lenA) nA = __ldg(reinterpret_cast<const uint32_t *>(pa + row + 4));
+          if (row + 4 < lenB) nB = __ldg(reinterpret_cast<const uint32_t *>(pb + row + 4));
+          // long records: pull the codes 256 rows ahead into L1, so the
+          // group's loads above hit L1 even when few warps are left to hide
+          // latency
+          if ((row & 127) == 0) {
+            if (row + 256 < lenA) asm volatile("prefetch.global.L1 [%0];" ::"l"(pa + row + 256));
+            if (row + 256 < lenB) asm volatile("prefetch.global.L1 [%0];" ::"l"(pb + row + 256));
+          }
         }
-      } else if (LAYOUT == PROF_S32) {
-        // 32-bit words holding the 16-bit score in the low half; the packed
-        // pair is b * 65536 + a, one integer multiply-add (the multiplier is a
-        // runtime value, so this stays an IMAD on the FMA pipe, which the DPX
-        // recurrence on the ALU pipe leaves idle)
-        const uint4 *ra = reinterpret_cast<const uint4 *>(prof32 + (cA * G + t) * p.kp);
-        const uint4 *rb = reinterpret_cast<const uint4 *>(prof32 + (cB * G + t) * p.kp);
-        const uint32_t mul = p.lane_mul;
-#pragma unroll
-        for (int v = 0; v < (K + 3) / 4; ++v) {
-          const uint4 a = ra[v], b = rb[v];
-          if (4 * v + 0 < K) P[4 * v + 0] = b.x * mul + a.x;
-          if (4 * v + 1 < K) P[4 * v + 1] = b.y * mul + a.y;
-          if (4 * v + 2 < K) P[4 * v + 2] = b.z * mul + a.z;
-          if (4 * v + 3 < K) P[4 * v + 3] = b.w * mul + a.w;
+        uint32_t cA = wA & 0xffu, cB = wB & 0xffu;
+        if (remap) {  // codes that score alike share a profile row
+          cA = prof[p.remap_off + cA];
+          cB = prof[p.remap_off + cB];
         }
-      } else {
-        // 16-bit words (profiles too large for the 32-bit layout): one PRMT
-        // per packed pair
-        const uint4 *ra = reinterpret_cast<const uint4 *>(prof16 + (cA * G + t) * p.kp);
-        const uint4 *rb = reinterpret_cast<const uint4 *>(prof16 + (cB * G + t) * p.kp);
+        wA >>= 8;
+        wB >>= 8;
+        if (LAYOUT == PROF_PAIR) {
+          const uint4 *r4 = reinterpret_cast<const uint4 *>(prof32 + ((cA * p.alphabet + cB) * G + t) * p.kp);
 #pragma unroll
-        for (int v = 0; v < (K + 7) / 8; ++v) {
-          const uint4 a = ra[v], b = rb[v];
-          const uint32_t aw[4] = {a.x, a.y, a.z, a.w}, bw[4] = {b.x, b.y, b.z, b.w};
+          for (int v = 0; v < (K + 3) / 4; ++v) {
+            const uint4 w = r4[v];
+            if (4 * v + 0 < K) P[4 * v + 0] = w.x;
+            if (4 * v + 1 < K) P[4 * v + 1] = w.y;
+            if (4 * v + 2 < K) P[4 * v + 2] = w.z;
+            if (4 * v + 3 < K) P[4 * v + 3] = w.w;
+          }
+        } else if (LAYOUT == PROF_S32) {
+          // 32-bit words holding the 16-bit score in the low half; the packed
+          // pair is b * 65536 + a, one integer multiply-add (the multiplier is
+          // a runtime value, so this stays an IMAD on the FMA pipe, which the
+          // DPX recurrence on the ALU pipe leaves idle)
+          const uint4 *ra = reinterpret_cast<const uint4 *>(prof32 + (cA * G + t) * p.kp);
+          const uint4 *rb = reinterpret_cast<const uint4 *>(prof32 + (cB * G + t) * p.kp);
+          const uint32_t mul = p.lane_mul;
 #pragma unroll
-          for (int m = 0; m < 4; ++m) {
-            if (8 * v + 2 * m < K) P[8 * v + 2 * m] = __byte_perm(aw[m], bw[m], 0x5410);
-            if (8 * v + 2 * m + 1 < K) P[8 * v + 2 * m + 1] = __byte_perm(aw[m], bw[m], 0x7632);
+          for (int v = 0; v < (K + 3) / 4; ++v) {
+            const uint4 a = ra[v], b = rb[v];
+            if (4 * v + 0 < K) P[4 * v + 0] = b.x * mul + a.x;
+            if (4 * v + 1 < K) P[4 * v + 1] = b.y * mul + a.y;
+            if (4 * v + 2 < K) P[4 * v + 2] = b.z * mul + a.z;
+            if (4 * v + 3 < K) P[4 * v + 3] = b.w * mul + a.w;
+          }
+        } else {
+          // 16-bit words (profiles too large for the 32-bit layout): one PRMT
+          // per packed pair
+          const uint4 *ra = reinterpret_cast<const uint4 *>(prof16 + (cA * G + t) * p.kp);
+          const uint4 *rb = reinterpret_cast<const uint4 *>(prof16 + (cB * G + t) * p.kp);
+#pragma unroll
+          for (int v = 0; v < (K + 7) / 8; ++v) {
+            const uint4 a = ra[v], b = rb[v];
+            const uint32_t aw[4] = {a.x, a.y, a.z, a.w}, bw[4] = {b.x, b.y, b.z, b.w};
+#pragma unroll
+            for (int m = 0; m < 4; ++m) {
+              if (8 * v + 2 * m < K) P[8 * v + 2 * m] = __byte_perm(aw[m], bw[m], 0x5410);
+              if (8 * v + 2 * m + 1 < K) P[8 * v + 2 * m + 1] = __byte_perm(aw[m], bw[m], 0x7632);
+            }
           }
         }
       }
@@ -234,8 +266,12 @@ __device__ __forceinline__ void wave_rows(const WaveParams &p, const unsigned ch
 #pragma unroll
       for (int j = K - 1; j >= 0; --j) {
         const uint32_t T = __viaddmax_s16x2(j == 0 ? prevH : H[j - 1], P[j], E[j]);
-        const uint32_t u = __viaddmax_s16x2(T, NOPEN, VFLOOR);
-        E[j] = __viaddmax_s16x2(E[j], NEXT, u);
+        if (MODE == SG) {
+          E[j] = __viaddmax_s16x2(T, EOPEN, E[j]);  // in the row frames (see the header)
+        } else {
+          const uint32_t u = __viaddmax_s16x2(T, NOPEN, VFLOOR);
+          E[j] = __viaddmax_s16x2(E[j], NEXT, u);
+        }
         H[j] = T;
       }
       uint32_t Fs = (t == 0) ? FS_IN : msgF;
@@ -245,21 +281,11 @@ __device__ __forceinline__ void wave_rows(const WaveParams &p, const unsigned ch
         H[j] = __viaddmax_s16x2(Fs, NOPEN, T);
         Fs = __viaddmax_s16x2(Fs, NEXT, T);
       }
-      prevH = (t == 0) ? dup16(p.hleft) : msgH;
+      prevH = (t == 0) ? dup16(p.hleft + frame) : msgH;  // this row's H left of column 0
       outH = H[K - 1];
       outF = Fs;
       outC = msgC;
 
-      if (MODE == SG && te) {
-        // running max of column Q-1 (register K-1 of thread G-1); a strict
-        // improvement records the row, so the FIRST row of the maximum wins
-        const uint32_t nb = __viaddmax_s16x2(best, 0u, H[K - 1]);
-        if (nb != best) {
-          if (lo16(nb) != lo16(best)) rowA = row;
-          if (hi16(nb) != hi16(best)) rowB = row;
-          best = nb;
-        }
-      }
       if (MODE == SW) {
         uint32_t cm = H[0];
 #pragma unroll
@@ -303,6 +329,17 @@ __device__ __forceinline__ void wave_rows(const WaveParams &p, const unsigned ch
           if (upA) rowA = row;
           if (upB) rowB = row;
           best = ((upA ? cm : best) & 0xffffu) | ((upB ? cm : best) & 0xffff0000u);
+        }
+      }
+
+      if (MODE == SG && te) {
+        // running max of column Q-1 (register K-1 of thread G-1); a strict
+        // improvement records the row, so the FIRST row of the maximum wins
+        const uint32_t nb = __viaddmax_s16x2(best, 0u, __viaddmax_s16x2(H[K - 1], dup16(-frame), NEGMIN));
+        if (nb != best) {
+          if (lo16(nb) != lo16(best)) rowA = row;
+          if (hi16(nb) != hi16(best)) rowB = row;
+          best = nb;
         }
       }
     } else {
@@ -375,13 +412,13 @@ __device__ __forceinline__ void wave_rows(const WaveParams &p, const unsigned ch
               const int T = x == 0 ? lenA : lenB;
               int score, er, eq = p.Q - 1;
               if (!te && !qe) {
-                score = x == 0 ? lo16(H[K - 1]) : hi16(H[K - 1]);
+                score = (x == 0 ? lo16(outH) : hi16(outH)) - frame;  // this row's H(i, Q-1)
                 er = T - 1;
               } else {
                 score = te ? (x == 0 ? lo16(best) : hi16(best)) : p.neg_limit;
                 er = x == 0 ? rowA : rowB;
                 if (qe) {
-                  const int s1 = x == 0 ? lo16(mx) : hi16(mx);
+                  const int s1 = (x == 0 ? lo16(mx) : hi16(mx)) - frame;
                   const int t1 = x == 0 ? (int)(mq & 0xffffu) : (int)(mq >> 16);
                   if (s1 > score) {
                     score = s1;

@@ -41,7 +41,7 @@ def random_text(rng, nlines):
     parts = []
     for i in range(nlines):
         L = int(rng.integers(0, 90))
-        line = bytes(rng.choice(list(b"ACGTacgtNRDEQ \t*xyz"), L))
+        line = rng.choice(np.frombuffer(b"ACGTacgtNRDEQ \t*xyz\x00", np.uint8), L).tobytes()
         end = [b"\n", b"\r\n", b"\n", b"\r\r\n"][int(rng.integers(0, 4))]
         if rng.random() < 0.05:
             line = b"\r"  # a lone carriage return is kept
@@ -122,4 +122,37 @@ def test_lines_against_oracle(ctx):
         assert list(r["hit_idx"]) == want and len(want) >= 300
     finally:
         ctx.records_free(sid)
+        ctx.free_query(qid)
+
+
+def test_freed_set_buffers_are_reused_exactly(ctx):
+    # records_free keeps a freed set's device buffers for the next load: sets
+    # of other sizes loaded into them score exactly like a set loaded fresh
+    rng = np.random.default_rng(47)
+    qid, m = query_for(ctx, O.BLOSUM62, rng, qlen=40)
+
+    def make(n, lo, hi):
+        recs = [rng.integers(0, 20, int(rng.integers(lo, hi)), dtype=np.uint8) for _ in range(n)]
+        return native.pack_records(recs)
+
+    sets = [make(3000, 50, 400), make(500, 1, 40), make(8000, 100, 900), make(2, 0, 3)]
+    keep = [ctx.records_load(b, o) for b, o in sets]  # fresh buffers: the expected results
+    expect = [ctx.score_set(qid, s) for s in keep]
+    for s in keep:
+        ctx.records_free(s)
+    try:
+        for order in ([0, 1, 2, 3], [2, 0, 3, 1], [1, 1, 2, 2, 0]):
+            for i in order:
+                sid = ctx.records_load(*sets[i])
+                got = ctx.score_set(qid, sid)
+                ctx.records_free(sid)
+                for k in ("score", "qend", "tend", "hit", "hit_idx"):
+                    assert np.array_equal(got[k], expect[i][k]), (order, i, k)
+        # two sets alive at once take different buffers
+        a, b = ctx.records_load(*sets[0]), ctx.records_load(*sets[2])
+        ra, rb = ctx.score_set(qid, a), ctx.score_set(qid, b)
+        assert np.array_equal(ra["score"], expect[0]["score"]) and np.array_equal(rb["score"], expect[2]["score"])
+        ctx.records_free(a)
+        ctx.records_free(b)
+    finally:
         ctx.free_query(qid)

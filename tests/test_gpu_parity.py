@@ -131,6 +131,27 @@ def test_forced_group_shapes(ctx, G):
         ctx.set_option(native.OPT_WAVE_K, 0)
 
 
+@pytest.mark.parametrize("G,K", [(2, 52), (2, 64), (4, 50), (4, 64), (16, 64)])
+def test_wide_rows_interleaved_schedule(ctx, G, K):
+    # from 49 columns per thread on, the next row's backward pass runs inside
+    # the current row's forward pass; every end rule, records of unequal
+    # lengths in a pair (one lane ends rows before the other) and empty ones
+    rng = np.random.default_rng(19 + K)
+    q = rng.integers(0, 20, 100, dtype=np.uint8)
+    recs = random_records(rng, 20, 160, 0, 500, q)
+    ctx.set_option(native.OPT_WAVE_GROUP, G)
+    ctx.set_option(native.OPT_WAVE_K, K)
+    try:
+        for ends in ALL_ENDS:
+            g, o = run_both(ctx, native.ALGO_SEMI_GLOBAL, O.BLOSUM62, q, recs, 10, 1, ends)
+            assert_same(g, o, f"G={G} K={K} SG ends={ends}")
+        g, o = run_both(ctx, native.ALGO_LOCAL, O.BLOSUM62, q, recs, 10, 1, 0)
+        assert_same(g, o, f"G={G} K={K} SW")
+    finally:
+        ctx.set_option(native.OPT_WAVE_GROUP, 0)
+        ctx.set_option(native.OPT_WAVE_K, 0)
+
+
 @pytest.mark.parametrize("algo", [native.ALGO_SEMI_GLOBAL, native.ALGO_LOCAL])
 def test_plain_kernel_parity(ctx, algo):
     rng = np.random.default_rng(13)
