@@ -79,6 +79,7 @@ extern "C" {
 #define ISH_OPT_WAVE_K 6      /* force query columns per thread (0 = autotuned) */
 #define ISH_OPT_PROFILE_LAYOUT 7 /* force the profile layout: -1 auto, 0 16-bit, 1 pair, 2 32-bit */
 #define ISH_OPT_WAVE_BLOCKS 8 /* cap wavefront blocks per SM (0 = as many as fit) */
+#define ISH_OPT_WAVE_LEAN 9   /* 34 <= K <= 48: -1 measured default, 0 128x3 blocks, 1 128x2 (more registers) */
 
 typedef struct ish_ctx ish_ctx;
 

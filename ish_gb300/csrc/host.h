@@ -136,6 +136,7 @@ struct ish_ctx {
   int sg_lanes = 8, sw_u8_lanes = 16, sw_u16_lanes = 8;
   int force_G = 0, force_K = 0, force_layout = -1;
   int force_blocks = 0;  // cap on wavefront blocks per SM (0: occupancy limit)
+  int force_lean = -1;   // lean kernel variant: -1 per (K, mode) default, 0 off, 1 on
   std::map<int32_t, ish::host::Query> queries;
   int32_t next_query = 1;
   std::map<int32_t, ish::host::RecordSet> sets;
@@ -183,6 +184,7 @@ extern thread_local std::string g_open_error;
 inline uint32_t ceil_div(uint64_t a, uint64_t b) { return (uint32_t)((a + b - 1) / b); }
 
 int frame_rows(int ext);
+int wave_lean(const ish_ctx *ctx, int K, int mode);
 Regime regime(const Query &q, int qpad);
 void release_query(Query &q);
 void release_set(RecordSet &rs);

@@ -123,6 +123,20 @@ int matrix_alphabet_ok(uint32_t alphabet) { return alphabet >= 1 && alphabet <= 
 // Semi-global rows are held in frames that rise by ext per row and drop back
 // to 0 every R rows, R a power of two with R * ext <= 2048 (the headroom the
 // regime keeps above the largest score).
+// Whether (K, mode) runs the lean kernel variant (128 x 2 blocks with more
+// registers instead of 128 x 3), as measured on GB300 for the protein search
+// (blosum62, 400k records, G = 8, Q = 8K - 2): semi-global +2.5 to +13.6 %
+// for K = 34..44 and -11 to -14 % at 46/48; local +0.3 to +7.4 % at
+// 34..38 and 46/48, -6 to -12 % at 40..44.
+int wave_lean(const ish_ctx *ctx, int K, int mode) {
+  if (K < WAVE_LEAN_KMIN || K > WAVE_LEAN_KMAX) return 0;
+  if (ctx->force_lean >= 0) return ctx->force_lean;
+  const int i = (K - WAVE_LEAN_KMIN) / 2;  //             K = 34 36 38 40 42 44 46 48
+  static const unsigned char lean[2][8] = {/* semi-global */ {1, 1, 1, 1, 1, 1, 0, 0},
+                                           /* local */ {1, 1, 1, 0, 0, 0, 1, 1}};
+  return lean[mode == SW][i];
+}
+
 int frame_rows(int ext) {
   int R = 1;
   while (R < (1 << 20) && (long)2 * R * std::max(ext, 1) <= 2048) R *= 2;
@@ -589,7 +603,7 @@ int launch_wave_range(ish_ctx *ctx, Query &q, RecordSet &rs, uint32_t first, uin
   int rc = build_wave_layout(ctx, q, G, K, layout, &L);
   if (rc) return rc;
   const int mode = q.algo == ISH_ALGO_LOCAL ? SW : SG;
-  WaveFn fn = wave_fn(K, mode, L->layout);
+  WaveFn fn = wave_fn(K, mode, L->layout, wave_lean(ctx, K, mode));
   if (!fn) return fail(ctx, ISH_EOVERFLOW, "no wavefront kernel for K=%d", K);
   const int threads = wave_block_threads(K, mode);
   const int groups = threads / G;
@@ -890,6 +904,11 @@ int ish_gpu_set_option(ish_ctx *ctx, int option, int64_t value) {
     ctx->force_K = (int)value;
     drop_plans(ctx, 0, 0);
     return ISH_OK;
+  case ISH_OPT_WAVE_LEAN:
+    if (value < -1 || value > 1) return fail(ctx, ISH_EINVAL, "lean variant must be -1, 0 or 1");
+    ctx->force_lean = (int)value;
+    drop_plans(ctx, 0, 0);
+    return ISH_OK;
   case ISH_OPT_WAVE_BLOCKS:
     if (value < 0 || value > 32) return fail(ctx, ISH_EINVAL, "blocks per SM must be in 0..32");
     ctx->force_blocks = (int)value;
@@ -1109,8 +1128,11 @@ WaveFn wave_fn_c(int, int, int);
 WaveFn wave_fn_d(int, int, int);
 WaveFn wave_fn_e(int, int, int);
 WaveFn wave_fn_f(int, int, int);
-WaveFn wave_fn(int K, int mode, int layout) {
+WaveFn wave_fn_g(int, int, int);
+BatchFn batch_fn_g(int, int, int);
+WaveFn wave_fn(int K, int mode, int layout, int lean) {
   if (K < 1) return nullptr;
+  if (lean && K >= WAVE_LEAN_KMIN && K <= WAVE_LEAN_KMAX) return wave_fn_g(K, mode, layout);
   if (K <= 8) return wave_fn_a(K, mode, layout);
   if (K <= 16) return wave_fn_b(K, mode, layout);
   if (K <= 24) return wave_fn_c(K, mode, layout);
@@ -1124,8 +1146,9 @@ BatchFn batch_fn_c(int, int, int);
 BatchFn batch_fn_d(int, int, int);
 BatchFn batch_fn_e(int, int, int);
 BatchFn batch_fn_f(int, int, int);
-BatchFn batch_fn(int K, int mode, int layout) {
+BatchFn batch_fn(int K, int mode, int layout, int lean) {
   if (K < 1) return nullptr;
+  if (lean && K >= WAVE_LEAN_KMIN && K <= WAVE_LEAN_KMAX) return batch_fn_g(K, mode, layout);
   if (K <= 8) return batch_fn_a(K, mode, layout);
   if (K <= 16) return batch_fn_b(K, mode, layout);
   if (K <= 24) return batch_fn_c(K, mode, layout);

@@ -48,14 +48,21 @@ __host__ __device__ constexpr int wave_block_threads(int K, int mode) {
 __host__ __device__ constexpr int wave_blocks_per_sm(int K, int mode) {
   return K <= 32 ? 2 : (K <= 48 ? 3 : (mode == 1 ? 1 : 2));
 }
+// The lean variant of 32 < K <= 48 runs 128 x 2 instead of 128 x 3: 8 warps
+// per SM with up to 255 registers per thread instead of 12 with 168, which is
+// faster for some (K, mode) -- spills against warps (wave_lean_default).
+constexpr int WAVE_LEAN_KMIN = 34, WAVE_LEAN_KMAX = 48;
+__host__ __device__ constexpr int wave_blocks_lean(int K, int mode, int lean) {
+  return (lean && K >= WAVE_LEAN_KMIN && K <= WAVE_LEAN_KMAX) ? 2 : wave_blocks_per_sm(K, mode);
+}
 // Local alignment keeps, per thread, the H row of each lane's last
 // improvement as 16-bit values: two arrays of K (rounded up to 8) halves,
 // strided by an odd number of 16-byte units.
 __host__ __device__ constexpr int wave_save_words(int K) { return ((((K + 7) & ~7) / 4) | 1) * 4; }
 typedef void (*WaveFn)(const WaveParams);
-// Returns the kernel for (K, mode, profile layout) or nullptr.
-WaveFn wave_fn(int K, int mode, int layout);
+// Returns the kernel for (K, mode, profile layout, lean variant) or nullptr.
+WaveFn wave_fn(int K, int mode, int layout, int lean = 0);
 typedef void (*BatchFn)(const BatchParams);
-BatchFn batch_fn(int K, int mode, int layout);  // batch_kernel<K, mode, layout> or nullptr
+BatchFn batch_fn(int K, int mode, int layout, int lean = 0);  // batch_kernel<K, mode, layout, lean> or nullptr
 
 }  // namespace ish

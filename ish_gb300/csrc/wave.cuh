@@ -73,9 +73,10 @@ __device__ __forceinline__ void wave_rows(const WaveParams &p, const unsigned ch
   const uint32_t FS_IN = dup16(p.fin + p.open);  // F + open entering the padding
   // semi-global row frames: row r is held raised by frame = (r mod R) * ext
   const uint32_t EOPEN = dup16(p.ext - p.open);                   // E' = max(T + ext - open, E)
-  const uint32_t FRAME_DROP = dup16(-(p.frame_mask + 1) * p.ext);  // back to frame 0 every R rows
   const uint32_t NEGMIN = dup16(-32768);
   const int f0 = (MODE == SG) ? p.ext : 0;  // row -1 sits in frame -ext
+  // the frame of a row (always 0 for local alignment)
+  auto frame_of = [&](int r) { return (MODE == SG) ? (r & p.frame_mask) * p.ext : 0; };
   const bool te = (MODE == SG) && (p.ends & 8);
   const bool qe = (MODE == SG) && (p.ends & 2);
   const uint32_t npairs = (p.count + 1) >> 1;
@@ -107,7 +108,6 @@ __device__ __forceinline__ void wave_rows(const WaveParams &p, const unsigned ch
   int f_left = 0;
   uint32_t f_ctl = CTL_IDLE;
   uint32_t f_seq = 31;
-  int frame = 0;    // semi-global: frame of the current row
   // the next row at which one of this thread's records ends (-3: none)
   int ev_row = -3;
   const bool remap = p.remap_off != 0;
@@ -170,7 +170,6 @@ __device__ __forceinline__ void wave_rows(const WaveParams &p, const unsigned ch
           E[j] = (MODE == SW) ? 0u : dup16(h0 - p.open);
         }
         prevH = (t == 0) ? dup16(p.hleft - f0) : dup16(p.hinit[t * K - 1] - f0);
-        frame = 0;
         best = (MODE == SW) ? 0u : dup16(p.neg_limit);
         rowA = rowB = -1;
         row = 0;
@@ -179,15 +178,13 @@ __device__ __forceinline__ void wave_rows(const WaveParams &p, const unsigned ch
         if (MODE == SG) {
           if ((row & p.frame_mask) == 0) {
             // frame R*ext -> 0: lower what this row takes from the row above
+            const uint32_t FRAME_DROP = dup16(-(p.frame_mask + 1) * p.ext);
 #pragma unroll
             for (int j = 0; j < K; ++j) {
               H[j] = __viaddmax_s16x2(H[j], FRAME_DROP, NEGMIN);
               E[j] = __viaddmax_s16x2(E[j], FRAME_DROP, NEGMIN);
             }
             prevH = __viaddmax_s16x2(prevH, FRAME_DROP, NEGMIN);
-            frame = 0;
-          } else {
-            frame += p.ext;
           }
         }
       }
@@ -281,7 +278,7 @@ __device__ __forceinline__ void wave_rows(const WaveParams &p, const unsigned ch
         H[j] = __viaddmax_s16x2(Fs, NOPEN, T);
         Fs = __viaddmax_s16x2(Fs, NEXT, T);
       }
-      prevH = (t == 0) ? dup16(p.hleft + frame) : msgH;  // this row's H left of column 0
+      prevH = (t == 0) ? dup16(p.hleft + frame_of(row)) : msgH;  // this row's H left of column 0
       outH = H[K - 1];
       outF = Fs;
       outC = msgC;
@@ -335,7 +332,7 @@ __device__ __forceinline__ void wave_rows(const WaveParams &p, const unsigned ch
       if (MODE == SG && te) {
         // running max of column Q-1 (register K-1 of thread G-1); a strict
         // improvement records the row, so the FIRST row of the maximum wins
-        const uint32_t nb = __viaddmax_s16x2(best, 0u, __viaddmax_s16x2(H[K - 1], dup16(-frame), NEGMIN));
+        const uint32_t nb = __viaddmax_s16x2(best, 0u, __viaddmax_s16x2(H[K - 1], dup16(-frame_of(row)), NEGMIN));
         if (nb != best) {
           if (lo16(nb) != lo16(best)) rowA = row;
           if (hi16(nb) != hi16(best)) rowB = row;
@@ -412,13 +409,13 @@ __device__ __forceinline__ void wave_rows(const WaveParams &p, const unsigned ch
               const int T = x == 0 ? lenA : lenB;
               int score, er, eq = p.Q - 1;
               if (!te && !qe) {
-                score = (x == 0 ? lo16(outH) : hi16(outH)) - frame;  // this row's H(i, Q-1)
+                score = (x == 0 ? lo16(outH) : hi16(outH)) - frame_of(row);  // this row's H(i, Q-1)
                 er = T - 1;
               } else {
                 score = te ? (x == 0 ? lo16(best) : hi16(best)) : p.neg_limit;
                 er = x == 0 ? rowA : rowB;
                 if (qe) {
-                  const int s1 = (x == 0 ? lo16(mx) : hi16(mx)) - frame;
+                  const int s1 = (x == 0 ? lo16(mx) : hi16(mx)) - frame_of(row);
                   const int t1 = x == 0 ? (int)(mq & 0xffffu) : (int)(mq >> 16);
                   if (s1 > score) {
                     score = s1;
@@ -502,8 +499,8 @@ __device__ __forceinline__ void wave_rows(const WaveParams &p, const unsigned ch
 
 // Shared memory of a block: the profile, then 32 slot words per group, then
 // (local alignment) wave_save_words(K) save words per thread.
-template <int K, int MODE, int LAYOUT>
-__global__ void __launch_bounds__(wave_block_threads(K, MODE), wave_blocks_per_sm(K, MODE))
+template <int K, int MODE, int LAYOUT, int LEAN = 0>
+__global__ void __launch_bounds__(wave_block_threads(K, MODE), wave_blocks_lean(K, MODE, LEAN))
     wave_kernel(const __grid_constant__ WaveParams p) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   {
@@ -526,8 +523,8 @@ __global__ void __launch_bounds__(wave_block_threads(K, MODE), wave_blocks_per_s
 // the queries) and stays on a query until its counter runs dry; a barrier and
 // a profile reload happen only at a query switch, where the pairs left are the
 // shortest of the set.  Queries whose counter is already exhausted are skipped.
-template <int K, int MODE, int LAYOUT>
-__global__ void __launch_bounds__(wave_block_threads(K, MODE), wave_blocks_per_sm(K, MODE))
+template <int K, int MODE, int LAYOUT, int LEAN = 0>
+__global__ void __launch_bounds__(wave_block_threads(K, MODE), wave_blocks_lean(K, MODE, LEAN))
     batch_kernel(const __grid_constant__ BatchParams b) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   __shared__ WaveParams sp;

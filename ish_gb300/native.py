@@ -19,6 +19,7 @@ KERNEL_AUTO, KERNEL_PLAIN, KERNEL_EXACT = 0, 1, 2
 OPT_KERNEL, OPT_SG_LANES, OPT_SW_U8_LANES, OPT_SW_U16_LANES, OPT_WAVE_GROUP, OPT_WAVE_K = 1, 2, 3, 4, 5, 6
 OPT_PROFILE_LAYOUT = 7
 OPT_WAVE_BLOCKS = 8
+OPT_WAVE_LEAN = 9
 PROF_AUTO, PROF_S16, PROF_PAIR, PROF_S32 = -1, 0, 1, 2
 
 # Entry points declared in include/ish_gpu.h (checked by the tests).
