@@ -79,6 +79,7 @@ extern "C" {
 #define ISH_OPT_WAVE_K 6      /* force query columns per thread (0 = autotuned) */
 #define ISH_OPT_PROFILE_LAYOUT 7 /* force the profile layout: -1 auto, 0 16-bit, 1 pair, 2 32-bit */
 #define ISH_OPT_WAVE_BLOCKS 8 /* cap wavefront blocks per SM (0 = as many as fit) */
+#define ISH_OPT_WINDOWS 10    /* 1 (default): window long records when they would bound the pass; 0: never */
 #define ISH_OPT_WAVE_LEAN 9   /* 34 <= K <= 48: -1 measured default, 0 128x3 blocks, 1 128x2 (more registers) */
 
 typedef struct ish_ctx ish_ctx;
@@ -267,6 +268,14 @@ ISH_API int ish_gpu_calibrate(ish_ctx *ctx, double *dpx_ops_per_s);
  * launch counts the kernel nodes of its graph).  No counterpart in the
  * reference: measurement support. */
 ISH_API int ish_gpu_launch_count(ish_ctx *ctx, uint64_t *count);
+
+/* Windows the last single-query scoring call cut its longest records into
+ * (0: the set was scored record by record).  With a free target start the
+ * best alignment spans a bounded number of record rows, so long records are
+ * scored as overlapping windows and folded per record, with results identical
+ * to whole-record scoring (see ISH_OPT_WINDOWS).  No counterpart in the
+ * reference: measurement support. */
+ISH_API int ish_gpu_last_windows(ish_ctx *ctx, uint32_t *windows);
 
 #ifdef __cplusplus
 }

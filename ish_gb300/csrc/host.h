@@ -89,6 +89,34 @@ inline void clone_params(const Query &src, Query &dst) {
   dst.rep = src.rep;
 }
 
+// Window view of a record set (windows.cu): its long records cut into
+// overlapping windows, the rest whole, longest first.
+struct WindowView {
+  uint64_t W = 0, O = 0;      // window stride and overlap (rows)
+  uint32_t entries = 0;       // sorted entries covered
+  uint32_t nw = 0;            // windows (slots)
+  uint64_t total = 0;         // rows over all windows
+  uint32_t max_len = 0;
+  DevBuf off, len, slot;      // per view entry (longest first): code offset, rows, slot
+  DevBuf start, cs;           // per slot: first record row; per entry: first slot (n + 1)
+  void release() {
+    DevBuf *b[] = {&off, &len, &slot, &start, &cs};
+    for (DevBuf *x : b) x->release();
+    nw = 0;
+  }
+};
+
+// Per-window results of the last windowed pass (windows.cu).
+struct WindowOut {
+  DevBuf score, qend, tend, hit;
+  void release() {
+    score.release();
+    qend.release();
+    tend.release();
+    hit.release();
+  }
+};
+
 struct RecordSet {
   uint32_t n = 0;
   uint64_t total = 0;
@@ -98,6 +126,7 @@ struct RecordSet {
   uint32_t n_empty = 0;
   uint32_t max_code = 0;       // largest record code in the set
   DevBuf inv;                  // sorted entry of each original record (built on first use)
+  WindowView windows;          // built on first windowed pass
 };
 
 struct Regime {
@@ -137,6 +166,7 @@ struct ish_ctx {
   int force_G = 0, force_K = 0, force_layout = -1;
   int force_blocks = 0;  // cap on wavefront blocks per SM (0: occupancy limit)
   int force_lean = -1;   // lean kernel variant: -1 per (K, mode) default, 0 off, 1 on
+  int windows_on = 1;    // window long records (windows.cu)
   std::map<int32_t, ish::host::Query> queries;
   int32_t next_query = 1;
   std::map<int32_t, ish::host::RecordSet> sets;
@@ -150,6 +180,8 @@ struct ish_ctx {
   ish::host::DevBuf plain_scratch;
   ish::host::DevBuf enc_tables, nl_pos, line_end;  // encoding tables; line splitting scratch
   ish::host::ExactRes exact;                        // exact kernels (exact.cu)
+  ish::host::WindowOut window_out;                  // windowed passes (windows.cu)
+  uint32_t last_windows = 0;                        // windows of the last windowed pass
   float last_ms = 0.f;
   // batched launches (multi.cu): plans cached per (queries, set, outputs)
   std::map<std::string, ish::host::MultiPlan *> plans;
@@ -185,6 +217,8 @@ inline uint32_t ceil_div(uint64_t a, uint64_t b) { return (uint32_t)((a + b - 1)
 
 int frame_rows(int ext);
 int wave_lean(const ish_ctx *ctx, int K, int mode);
+uint64_t window_overlap(const Query &q);
+int launch_windows(ish_ctx *ctx, Query &q, RecordSet &rs, uint32_t nonempty, OutDev out, cudaStream_t s, bool *done);
 Regime regime(const Query &q, int qpad);
 void release_query(Query &q);
 void release_set(RecordSet &rs);

@@ -52,6 +52,7 @@ void release_query(Query &q) {
 void release_set(RecordSet &rs) {
   DevBuf *b[] = {&rs.codes, &rs.off_s, &rs.len_s, &rs.orig_s, &rs.inv};
   for (DevBuf *x : b) x->release();
+  rs.windows.release();
 }
 
 // Freed sets keep their device buffers for the next load: at most two sets,
@@ -60,6 +61,7 @@ static constexpr size_t kSpareSets = 2, kSpareCodesMax = size_t(1) << 30;
 
 void recycle_set(ish_ctx *ctx, RecordSet &rs) {
   rs.inv.release();  // rebuilt on first use by the next set
+  rs.windows.release();
   if (!rs.codes.p || rs.codes.cap > kSpareCodesMax) {
     release_set(rs);
     return;
@@ -768,10 +770,14 @@ int run_scoring(ish_ctx *ctx, Query &q, RecordSet &rs) {
     if (rs.max_code >= (uint32_t)q.alphabet)
       return fail(ctx, ISH_EINVAL, "a record contains code %u >= the alphabet size %d of the query", rs.max_code,
                   q.alphabet);
-    if (ctx->kernel == ISH_KERNEL_EXACT || !fast_regime(ctx, q, rs))
+    if (ctx->kernel == ISH_KERNEL_EXACT || !fast_regime(ctx, q, rs)) {
       rc = launch_exact(ctx, q, rs, 0, nonempty, out, s);
-    else
-      rc = launch_range(ctx, q, rs, 0, nonempty, out, s);
+    } else {
+      bool windowed = false;
+      ctx->last_windows = 0;
+      rc = launch_windows(ctx, q, rs, nonempty, out, s, &windowed);
+      if (!rc && !windowed) rc = launch_range(ctx, q, rs, 0, nonempty, out, s);
+    }
     if (rc) return rc;
   }
   return ISH_OK;
@@ -865,6 +871,7 @@ void ish_gpu_close(ish_ctx *ctx) {
                     &ctx->enc_tables, &ctx->nl_pos, &ctx->line_end};
   for (DevBuf *b : bufs) b->release();
   ctx->exact.release();
+  ctx->window_out.release();
   cudaEventDestroy(ctx->ev0);
   cudaEventDestroy(ctx->ev1);
   cudaStreamDestroy(ctx->stream);
@@ -903,6 +910,10 @@ int ish_gpu_set_option(ish_ctx *ctx, int option, int64_t value) {
       return fail(ctx, ISH_EINVAL, "K must be 0, 1..32 or even up to %d", WAVE_KMAX);
     ctx->force_K = (int)value;
     drop_plans(ctx, 0, 0);
+    return ISH_OK;
+  case ISH_OPT_WINDOWS:
+    if (value != 0 && value != 1) return fail(ctx, ISH_EINVAL, "windows must be 0 or 1");
+    ctx->windows_on = (int)value;
     return ISH_OK;
   case ISH_OPT_WAVE_LEAN:
     if (value < -1 || value > 1) return fail(ctx, ISH_EINVAL, "lean variant must be -1, 0 or 1");
@@ -1109,6 +1120,12 @@ int ish_gpu_calibrate(ish_ctx *ctx, double *dpx_ops_per_s) {
 int ish_gpu_launch_count(ish_ctx *ctx, uint64_t *count) {
   if (!ctx || !count) return ISH_EINVAL;
   *count = ctx->launches.load();
+  return ISH_OK;
+}
+
+int ish_gpu_last_windows(ish_ctx *ctx, uint32_t *windows) {
+  if (!ctx || !windows) return ISH_EINVAL;
+  *windows = ctx->last_windows;
   return ISH_OK;
 }
 

@@ -1,0 +1,202 @@
+// windows.cu -- long records scored as overlapping windows.
+//
+// With a free target start, the best alignment of a query against a long
+// record never spans more than a bounded number of record rows: a path over S
+// rows makes at most Q diagonal steps, so at least S - Q rows are a gap in the
+// query, and its score is at most Q * mmax - open - (S - Q - 1) * ext, while
+// the best score is at least the full-query diagonal's Q * mmin (semi-global)
+// or positive (local).  So S <= O = Q + 1 + (Q * mmax - open - M_min) / ext.
+//
+// A window of a record that starts at row s >= 0 and runs the same
+// recurrence from the fresh boundary of row s scores every cell at most as
+// high as the whole record does (its paths are a subset), and exactly as
+// high at every cell whose best path starts inside the window.  Windows that
+// overlap by O rows therefore hold, for the record's best cell (the first
+// row, then the smallest column, of its maximum), that cell's exact value in
+// some window, and no cell before it reaches that value in any window.  The
+// record's result is the window result with the largest score, then the
+// smallest record row, then the smallest query column -- exactly the
+// whole-record result, end coordinates and tie rules included:
+//   semi-global with free target start and end and a fixed query end (the
+//     target-end maximum of semi_global_aln/striped.mojo:436-450);
+//   local alignment (local_aln/striped.mojo:395-428).
+//
+// The point is load balance: a pass over records of very unequal lengths is
+// bound by its longest record pairs, one group each, however many groups
+// finish early.  Windows of equal length spread those records over all
+// groups.  This file decides when to window, builds the window view of the
+// set (windows of the long records plus the other records whole, longest
+// first), scores it with the wavefront kernel into per-window results, and
+// folds them per record on the device.
+#include <algorithm>
+#include <numeric>
+#include <vector>
+
+#include "host.h"
+
+namespace ish {
+
+// One thread per sorted entry: fold the entry's window results (slots
+// [cs[e], cs[e+1]), window w starting at record row start[w]) into its outputs.
+__global__ void k_merge_windows(const uint32_t *orig_s, uint32_t n, const uint32_t *cs, const uint32_t *start,
+                                const int32_t *ws, const int32_t *wq, const int32_t *wt, int mode, OutDev out,
+                                Decision dec) {
+  for (uint32_t e = blockIdx.x * blockDim.x + threadIdx.x; e < n; e += gridDim.x * blockDim.x) {
+    const uint32_t a = cs[e], b = cs[e + 1];
+    int bs = ws[a], bq = wq[a];
+    long long bt = wt[a] >= 0 ? (long long)wt[a] + start[a] : -1;
+    for (uint32_t w = a + 1; w < b; ++w) {
+      const int sc = ws[w], tq = wq[w];
+      const long long tt = wt[w] >= 0 ? (long long)wt[w] + start[w] : -1;
+      // equal scores carry rows of the same kind (all -1 when nothing beat
+      // the initial best), so the row and column order the ties
+      if (sc > bs || (sc == bs && tt >= 0 && (tt < bt || (tt == bt && tq < bq)))) {
+        bs = sc;
+        bq = tq;
+        bt = tt;
+      }
+    }
+    const uint32_t o = orig_s[e];
+    if (out.score) out.score[o] = bs;
+    if (out.qend) out.qend[o] = bq;
+    if (out.tend) out.tend[o] = (int32_t)bt;
+    if (out.hit) out.hit[o] = decide(mode, bs, bq, (int)bt, dec);
+  }
+}
+
+namespace host {
+
+// Rows two windows of a record must share (see above), or 0 when no bound
+// holds for this query.
+uint64_t window_overlap(const Query &q) {
+  const int mode = q.algo == ISH_ALGO_LOCAL ? SW : SG;
+  if (q.ext < 1 || q.Q == 0) return 0;
+  if (mode == SG && !((q.ends & ISH_FREE_TARGET_START) && (q.ends & ISH_FREE_TARGET_END) &&
+                      !(q.ends & ISH_FREE_QUERY_END)))
+    return 0;
+  const long long mmin = mode == SG ? std::min(q.mmin, 0) : 0;
+  const long long min_best = mode == SG ? (long long)q.Q * mmin : 0;
+  const long long top = (long long)q.Q * std::max(q.mmax, 0) - q.open - min_best;
+  const long long o = (long long)q.Q + 2 + std::max(0LL, (top + q.ext - 1) / q.ext);
+  return (uint64_t)((o + 15) & ~15LL);
+}
+
+// Scores sorted entries [0, nonempty) of rs through the window view when its
+// longest records would bound the pass; *done is false when it did nothing.
+// The view is built once per (set, stride, overlap) and kept with the set.
+int launch_windows(ish_ctx *ctx, Query &q, RecordSet &rs, uint32_t nonempty, OutDev out, cudaStream_t s,
+                   bool *done) {
+  *done = false;
+  if (!ctx->windows_on || ctx->kernel != ISH_KERNEL_AUTO || nonempty == 0 || nonempty > (1u << 22)) return ISH_OK;
+  const uint64_t O = window_overlap(q);
+  if (!O) return ISH_OK;
+  const int mode = q.algo == ISH_ALGO_LOCAL ? SW : SG;
+  int G, K, layout;
+  pick_shape(ctx, q, &G, &K, &layout);
+  if (!G || !wave_fits(q, G, K, layout)) return ISH_OK;
+  // groups in flight and the rows each would score on average (two records
+  // per pair share their rows)
+  const uint64_t groups = (uint64_t)ctx->num_sms * wave_blocks_lean(K, mode, wave_lean(ctx, K, mode)) *
+                          (wave_block_threads(K, mode) / G);
+  const uint64_t avg_rows = rs.total / 2 / std::max<uint64_t>(groups, 1);
+  // window stride: about four pairs of windows per group, and at least 8x
+  // the overlap so that windowing adds at most an eighth of the work
+  uint64_t W = std::max<uint64_t>(8 * O, rs.total / std::max<uint64_t>(8 * groups, 1));
+  W = (W + 15) & ~15ull;
+  if (rs.max_len <= 2 * avg_rows || rs.max_len <= W + O) return ISH_OK;
+
+  WindowView &V = rs.windows;
+  if (!(V.nw && V.W == W && V.O == O && V.entries == nonempty)) {
+    V.release();
+    std::vector<uint32_t> len(nonempty);
+    std::vector<uint64_t> off(nonempty);
+    CU(cudaStreamSynchronize(s));
+    CU(cudaMemcpy(len.data(), rs.len_s.p, (size_t)nonempty * 4, cudaMemcpyDeviceToHost));
+    CU(cudaMemcpy(off.data(), rs.off_s.p, (size_t)nonempty * 8, cudaMemcpyDeviceToHost));
+    // slots: the windows of entry e are [cs[e], cs[e+1]); each has a first
+    // record row, a length and a code offset
+    std::vector<uint32_t> cs(nonempty + 1), wstart, wlen;
+    std::vector<uint64_t> woff;
+    for (uint32_t e = 0; e < nonempty; ++e) {
+      cs[e] = (uint32_t)wstart.size();
+      const uint64_t L = len[e];
+      if (L <= W + O) {
+        wstart.push_back(0);
+        wlen.push_back((uint32_t)L);
+        woff.push_back(off[e]);
+        continue;
+      }
+      for (uint64_t k = 0; k * W < L; ++k) {
+        const uint64_t st = k == 0 ? 0 : ((k * W - O) & ~15ull);
+        const uint64_t en = std::min<uint64_t>(L, (k + 1) * W);
+        wstart.push_back((uint32_t)st);
+        wlen.push_back((uint32_t)(en - st));
+        woff.push_back(off[e] + st);
+      }
+    }
+    const uint32_t nw = (uint32_t)wstart.size();
+    cs[nonempty] = nw;
+    // the view: slots ordered longest first (pairs of similar length)
+    std::vector<uint32_t> order(nw);
+    std::iota(order.begin(), order.end(), 0u);
+    std::stable_sort(order.begin(), order.end(), [&](uint32_t a, uint32_t b) { return wlen[a] > wlen[b]; });
+    std::vector<uint32_t> vlen(nw), vslot(nw);
+    std::vector<uint64_t> voff(nw);
+    uint64_t vtotal = 0;
+    for (uint32_t i = 0; i < nw; ++i) {
+      vlen[i] = wlen[order[i]];
+      voff[i] = woff[order[i]];
+      vslot[i] = order[i];
+      vtotal += vlen[i];
+    }
+    CU(V.off.ensure((size_t)nw * 8));
+    CU(V.len.ensure((size_t)nw * 4));
+    CU(V.slot.ensure((size_t)nw * 4));
+    CU(V.start.ensure((size_t)nw * 4));
+    CU(V.cs.ensure((size_t)(nonempty + 1) * 4));
+    CU(cudaMemcpy(V.off.p, voff.data(), (size_t)nw * 8, cudaMemcpyHostToDevice));
+    CU(cudaMemcpy(V.len.p, vlen.data(), (size_t)nw * 4, cudaMemcpyHostToDevice));
+    CU(cudaMemcpy(V.slot.p, vslot.data(), (size_t)nw * 4, cudaMemcpyHostToDevice));
+    CU(cudaMemcpy(V.start.p, wstart.data(), (size_t)nw * 4, cudaMemcpyHostToDevice));
+    CU(cudaMemcpy(V.cs.p, cs.data(), (size_t)(nonempty + 1) * 4, cudaMemcpyHostToDevice));
+    V.W = W;
+    V.O = O;
+    V.entries = nonempty;
+    V.nw = nw;
+    V.total = vtotal;
+    V.max_len = vlen[0];
+  }
+  const uint32_t nw = V.nw;
+  WindowOut &R = ctx->window_out;
+  CU(R.score.ensure((size_t)nw * 4));
+  CU(R.qend.ensure((size_t)nw * 4));
+  CU(R.tend.ensure((size_t)nw * 4));
+  CU(R.hit.ensure((size_t)nw));
+
+  // a record set over the same codes whose entries are the windows (the
+  // buffers are borrowed: `view` is never released)
+  RecordSet view;
+  view.n = nw;
+  view.total = V.total;
+  view.max_len = V.max_len;
+  view.codes = rs.codes;
+  view.off_s = V.off;
+  view.len_s = V.len;
+  view.orig_s = V.slot;
+  OutDev wout{R.score.as<int32_t>(), R.qend.as<int32_t>(), R.tend.as<int32_t>(), R.hit.as<uint8_t>()};
+  int rc = launch_wave_range(ctx, q, view, 0, nw, wout, G, K, layout, s);
+  if (rc) return rc;
+  const uint32_t nb = std::max<uint32_t>(1, std::min<uint32_t>(ceil_div(nonempty, 256), (uint32_t)ctx->num_sms * 8));
+  k_merge_windows<<<nb, 256, 0, s>>>(rs.orig_s.as<const uint32_t>(), nonempty, V.cs.as<const uint32_t>(),
+                                     V.start.as<const uint32_t>(), R.score.as<const int32_t>(),
+                                     R.qend.as<const int32_t>(), R.tend.as<const int32_t>(), mode, out,
+                                     Decision{q.max_score, q.thr});
+  ++ctx->launches;
+  CU(cudaGetLastError());
+  ctx->last_windows = nw;
+  *done = true;
+  return ISH_OK;
+}
+
+}  // namespace host
+}  // namespace ish

@@ -20,6 +20,7 @@ OPT_KERNEL, OPT_SG_LANES, OPT_SW_U8_LANES, OPT_SW_U16_LANES, OPT_WAVE_GROUP, OPT
 OPT_PROFILE_LAYOUT = 7
 OPT_WAVE_BLOCKS = 8
 OPT_WAVE_LEAN = 9
+OPT_WINDOWS = 10
 PROF_AUTO, PROF_S16, PROF_PAIR, PROF_S32 = -1, 0, 1, 2
 
 # Entry points declared in include/ish_gpu.h (checked by the tests).
@@ -29,7 +30,7 @@ EXPORTS = (
     "ish_gpu_records_info", "ish_gpu_score_set", "ish_gpu_last_kernel_ms", "ish_gpu_calibrate",
     "ish_gpu_score_noalloc", "ish_gpu_score_multi", "ish_gpu_autotune", "ish_gpu_serve_start", "ish_gpu_submit",
     "ish_gpu_poll", "ish_gpu_serve_stop", "ish_gpu_serve_stats", "ish_gpu_match_starts",
-    "ish_gpu_launch_count", "ish_gpu_records_load_raw", "ish_gpu_records_load_lines",
+    "ish_gpu_launch_count", "ish_gpu_records_load_raw", "ish_gpu_records_load_lines", "ish_gpu_last_windows",
 )
 
 
@@ -91,6 +92,7 @@ def load(build_if_missing: bool = False):
     L.ish_gpu_score_multi.argtypes = [vp, i32p, C.c_uint32, C.c_int32, i32p, i32p, i32p, u8p, u32p, C.c_uint64, u64p]
     L.ish_gpu_autotune.argtypes = [vp, C.c_int32, i32p, C.c_uint32, i32p, i32p]
     L.ish_gpu_launch_count.argtypes = [vp, u64p]
+    L.ish_gpu_last_windows.argtypes = [vp, C.POINTER(C.c_uint32)]
     L.ish_gpu_records_load_raw.argtypes = [vp, u8p, u64p, C.c_uint32, C.c_int, i32p]
     L.ish_gpu_records_load_lines.argtypes = [vp, u8p, C.c_uint64, C.c_int, i32p, u32p]
     L.ish_gpu_match_starts.argtypes = [vp, C.c_int32, C.c_int32, u32p, i32p, C.c_uint32, C.POINTER(C.c_int64)]
@@ -356,6 +358,12 @@ class Context:
         c = C.c_uint64()
         self._check(self._L.ish_gpu_launch_count(self._h, C.byref(c)))
         return c.value
+
+    def last_windows(self) -> int:
+        """Windows the last single-query scoring call cut long records into (0: none)."""
+        w = C.c_uint32()
+        self._check(self._L.ish_gpu_last_windows(self._h, C.byref(w)))
+        return w.value
 
     def last_kernel_ms(self) -> float:
         ms = C.c_double()
