@@ -139,6 +139,16 @@ int wave_lean(const ish_ctx *ctx, int K, int mode) {
   return lean[mode == SW][i];
 }
 
+// The same choice for the batched kernel (parameters in shared memory, one
+// more live pointer), measured the same way through ish_gpu_score_multi: the
+// 128 x 3 build wins everywhere but local alignment at K = 36 (+2.0 %) and
+// K = 48 (+6.7 %); the lean build loses 12-17 % from K = 38 on.
+int batch_lean(const ish_ctx *ctx, int K, int mode) {
+  if (K < WAVE_LEAN_KMIN || K > WAVE_LEAN_KMAX) return 0;
+  if (ctx->force_lean >= 0) return ctx->force_lean;
+  return mode == SW && (K == 36 || K == 48);
+}
+
 int frame_rows(int ext) {
   int R = 1;
   while (R < (1 << 20) && (long)2 * R * std::max(ext, 1) <= 2048) R *= 2;
@@ -1093,7 +1103,7 @@ int ish_gpu_score(ish_ctx *ctx, int32_t query_id, const uint8_t *records, const 
   if (!rc) rc = run_scoring(ctx, qi->second, rs);
   if (!rc) rc = fetch_outputs(ctx, n, score, query_end, target_end, hit, hit_idx, n_hits);
   cudaStreamSynchronize(ctx->stream);
-  release_set(rs);
+  recycle_set(ctx, rs);  // the next call's set takes these buffers
   return rc;
 }
 

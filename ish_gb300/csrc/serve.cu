@@ -290,7 +290,7 @@ int step(Server &S, char *msg) {
     }
     for (size_t c = 0; c < cls.size(); ++c) {
       const Cls &C = cls[c];
-      BatchFn fn = batch_fn(C.K, C.mode, C.layout, wave_lean(S.ctx, C.K, C.mode));
+      BatchFn fn = batch_fn(C.K, C.mode, C.layout, batch_lean(S.ctx, C.K, C.mode));
       if (!fn) {
         snprintf(msg, 256, "no batch kernel for K=%d", C.K);
         return ISH_EOVERFLOW;

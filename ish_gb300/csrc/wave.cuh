@@ -75,14 +75,18 @@ __device__ __forceinline__ void wave_rows(const WaveParams &p, const unsigned ch
   const uint32_t EOPEN = dup16(p.ext - p.open);                   // E' = max(T + ext - open, E)
   const uint32_t NEGMIN = dup16(-32768);
   const int f0 = (MODE == SG) ? p.ext : 0;  // row -1 sits in frame -ext
-  // the frame of a row (always 0 for local alignment)
-  auto frame_of = [&](int r) { return (MODE == SG) ? (r & p.frame_mask) * p.ext : 0; };
   const bool te = (MODE == SG) && (p.ends & 8);
   const bool qe = (MODE == SG) && (p.ends & 2);
   const uint32_t npairs = (p.count + 1) >> 1;
   const uint16_t *prof16 = reinterpret_cast<const uint16_t *>(prof);
   const uint32_t *prof32 = reinterpret_cast<const uint32_t *>(prof);
   const int col0 = t * K - p.d;  // query column of register 0
+  // parameters read every row, held in registers (the batched kernel's
+  // parameters live in shared memory)
+  const int kp = p.kp, alpha = p.alphabet, fmask = p.frame_mask, ext = p.ext, hleft = p.hleft;
+  const uint32_t remap_off = p.remap_off, lane_mul = p.lane_mul;
+  // the frame of a row (always 0 for local alignment)
+  auto frame_of = [&](int r) { return (MODE == SG) ? (r & fmask) * ext : 0; };
 
   uint32_t H[K], E[K];
 #pragma unroll
@@ -110,7 +114,7 @@ __device__ __forceinline__ void wave_rows(const WaveParams &p, const unsigned ch
   uint32_t f_seq = 31;
   // the next row at which one of this thread's records ends (-3: none)
   int ev_row = -3;
-  const bool remap = p.remap_off != 0;
+  const bool remap = remap_off != 0;
   uint64_t steps = 0;
   int chk = 8;
 
@@ -176,7 +180,7 @@ __device__ __forceinline__ void wave_rows(const WaveParams &p, const unsigned ch
       } else {
         ++row;
         if (MODE == SG) {
-          if ((row & p.frame_mask) == 0) {
+          if ((row & fmask) == 0) {
             // frame R*ext -> 0: lower what this row takes from the row above
             const uint32_t FRAME_DROP = dup16(-(p.frame_mask + 1) * p.ext);
 #pragma unroll
@@ -210,13 +214,13 @@ __device__ __forceinline__ void wave_rows(const WaveParams &p, const unsigned ch
         }
         uint32_t cA = wA & 0xffu, cB = wB & 0xffu;
         if (remap) {  // codes that score alike share a profile row
-          cA = prof[p.remap_off + cA];
-          cB = prof[p.remap_off + cB];
+          cA = prof[remap_off + cA];
+          cB = prof[remap_off + cB];
         }
         wA >>= 8;
         wB >>= 8;
         if (LAYOUT == PROF_PAIR) {
-          const uint4 *r4 = reinterpret_cast<const uint4 *>(prof32 + ((cA * p.alphabet + cB) * G + t) * p.kp);
+          const uint4 *r4 = reinterpret_cast<const uint4 *>(prof32 + ((cA * alpha + cB) * G + t) * kp);
 #pragma unroll
           for (int v = 0; v < (K + 3) / 4; ++v) {
             const uint4 w = r4[v];
@@ -230,9 +234,9 @@ __device__ __forceinline__ void wave_rows(const WaveParams &p, const unsigned ch
           // pair is b * 65536 + a, one integer multiply-add (the multiplier is
           // a runtime value, so this stays an IMAD on the FMA pipe, which the
           // DPX recurrence on the ALU pipe leaves idle)
-          const uint4 *ra = reinterpret_cast<const uint4 *>(prof32 + (cA * G + t) * p.kp);
-          const uint4 *rb = reinterpret_cast<const uint4 *>(prof32 + (cB * G + t) * p.kp);
-          const uint32_t mul = p.lane_mul;
+          const uint4 *ra = reinterpret_cast<const uint4 *>(prof32 + (cA * G + t) * kp);
+          const uint4 *rb = reinterpret_cast<const uint4 *>(prof32 + (cB * G + t) * kp);
+          const uint32_t mul = lane_mul;
 #pragma unroll
           for (int v = 0; v < (K + 3) / 4; ++v) {
             const uint4 a = ra[v], b = rb[v];
@@ -244,8 +248,8 @@ __device__ __forceinline__ void wave_rows(const WaveParams &p, const unsigned ch
         } else {
           // 16-bit words (profiles too large for the 32-bit layout): one PRMT
           // per packed pair
-          const uint4 *ra = reinterpret_cast<const uint4 *>(prof16 + (cA * G + t) * p.kp);
-          const uint4 *rb = reinterpret_cast<const uint4 *>(prof16 + (cB * G + t) * p.kp);
+          const uint4 *ra = reinterpret_cast<const uint4 *>(prof16 + (cA * G + t) * kp);
+          const uint4 *rb = reinterpret_cast<const uint4 *>(prof16 + (cB * G + t) * kp);
 #pragma unroll
           for (int v = 0; v < (K + 7) / 8; ++v) {
             const uint4 a = ra[v], b = rb[v];
@@ -278,7 +282,7 @@ __device__ __forceinline__ void wave_rows(const WaveParams &p, const unsigned ch
         H[j] = __viaddmax_s16x2(Fs, NOPEN, T);
         Fs = __viaddmax_s16x2(Fs, NEXT, T);
       }
-      prevH = (t == 0) ? dup16(p.hleft + frame_of(row)) : msgH;  // this row's H left of column 0
+      prevH = (t == 0) ? dup16(hleft + frame_of(row)) : msgH;  // this row's H left of column 0
       outH = H[K - 1];
       outF = Fs;
       outC = msgC;
