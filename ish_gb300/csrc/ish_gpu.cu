@@ -131,8 +131,9 @@ int matrix_alphabet_ok(uint32_t alphabet) { return alphabet >= 1 && alphabet <= 
 // for K = 34..44 and -11 to -14 % at 46/48; local +0.3 to +7.4 % at
 // 34..38 and 46/48, -6 to -12 % at 40..44.
 int wave_lean(const ish_ctx *ctx, int K, int mode) {
-  if (K < WAVE_LEAN_KMIN || K > WAVE_LEAN_KMAX) return 0;
+  if (!wave_has_lean(K)) return 0;
   if (ctx->force_lean >= 0) return ctx->force_lean;
+  if (K <= 32) return 0;
   const int i = (K - WAVE_LEAN_KMIN) / 2;  //             K = 34 36 38 40 42 44 46 48
   static const unsigned char lean[2][8] = {/* semi-global */ {1, 1, 1, 1, 1, 1, 0, 0},
                                            /* local */ {1, 1, 1, 0, 0, 0, 1, 1}};
@@ -144,8 +145,9 @@ int wave_lean(const ish_ctx *ctx, int K, int mode) {
 // 128 x 3 build wins everywhere but local alignment at K = 36 (+2.0 %) and
 // K = 48 (+6.7 %); the lean build loses 12-17 % from K = 38 on.
 int batch_lean(const ish_ctx *ctx, int K, int mode) {
-  if (K < WAVE_LEAN_KMIN || K > WAVE_LEAN_KMAX) return 0;
+  if (!wave_has_lean(K)) return 0;
   if (ctx->force_lean >= 0) return ctx->force_lean;
+  if (K <= 32) return 0;
   return mode == SW && (K == 36 || K == 48);
 }
 
@@ -615,9 +617,10 @@ int launch_wave_range(ish_ctx *ctx, Query &q, RecordSet &rs, uint32_t first, uin
   int rc = build_wave_layout(ctx, q, G, K, layout, &L);
   if (rc) return rc;
   const int mode = q.algo == ISH_ALGO_LOCAL ? SW : SG;
-  WaveFn fn = wave_fn(K, mode, L->layout, wave_lean(ctx, K, mode));
+  const int lean = wave_lean(ctx, K, mode);
+  WaveFn fn = wave_fn(K, mode, L->layout, lean);
   if (!fn) return fail(ctx, ISH_EOVERFLOW, "no wavefront kernel for K=%d", K);
-  const int threads = wave_block_threads(K, mode);
+  const int threads = wave_threads_lean(K, mode, lean);
   const int groups = threads / G;
   const size_t smem = wave_smem((L->prof_bytes + 15) & ~15u, threads, G, K, mode);
   {
@@ -1157,9 +1160,11 @@ WaveFn wave_fn_e(int, int, int);
 WaveFn wave_fn_f(int, int, int);
 WaveFn wave_fn_g(int, int, int);
 BatchFn batch_fn_g(int, int, int);
+WaveFn wave_fn_h(int, int, int);
+BatchFn batch_fn_h(int, int, int);
 WaveFn wave_fn(int K, int mode, int layout, int lean) {
   if (K < 1) return nullptr;
-  if (lean && K >= WAVE_LEAN_KMIN && K <= WAVE_LEAN_KMAX) return wave_fn_g(K, mode, layout);
+  if (lean && wave_has_lean(K)) return K <= 32 ? wave_fn_h(K, mode, layout) : wave_fn_g(K, mode, layout);
   if (K <= 8) return wave_fn_a(K, mode, layout);
   if (K <= 16) return wave_fn_b(K, mode, layout);
   if (K <= 24) return wave_fn_c(K, mode, layout);
@@ -1175,7 +1180,7 @@ BatchFn batch_fn_e(int, int, int);
 BatchFn batch_fn_f(int, int, int);
 BatchFn batch_fn(int K, int mode, int layout, int lean) {
   if (K < 1) return nullptr;
-  if (lean && K >= WAVE_LEAN_KMIN && K <= WAVE_LEAN_KMAX) return batch_fn_g(K, mode, layout);
+  if (lean && wave_has_lean(K)) return K <= 32 ? batch_fn_h(K, mode, layout) : batch_fn_g(K, mode, layout);
   if (K <= 8) return batch_fn_a(K, mode, layout);
   if (K <= 16) return batch_fn_b(K, mode, layout);
   if (K <= 24) return batch_fn_c(K, mode, layout);

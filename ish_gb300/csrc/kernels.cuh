@@ -48,13 +48,24 @@ __host__ __device__ constexpr int wave_block_threads(int K, int mode) {
 __host__ __device__ constexpr int wave_blocks_per_sm(int K, int mode) {
   return K <= 32 ? 2 : (K <= 48 ? 3 : (mode == 1 ? 1 : 2));
 }
-// The lean variant of 32 < K <= 48 runs 128 x 2 instead of 128 x 3: 8 warps
-// per SM with up to 255 registers per thread instead of 12 with 168, which is
-// faster for some (K, mode) -- spills against warps (wave_lean_default).
-constexpr int WAVE_LEAN_KMIN = 34, WAVE_LEAN_KMAX = 48;
-__host__ __device__ constexpr int wave_blocks_lean(int K, int mode, int lean) {
-  return (lean && K >= WAVE_LEAN_KMIN && K <= WAVE_LEAN_KMAX) ? 2 : wave_blocks_per_sm(K, mode);
+// Register-lean builds trade warps for registers per thread: for
+// 25 <= K <= 32, 128 x 3 (12 warps, 170 registers) instead of 256 x 2 (16
+// warps, 128); for 34 <= K <= 48, 128 x 2 instead of 128 x 3 (168).  Which
+// build runs is chosen per (K, mode) from measurements (wave_lean, batch_lean).
+constexpr int WAVE_LEAN_KMIN = 25, WAVE_LEAN_KMAX = 48;
+__host__ __device__ constexpr bool wave_has_lean(int K) { return K >= WAVE_LEAN_KMIN && K <= WAVE_LEAN_KMAX && K != 33; }
+__host__ __device__ constexpr int wave_threads_lean(int K, int mode, int lean) {
+  return (lean && wave_has_lean(K) && K <= 32) ? 128 : wave_block_threads(K, mode);
 }
+__host__ __device__ constexpr int wave_blocks_lean(int K, int mode, int lean) {
+  return (lean && wave_has_lean(K)) ? (K <= 32 ? 3 : 2) : wave_blocks_per_sm(K, mode);
+}
+// wave_kernel reads its parameters from a shared-memory copy for these
+// (K, mode, lean build) (see wave.cuh): semi-global at K = 9..32 gains 1 to
+// 12 % (protein, 400k records, G = 8, Q = 8K - 2; 7-9 % from K = 26 on).
+#ifndef WAVE_PARAMS_SMEM
+#define WAVE_PARAMS_SMEM(K, MODE, LEAN) ((MODE) == 0 && (K) >= 9 && (K) <= 32)
+#endif
 // Local alignment keeps, per thread, the H row of each lane's last
 // improvement as 16-bit values: two arrays of K (rounded up to 8) halves,
 // strided by an odd number of 16-byte units.

@@ -160,9 +160,10 @@ int build_plan(ish_ctx *ctx, const int32_t *qids, uint32_t nq, int32_t set_id, R
 
   // ---- per class: kernel, occupancy, parameters, tiles ----
   for (MultiClass &c : P.classes) {
-    c.fn = batch_fn(c.K, c.mode, c.layout, batch_lean(ctx, c.K, c.mode));
+    const int lean = batch_lean(ctx, c.K, c.mode);
+    c.fn = batch_fn(c.K, c.mode, c.layout, lean);
     if (!c.fn) return fail(ctx, ISH_EOVERFLOW, "no batch kernel for K=%d", c.K);
-    c.threads = wave_block_threads(c.K, c.mode);
+    c.threads = wave_threads_lean(c.K, c.mode, lean);
     const size_t slot_words = (size_t)(c.threads / c.Gmin) * 32;
     const size_t save = c.mode == SW ? (size_t)c.threads * wave_save_words(c.K) * 4 : 0;
     c.smem = c.prof_area + slot_words * 4 + save;

@@ -290,12 +290,13 @@ int step(Server &S, char *msg) {
     }
     for (size_t c = 0; c < cls.size(); ++c) {
       const Cls &C = cls[c];
-      BatchFn fn = batch_fn(C.K, C.mode, C.layout, batch_lean(S.ctx, C.K, C.mode));
+      const int lean = batch_lean(S.ctx, C.K, C.mode);
+      BatchFn fn = batch_fn(C.K, C.mode, C.layout, lean);
       if (!fn) {
         snprintf(msg, 256, "no batch kernel for K=%d", C.K);
         return ISH_EOVERFLOW;
       }
-      const int threads = wave_block_threads(C.K, C.mode);
+      const int threads = wave_threads_lean(C.K, C.mode, lean);
       const size_t slot_words = (size_t)(threads / C.Gmin) * 32;
       const size_t save = C.mode == SW ? (size_t)threads * wave_save_words(C.K) * 4 : 0;
       const size_t smem = C.prof_area + slot_words * 4 + save;

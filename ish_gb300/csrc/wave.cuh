@@ -504,7 +504,7 @@ __device__ __forceinline__ void wave_rows(const WaveParams &p, const unsigned ch
 // Shared memory of a block: the profile, then 32 slot words per group, then
 // (local alignment) wave_save_words(K) save words per thread.
 template <int K, int MODE, int LAYOUT, int LEAN = 0>
-__global__ void __launch_bounds__(wave_block_threads(K, MODE), wave_blocks_lean(K, MODE, LEAN))
+__global__ void __launch_bounds__(wave_threads_lean(K, MODE, LEAN), wave_blocks_lean(K, MODE, LEAN))
     wave_kernel(const __grid_constant__ WaveParams p) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   {
@@ -515,8 +515,19 @@ __global__ void __launch_bounds__(wave_block_threads(K, MODE), wave_blocks_lean(
   }
   uint32_t *slots_all = reinterpret_cast<uint32_t *>(smem_raw + ((p.prof_bytes + 15u) & ~15u));
   uint32_t *save_all = slots_all + (blockDim.x / p.G) * 32;
-  __syncthreads();
-  wave_rows<K, MODE, LAYOUT>(p, smem_raw, slots_all, save_all, p.counter);
+  if (WAVE_PARAMS_SMEM(K, MODE, LEAN)) {
+    // narrow rows: read the parameters from a shared-memory copy, as the
+    // batched kernel does -- kept in the parameter bank, the compiler holds
+    // them in registers across the row loop and the 128-register budget of
+    // 16 warps per SM spills
+    __shared__ WaveParams sp;
+    if (threadIdx.x == 0) sp = p;
+    __syncthreads();
+    wave_rows<K, MODE, LAYOUT>(sp, smem_raw, slots_all, save_all, p.counter);
+  } else {
+    __syncthreads();
+    wave_rows<K, MODE, LAYOUT>(p, smem_raw, slots_all, save_all, p.counter);
+  }
 }
 
 // The batched launch: one persistent kernel for every query of a shape class
@@ -528,7 +539,7 @@ __global__ void __launch_bounds__(wave_block_threads(K, MODE), wave_blocks_lean(
 // a profile reload happen only at a query switch, where the pairs left are the
 // shortest of the set.  Queries whose counter is already exhausted are skipped.
 template <int K, int MODE, int LAYOUT, int LEAN = 0>
-__global__ void __launch_bounds__(wave_block_threads(K, MODE), wave_blocks_lean(K, MODE, LEAN))
+__global__ void __launch_bounds__(wave_threads_lean(K, MODE, LEAN), wave_blocks_lean(K, MODE, LEAN))
     batch_kernel(const __grid_constant__ BatchParams b) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   __shared__ WaveParams sp;

@@ -96,8 +96,9 @@ int launch_windows(ish_ctx *ctx, Query &q, RecordSet &rs, uint32_t nonempty, Out
   if (!G || !wave_fits(q, G, K, layout)) return ISH_OK;
   // groups in flight and the rows each would score on average (two records
   // per pair share their rows)
-  const uint64_t groups = (uint64_t)ctx->num_sms * wave_blocks_lean(K, mode, wave_lean(ctx, K, mode)) *
-                          (wave_block_threads(K, mode) / G);
+  const int lean = wave_lean(ctx, K, mode);
+  const uint64_t groups =
+      (uint64_t)ctx->num_sms * wave_blocks_lean(K, mode, lean) * (wave_threads_lean(K, mode, lean) / G);
   const uint64_t avg_rows = rs.total / 2 / std::max<uint64_t>(groups, 1);
   // window stride: about four pairs of windows per group, and at least 8x
   // the overlap so that windowing adds at most an eighth of the work

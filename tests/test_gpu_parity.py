@@ -152,6 +152,40 @@ def test_wide_rows_interleaved_schedule(ctx, G, K):
         ctx.set_option(native.OPT_WAVE_K, 0)
 
 
+@pytest.mark.parametrize("K", [25, 28, 32, 34, 38, 44, 48])
+def test_register_lean_builds(ctx, K):
+    # both builds of a K (the register-lean one with fewer warps per SM, and
+    # the default), single and batched launches, give the oracle's results
+    rng = np.random.default_rng(23 + K)
+    G = 4
+    q = rng.integers(0, 20, G * K - 3, dtype=np.uint8)
+    recs = random_records(rng, 20, 120, 0, 2 * len(q) + 30, q)
+    ctx.set_option(native.OPT_WAVE_GROUP, G)
+    ctx.set_option(native.OPT_WAVE_K, K)
+    try:
+        for lean in (0, 1):
+            ctx.set_option(native.OPT_WAVE_LEAN, lean)
+            for algo, ends in ((native.ALGO_SEMI_GLOBAL, 12), (native.ALGO_SEMI_GLOBAL, 15), (native.ALGO_LOCAL, 0)):
+                g, o = run_both(ctx, algo, O.BLOSUM62, q, recs, 10, 1, ends)
+                assert_same(g, o, f"K={K} lean={lean} algo={algo} ends={ends}")
+            m = ScoringMatrix(O.BLOSUM62)
+            buf, off = native.pack_records(recs)
+            sid = ctx.records_load(buf, off)
+            qid = ctx.set_query(q, O.BLOSUM62, m.values, native.ALGO_LOCAL, 10, 1, 0, int(m.values[q, q].sum()), 0.5)
+            try:
+                single = ctx.score_set(qid, sid)
+                batched = ctx.score_multi([qid], sid)
+                for k in ("score", "qend", "tend"):
+                    assert np.array_equal(single[k], batched[k][0]), f"K={K} lean={lean} batched {k}"
+            finally:
+                ctx.free_query(qid)
+                ctx.records_free(sid)
+    finally:
+        ctx.set_option(native.OPT_WAVE_LEAN, -1)
+        ctx.set_option(native.OPT_WAVE_GROUP, 0)
+        ctx.set_option(native.OPT_WAVE_K, 0)
+
+
 @pytest.mark.parametrize("algo", [native.ALGO_SEMI_GLOBAL, native.ALGO_LOCAL])
 def test_plain_kernel_parity(ctx, algo):
     rng = np.random.default_rng(13)
