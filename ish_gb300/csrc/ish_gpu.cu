@@ -126,17 +126,18 @@ int matrix_alphabet_ok(uint32_t alphabet) { return alphabet >= 1 && alphabet <= 
 // to 0 every R rows, R a power of two with R * ext <= 2048 (the headroom the
 // regime keeps above the largest score).
 // Whether (K, mode) runs the lean kernel variant (128 x 2 blocks with more
-// registers instead of 128 x 3), as measured on GB300 for the protein search
-// (blosum62, 400k records, G = 8, Q = 8K - 2): semi-global +2.5 to +13.6 %
-// for K = 34..44 and -11 to -14 % at 46/48; local +0.3 to +7.4 % at
-// 34..38 and 46/48, -6 to -12 % at 40..44.
+// registers instead of 128 x 3, whose parameters come from shared memory),
+// as measured on GB300 for the protein search (blosum62, 400k records,
+// G = 8, Q = 8K - 2): lean is ahead for semi-global at K = 34..40 (+0.5 to
+// +5.7 %) and local at 34..38 (+1.3 to +2.4 %), behind from there on (up to
+// -15 %).
 int wave_lean(const ish_ctx *ctx, int K, int mode) {
   if (!wave_has_lean(K)) return 0;
   if (ctx->force_lean >= 0) return ctx->force_lean;
   if (K <= 32) return 0;
   const int i = (K - WAVE_LEAN_KMIN) / 2;  //             K = 34 36 38 40 42 44 46 48
-  static const unsigned char lean[2][8] = {/* semi-global */ {1, 1, 1, 1, 1, 1, 0, 0},
-                                           /* local */ {1, 1, 1, 0, 0, 0, 1, 1}};
+  static const unsigned char lean[2][8] = {/* semi-global */ {1, 1, 1, 1, 0, 0, 0, 0},
+                                           /* local */ {1, 1, 1, 0, 0, 0, 0, 0}};
   return lean[mode == SW][i];
 }
 

@@ -61,10 +61,15 @@ __host__ __device__ constexpr int wave_blocks_lean(int K, int mode, int lean) {
   return (lean && wave_has_lean(K)) ? (K <= 32 ? 3 : 2) : wave_blocks_per_sm(K, mode);
 }
 // wave_kernel reads its parameters from a shared-memory copy for these
-// (K, mode, lean build) (see wave.cuh): semi-global at K = 9..32 gains 1 to
-// 12 % (protein, 400k records, G = 8, Q = 8K - 2; 7-9 % from K = 26 on).
+// (K, mode, lean build) (see wave.cuh).  Measured on the protein search
+// (400k records, G = 8, Q = 8K - 2): semi-global at K = 9..32 +1 to +12 %;
+// local at K = 12..32 mostly +1.4 to +9.7 %; the 128 x 3 builds of K = 34..48
+// +5 to +10 % (semi-global), -1 to +10 % (local).  The register-lean builds
+// of K >= 34 keep the parameter bank.
 #ifndef WAVE_PARAMS_SMEM
-#define WAVE_PARAMS_SMEM(K, MODE, LEAN) ((MODE) == 0 && (K) >= 9 && (K) <= 32)
+#define WAVE_PARAMS_SMEM(K, MODE, LEAN)                                              \
+  (((MODE) == 0 && (K) >= 9 && (K) <= 32) || ((MODE) == 1 && (K) >= 12 && (K) <= 32) || \
+   (!(LEAN) && (K) >= 34 && (K) <= 48))
 #endif
 // Local alignment keeps, per thread, the H row of each lane's last
 // improvement as 16-bit values: two arrays of K (rounded up to 8) halves,
