@@ -64,12 +64,13 @@ __host__ __device__ constexpr int wave_blocks_lean(int K, int mode, int lean) {
 // (K, mode, lean build) (see wave.cuh).  Measured on the protein search
 // (400k records, G = 8, Q = 8K - 2): semi-global at K = 9..32 +1 to +12 %;
 // local at K = 12..32 mostly +1.4 to +9.7 %; the 128 x 3 builds of K = 34..48
-// +5 to +10 % (semi-global), -1 to +10 % (local).  The register-lean builds
-// of K >= 34 keep the parameter bank.
+// +5 to +10 % (semi-global), -1 to +10 % (local); K = 58..64 +1.5 to +6.6 %
+// and local K = 50 +3 % (K = 52..56: -2.6 to +0.2 %).  The register-lean
+// builds of K >= 34 keep the parameter bank.
 #ifndef WAVE_PARAMS_SMEM
 #define WAVE_PARAMS_SMEM(K, MODE, LEAN)                                              \
   (((MODE) == 0 && (K) >= 9 && (K) <= 32) || ((MODE) == 1 && (K) >= 12 && (K) <= 32) || \
-   (!(LEAN) && (K) >= 34 && (K) <= 48))
+   (!(LEAN) && (K) >= 34 && (K) <= 48) || (K) >= 58 || ((MODE) == 1 && (K) == 50))
 #endif
 // Local alignment keeps, per thread, the H row of each lane's last
 // improvement as 16-bit values: two arrays of K (rounded up to 8) halves,
