@@ -135,7 +135,8 @@ int wave_lean(const ish_ctx *ctx, int K, int mode) {
   if (!wave_has_lean(K)) return 0;
   if (ctx->force_lean >= 0) return ctx->force_lean;
   if (K <= 32) return 0;
-  const int i = (K - WAVE_LEAN_KMIN) / 2;  //             K = 34 36 38 40 42 44 46 48
+  const int i = (K - 34) / 2;  //                         K = 34 36 38 40 42 44 46 48
+  if (i < 0 || i >= 8) return 0;
   static const unsigned char lean[2][8] = {/* semi-global */ {1, 1, 1, 1, 0, 0, 0, 0},
                                            /* local */ {1, 1, 1, 0, 0, 0, 0, 0}};
   return lean[mode == SW][i];

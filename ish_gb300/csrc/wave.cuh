@@ -501,6 +501,19 @@ __device__ __forceinline__ void wave_rows(const WaveParams &p, const unsigned ch
   }
 }
 
+// Rows with the parameters read from a shared-memory copy, as the batched
+// kernel does: kept in the parameter bank, the compiler holds them in
+// registers across the row loop, which some shapes pay for in spills
+// (WAVE_PARAMS_SMEM).  Only the kernels that call this declare the copy.
+template <int K, int MODE, int LAYOUT>
+__device__ __forceinline__ void wave_rows_smem_params(const WaveParams &p, const unsigned char *prof,
+                                                      uint32_t *slots_all, uint32_t *save_all) {
+  __shared__ WaveParams sp;
+  if (threadIdx.x == 0) sp = p;
+  __syncthreads();
+  wave_rows<K, MODE, LAYOUT>(sp, prof, slots_all, save_all, p.counter);
+}
+
 // Shared memory of a block: the profile, then 32 slot words per group, then
 // (local alignment) wave_save_words(K) save words per thread.
 template <int K, int MODE, int LAYOUT, int LEAN = 0>
@@ -515,15 +528,8 @@ __global__ void __launch_bounds__(wave_threads_lean(K, MODE, LEAN), wave_blocks_
   }
   uint32_t *slots_all = reinterpret_cast<uint32_t *>(smem_raw + ((p.prof_bytes + 15u) & ~15u));
   uint32_t *save_all = slots_all + (blockDim.x / p.G) * 32;
-  if (WAVE_PARAMS_SMEM(K, MODE, LEAN)) {
-    // narrow rows: read the parameters from a shared-memory copy, as the
-    // batched kernel does -- kept in the parameter bank, the compiler holds
-    // them in registers across the row loop and the 128-register budget of
-    // 16 warps per SM spills
-    __shared__ WaveParams sp;
-    if (threadIdx.x == 0) sp = p;
-    __syncthreads();
-    wave_rows<K, MODE, LAYOUT>(sp, smem_raw, slots_all, save_all, p.counter);
+  if constexpr (WAVE_PARAMS_SMEM(K, MODE, LEAN)) {
+    wave_rows_smem_params<K, MODE, LAYOUT>(p, smem_raw, slots_all, save_all);
   } else {
     __syncthreads();
     wave_rows<K, MODE, LAYOUT>(p, smem_raw, slots_all, save_all, p.counter);
