@@ -417,9 +417,16 @@ def _pinned(wl):
     try:
         import torch
 
-        pin = torch.empty(len(wl.records), dtype=torch.uint8, pin_memory=True).numpy()
-        pin_off = torch.empty(len(wl.offsets), dtype=torch.int64, pin_memory=True).numpy().view(np.uint64)
-    except Exception:
+        t_rec = torch.empty(len(wl.records), dtype=torch.uint8, pin_memory=True)
+        t_off = torch.empty(len(wl.offsets), dtype=torch.int64, pin_memory=True)
+        if not (t_rec.is_pinned() and t_off.is_pinned()):
+            raise RuntimeError("torch returned unpinned host memory")
+        pin = t_rec.numpy()
+        pin_off = t_off.numpy().view(np.uint64)
+        _pinned.ok = True
+    except Exception as e:
+        print(f"bench: pinned host buffers unavailable ({e}); end-to-end copies are pageable", file=sys.stderr)
+        _pinned.ok = False
         pin = np.empty(len(wl.records), np.uint8)
         pin_off = np.empty(len(wl.offsets), np.uint64)
     pin[:] = wl.records
@@ -540,21 +547,30 @@ def run_workload(args):
     # end to end from pinned host memory: upload + pack + score + results
     pin, pin_off = _pinned(wl)
     e2e = []
+    phases = []
     nh = 0
     for s in range(args.warmup + args.steps):
         barrier(dist)
         t = time.perf_counter()
         sid3 = ctx.records_load(pin, pin_off)
+        t1 = time.perf_counter()
         if name == "batched":
             r = ctx.score_multi(qids, sid3, want=("hit_idx",))
             nh = sum(len(h) for h in r["hit_idx"])
         else:
             r = ctx.score_set(qids[0], sid3, want=("score", "qend", "tend", "hit_idx"))
             nh = len(r["hit_idx"])
+        t2 = time.perf_counter()
+        dev_ms = ctx.last_kernel_ms()
         ctx.records_free(sid3)
         if s >= args.warmup:
             e2e.append(1e3 * (time.perf_counter() - t))
+            phases.append((1e3 * (t1 - t), 1e3 * (t2 - t1), dev_ms, 1e3 * (time.perf_counter() - t2)))
     e2e_ms = reduce_max(dist, float(np.mean(e2e)))
+    ph = np.mean(np.array(phases), axis=0)
+    extra["e2e_phases_ms"] = {"load": round(float(ph[0]), 2), "score": round(float(ph[1]), 2),
+                              "score_device": round(float(ph[2]), 2), "free": round(float(ph[3]), 2),
+                              "pinned": bool(getattr(_pinned, "ok", False))}
     d2h = 4 * nh + (0 if name == "batched" else 12 * wl.n) + 8 * (len(qids) + 1)
     if name == "line":
         # from raw text, as a line runner holds a file: upload, split into

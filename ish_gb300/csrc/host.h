@@ -158,6 +158,7 @@ struct Tuned {
 struct ish_ctx {
   int device = 0;
   int num_sms = 0;
+  size_t mem_total = 0;  // device memory (bytes)
   cudaStream_t stream = nullptr;
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
   std::string err;

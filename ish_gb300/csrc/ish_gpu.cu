@@ -56,13 +56,16 @@ void release_set(RecordSet &rs) {
 }
 
 // Freed sets keep their device buffers for the next load: at most two sets,
-// each under 1 GiB of packed codes, so the cache stays small next to HBM.
-static constexpr size_t kSpareSets = 2, kSpareCodesMax = size_t(1) << 30;
+// each with packed codes under a sixteenth of device memory (at least 1 GiB),
+// so the cache stays small next to HBM; an allocation that fails gives the
+// cached buffers back first (pack_set).
+static constexpr size_t kSpareSets = 2;
+static size_t spare_codes_max(const ish_ctx *ctx) { return std::max<size_t>(size_t(1) << 30, ctx->mem_total / 16); }
 
 void recycle_set(ish_ctx *ctx, RecordSet &rs) {
   rs.inv.release();  // rebuilt on first use by the next set
   rs.windows.release();
-  if (!rs.codes.p || rs.codes.cap > kSpareCodesMax) {
+  if (!rs.codes.p || rs.codes.cap > spare_codes_max(ctx)) {
     release_set(rs);
     return;
   }
@@ -863,6 +866,11 @@ int ish_gpu_open(int device, ish_ctx **out) {
   if ((e = cudaSetDevice(device)) != cudaSuccess) return bail(e, "cudaSetDevice");
   if ((e = cudaDeviceGetAttribute(&ctx->num_sms, cudaDevAttrMultiProcessorCount, device)) != cudaSuccess)
     return bail(e, "cudaDeviceGetAttribute");
+  {
+    size_t free_b = 0, total_b = 0;
+    if (cudaMemGetInfo(&free_b, &total_b) == cudaSuccess) ctx->mem_total = total_b;
+    (void)cudaGetLastError();
+  }
   if ((e = cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking)) != cudaSuccess)
     return bail(e, "cudaStreamCreate");
   if ((e = cudaEventCreate(&ctx->ev0)) != cudaSuccess) return bail(e, "cudaEventCreate");
