@@ -152,6 +152,31 @@ def test_wide_rows_interleaved_schedule(ctx, G, K):
         ctx.set_option(native.OPT_WAVE_K, 0)
 
 
+@pytest.mark.parametrize("ext", [0, 1, 3, 200, 1000, 2048, 2049])
+def test_semi_global_row_frames(ctx, ext):
+    # semi-global rows are held in frames rising by ext per row and dropped
+    # back every R rows (R * ext <= 2048): R = 2048 at ext 1, 8 at ext 200,
+    # 2 at ext 1000, 1 at ext 2048 (a drop every row); ext 0 never moves the
+    # frame; ext 2049 leaves the fast regime (exact kernels).  Records run
+    # through many drops, every end rule, several group shapes.
+    rng = np.random.default_rng(29 + ext)
+    gap_open = ext + 7
+    # query lengths that keep the fast regime's headroom check (about
+    # 2 * open + ext * (padded Q + 3) <= 30000) so the frames are what runs
+    shapes = {1000: ((12, 0), (20, 0)), 2048: ((5, 0), (8, 0))}.get(ext, ((40, 0), (40, 4), (120, 0)))
+    for qlen, G in shapes:
+        q = rng.integers(0, 20, qlen, dtype=np.uint8)
+        recs = random_records(rng, 20, 60, 0, 700, q, plant_frac=0.4, sub=0.05)
+        if G:
+            ctx.set_option(native.OPT_WAVE_GROUP, G)
+        try:
+            for ends in ALL_ENDS:
+                g, o = run_both(ctx, native.ALGO_SEMI_GLOBAL, O.BLOSUM62, q, recs, gap_open, ext, ends, thr=0.2)
+                assert_same(g, o, f"ext={ext} Q={qlen} G={G} ends={ends}")
+        finally:
+            ctx.set_option(native.OPT_WAVE_GROUP, 0)
+
+
 @pytest.mark.parametrize("K", [25, 28, 32, 34, 38, 44, 48])
 def test_register_lean_builds(ctx, K):
     # both builds of a K (the register-lean one with fewer warps per SM, and
