@@ -64,6 +64,7 @@ struct Query {
   bool plain_ready = false;
   std::map<long, WaveLayout> layouts;
   std::unique_ptr<Query> reverse;  // reversed query with swapped free ends (start finding)
+  std::unique_ptr<Query> fixed_start;  // the query with its start fixed (windows past row 0, windows.cu)
   std::map<long, DevBuf> exact_prof;  // striped profiles of the exact kernels (exact.cu)
 };
 
@@ -95,6 +96,7 @@ struct WindowView {
   uint64_t W = 0, O = 0;      // window stride and overlap (rows)
   uint32_t entries = 0;       // sorted entries covered
   uint32_t nw = 0;            // windows (slots)
+  uint32_t n_first = 0;       // view entries [0, n_first) start at record row 0, the rest later
   uint64_t total = 0;         // rows over all windows
   uint32_t max_len = 0;
   DevBuf off, len, slot;      // per view entry (longest first): code offset, rows, slot

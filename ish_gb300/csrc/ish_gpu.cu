@@ -47,6 +47,8 @@ void release_query(Query &q) {
   q.exact_prof.clear();
   if (q.reverse) release_query(*q.reverse);
   q.reverse.reset();
+  if (q.fixed_start) release_query(*q.fixed_start);
+  q.fixed_start.reset();
 }
 
 void release_set(RecordSet &rs) {

@@ -7,10 +7,15 @@
 // the best score is at least the full-query diagonal's Q * mmin (semi-global)
 // or positive (local).  So S <= O = Q + 1 + (Q * mmax - open - M_min) / ext.
 //
-// A window of a record that starts at row s >= 0 and runs the same
-// recurrence from the fresh boundary of row s scores every cell at most as
-// high as the whole record does (its paths are a subset), and exactly as
-// high at every cell whose best path starts inside the window.  Windows that
+// A window of a record that starts at row s runs the same recurrence from a
+// top boundary that only holds paths the whole record also has: for s = 0 the
+// query's own, for s > 0 the fixed-query-start one, H(s-1, j) = -(open +
+// ext*j) -- a start on the free left boundary at row s-1 followed by a query
+// gap.  (A free query start may begin a path at any query column on row 0
+// only; letting a later window begin one there would invent alignments.)  It
+// then scores every cell at most as high as the whole record does (its paths
+// are a subset), and exactly as high at every cell whose best path starts
+// inside the window.  Windows that
 // overlap by O rows therefore hold, for the record's best cell (the first
 // row, then the smallest column, of its maximum), that cell's exact value in
 // some window, and no cell before it reaches that value in any window.  The
@@ -65,6 +70,17 @@ __global__ void k_merge_windows(const uint32_t *orig_s, uint32_t n, const uint32
 }
 
 namespace host {
+
+// The query as windows past row 0 run it: its start fixed.
+static Query &fixed_start_of(Query &q) {
+  if (!(q.algo == ISH_ALGO_SEMI_GLOBAL && (q.ends & ISH_FREE_QUERY_START))) return q;
+  if (!q.fixed_start) {
+    q.fixed_start.reset(new Query());
+    clone_params(q, *q.fixed_start);
+    q.fixed_start->ends = q.ends & ~ISH_FREE_QUERY_START;
+  }
+  return *q.fixed_start;
+}
 
 // Rows two windows of a record must share (see above), or 0 when no bound
 // holds for this query.
@@ -137,10 +153,16 @@ int launch_windows(ish_ctx *ctx, Query &q, RecordSet &rs, uint32_t nonempty, Out
     }
     const uint32_t nw = (uint32_t)wstart.size();
     cs[nonempty] = nw;
-    // the view: slots ordered longest first (pairs of similar length)
+    // the view: windows that start at record row 0 first, then the others,
+    // each group longest first (pairs of similar length)
     std::vector<uint32_t> order(nw);
     std::iota(order.begin(), order.end(), 0u);
-    std::stable_sort(order.begin(), order.end(), [&](uint32_t a, uint32_t b) { return wlen[a] > wlen[b]; });
+    std::stable_sort(order.begin(), order.end(), [&](uint32_t a, uint32_t b) {
+      if ((wstart[a] == 0) != (wstart[b] == 0)) return wstart[a] == 0;
+      return wlen[a] > wlen[b];
+    });
+    uint32_t n_first = 0;
+    while (n_first < nw && wstart[order[n_first]] == 0) ++n_first;
     std::vector<uint32_t> vlen(nw), vslot(nw);
     std::vector<uint64_t> voff(nw);
     uint64_t vtotal = 0;
@@ -164,8 +186,9 @@ int launch_windows(ish_ctx *ctx, Query &q, RecordSet &rs, uint32_t nonempty, Out
     V.O = O;
     V.entries = nonempty;
     V.nw = nw;
+    V.n_first = n_first;
     V.total = vtotal;
-    V.max_len = vlen[0];
+    V.max_len = *std::max_element(vlen.begin(), vlen.end());
   }
   const uint32_t nw = V.nw;
   WindowOut &R = ctx->window_out;
@@ -185,7 +208,14 @@ int launch_windows(ish_ctx *ctx, Query &q, RecordSet &rs, uint32_t nonempty, Out
   view.len_s = V.len;
   view.orig_s = V.slot;
   OutDev wout{R.score.as<int32_t>(), R.qend.as<int32_t>(), R.tend.as<int32_t>(), R.hit.as<uint8_t>()};
-  int rc = launch_wave_range(ctx, q, view, 0, nw, wout, G, K, layout, s);
+  Query &qc = fixed_start_of(q);
+  int rc;
+  if (&qc == &q) {
+    rc = launch_wave_range(ctx, q, view, 0, nw, wout, G, K, layout, s);
+  } else {
+    rc = launch_wave_range(ctx, q, view, 0, V.n_first, wout, G, K, layout, s);
+    if (!rc && nw > V.n_first) rc = launch_wave_range(ctx, qc, view, V.n_first, nw - V.n_first, wout, G, K, layout, s);
+  }
   if (rc) return rc;
   const uint32_t nb = std::max<uint32_t>(1, std::min<uint32_t>(ceil_div(nonempty, 256), (uint32_t)ctx->num_sms * 8));
   k_merge_windows<<<nb, 256, 0, s>>>(rs.orig_s.as<const uint32_t>(), nonempty, V.cs.as<const uint32_t>(),

@@ -128,3 +128,20 @@ def test_no_windows_when_the_span_is_unbounded(ctx, ends):
     g, nwin = score(ctx, native.ALGO_SEMI_GLOBAL, O.BLOSUM62, q, buf, off, 10, 1, ends, 1)
     assert nwin == 0
     same(g, oracle(native.ALGO_SEMI_GLOBAL, O.BLOSUM62, q, buf, off, 10, 1, ends), f"ends={ends}")
+
+
+@pytest.mark.parametrize("algo,ends", CASES)
+@pytest.mark.parametrize("gaps", [(10, 1), (207, 200)])
+def test_windows_invent_no_alignment(ctx, algo, ends, gaps):
+    # random records with no copy of the query: the best score of a record is
+    # small, so a window that let an alignment begin where the whole record
+    # does not (a free query start past row 0) would show up as a larger
+    # score at a later row
+    rng = np.random.default_rng(73 + ends + gaps[1])
+    q = rng.integers(0, 20, 30, dtype=np.uint8)
+    recs = [rng.integers(0, 20, int(rng.integers(1, 300)), dtype=np.uint8) for _ in range(150)]
+    recs += [rng.integers(0, 20, L, dtype=np.uint8) for L in (60_000, 31_111, 9_000)]
+    buf, off = native.pack_records(recs)
+    g, nwin = score(ctx, algo, O.BLOSUM62, q, buf, off, gaps[0], gaps[1], ends, 1)
+    assert nwin > len(recs)
+    same(g, oracle(algo, O.BLOSUM62, q, buf, off, gaps[0], gaps[1], ends), f"algo={algo} ends={ends} gaps={gaps}")
