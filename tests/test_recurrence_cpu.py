@@ -1,0 +1,215 @@
+"""CPU models of two pieces of the wavefront engine's arithmetic, checked
+against plain Gotoh on small random inputs (no GPU needed):
+
+* semi-global row frames: row r is held raised by (r mod R) * ext with the
+  profile carrying +ext, the E update becomes max(T + ext - open, E), and every
+  R rows (R * ext <= 2048) the carried row drops back -- all in 16-bit
+  wrapping arithmetic, as the DPX add-max instructions compute it;
+* long records as overlapping windows: window results folded by (score,
+  first row, smallest column) equal the whole-record result when windows past
+  row 0 start from the fixed-query-start boundary (and, as the counterexample
+  shows, not when they start from a free-query-start one).
+"""
+import numpy as np
+import pytest
+
+NEG = -(10 ** 9)
+
+
+def gotoh_rows(q, r, M, op, ex, ends, local=False, start_row=0, top=None):
+    """Row-by-row plain Gotoh; yields (row, H row).  `top` overrides the
+    boundary above the first row (query-start rule), as a window uses it."""
+    Q = len(q)
+    qs, ts = ends & 1, ends & 4
+    if top is None:
+        top = [0] * Q if (local or qs) else [-(op + ex * j) for j in range(Q)]
+    Hp = list(top)
+    Ep = [h - op for h in Hp] if not local else [0] * Q
+    for i in range(len(r)):
+        gi = start_row + i
+        Hn, En = [0] * Q, [0] * Q
+        left = 0 if (local or ts) else -(op + ex * gi)
+        diag_left = 0 if (local or ts or gi == 0) else -(op + ex * (gi - 1))
+        F = NEG
+        for j in range(Q):
+            diag = diag_left if j == 0 else Hp[j - 1]
+            En[j] = max(Ep[j] - ex, Hp[j] - op)
+            F = max(F - ex, (Hn[j - 1] if j > 0 else left) - op)
+            h = max(diag + M[r[i]][q[j]], En[j], F)
+            Hn[j] = max(h, 0) if local else h
+        Hp, Ep = Hn, En
+        yield gi, Hp
+
+
+def sg_target_end(q, r, M, op, ex, ends, **kw):
+    """Semi-global with a free target end: (max over rows of H(i, Q-1), first row)."""
+    best, br = NEG, -1
+    for i, H in gotoh_rows(q, r, M, op, ex, ends, **kw):
+        if H[-1] > best:
+            best, br = H[-1], i
+    return best, br
+
+
+def sw_best(q, r, M, op, ex, **kw):
+    """Local: (best, first row, smallest column of it in that row)."""
+    best, br, bc = 0, -1, 0
+    for i, H in gotoh_rows(q, r, M, op, ex, 0, local=True, **kw):
+        m = max(H)
+        if m > best:
+            best, br, bc = m, i, H.index(m)
+    return best, br, bc
+
+
+def w16(x):
+    x &= 0xFFFF
+    return x - 0x10000 if x >= 0x8000 else x
+
+
+def frames_sg(q, r, M, op, ex, ends, G=2):
+    """The kernel's semi-global recurrence in row frames, G pipeline threads,
+    16-bit wrapping add-max."""
+    Q = len(q)
+    K = (Q + 1 + G - 1) // G
+    d = G * K - Q
+    R = 1
+    while R < (1 << 20) and 2 * R * max(ex, 1) <= 2048:
+        R *= 2
+    qs, ts = ends & 1, ends & 4
+    ppad = 0 if ts else -(op + ex)
+
+    def P(row, col):
+        return w16((ppad if col < 0 else int(M[r[row]][q[col]])) + ex)
+
+    def hinit(col):
+        return 0 if (col < 0 or qs) else -op - ex * col
+
+    hleft = 0 if ts else -20000
+    am = lambda a, b, c: max(w16(a + b), c)  # noqa: E731 -- DPX add-max
+    frame = lambda row: (row & (R - 1)) * ex  # noqa: E731
+    H = [[w16(hinit(t * K - d + j) - ex) for j in range(K)] for t in range(G)]
+    E = [[w16(hinit(t * K - d + j) - op) for j in range(K)] for t in range(G)]
+    prevH = [w16((hleft if t == 0 else hinit(t * K - d - 1)) - ex) for t in range(G)]
+    outH, outF = [0] * G, [0] * G
+    best, brow = -32768, -1
+    for step in range(len(r) + G - 1):
+        msgH, msgF = [0] + outH[:-1], [0] + outF[:-1]
+        newH, newF = list(outH), list(outF)
+        for t in range(G):
+            row = step - t
+            if row < 0 or row >= len(r):
+                continue
+            col0 = t * K - d
+            if row > 0 and (row & (R - 1)) == 0:
+                H[t] = [am(x, -R * ex, -32768) for x in H[t]]
+                E[t] = [am(x, -R * ex, -32768) for x in E[t]]
+                prevH[t] = am(prevH[t], -R * ex, -32768)
+            for j in range(K - 1, -1, -1):
+                T = am(prevH[t] if j == 0 else H[t][j - 1], P(row, col0 + j), E[t][j])
+                E[t][j] = am(T, ex - op, E[t][j])
+                H[t][j] = T
+            Fs = w16(-20000 + op) if t == 0 else msgF[t]
+            for j in range(K):
+                T = H[t][j]
+                H[t][j] = am(Fs, -op, T)
+                Fs = am(Fs, -ex, T)
+            prevH[t] = w16(hleft + frame(row)) if t == 0 else msgH[t]
+            newH[t], newF[t] = H[t][K - 1], Fs
+            if t == G - 1:
+                c = am(H[t][K - 1], -frame(row), -32768)
+                if c > best:
+                    best, brow = c, row
+        outH, outF = newH, newF
+    return best, brow
+
+
+def blosum_like(rng, n=20):
+    """Symmetric, mostly negative off the diagonal, positive on it."""
+    M = rng.integers(-4, 3, (n, n))
+    M = np.minimum(M, M.T)
+    M[np.arange(n), np.arange(n)] = rng.integers(4, 12, n)
+    return M
+
+
+@pytest.mark.parametrize("ext", [0, 1, 3, 200, 1000])
+def test_row_frames_equal_plain_gotoh(ext):
+    rng = np.random.default_rng(100 + ext)
+    M = blosum_like(rng)
+    op = ext + 7
+    qlen = 6 if ext >= 1000 else 12
+    for trial in range(6):
+        q = rng.integers(0, 20, qlen)
+        r = rng.integers(0, 20, int(rng.integers(1, 90)))
+        for ends in (12, 13, 8, 9):
+            for G in (1, 2, 4):
+                assert frames_sg(q, r, M, op, ext, ends, G) == sg_target_end(q, r, M, op, ext, ends), \
+                    (ext, trial, ends, G)
+
+
+def window_overlap(Q, mmax, mmin, op, ex, local):
+    min_best = 0 if local else Q * min(mmin, 0)
+    top = Q * max(mmax, 0) - op - min_best
+    return Q + 2 + max(0, -(-top // ex))
+
+
+def windowed(q, r, M, op, ex, ends, W, O, local, fixed_start_past_row0=True):
+    """Fold of window results, windows [k*W - O, (k+1)*W)."""
+    Q = len(q)
+    res = []
+    k = 0
+    while k * W < len(r):
+        st = 0 if k == 0 else k * W - O
+        en = min(len(r), (k + 1) * W)
+        top = None
+        if st > 0 and not local:
+            top = [-(op + ex * j) for j in range(Q)] if fixed_start_past_row0 else None
+        sub = r[st:en]
+        if local:
+            b, i, c = sw_best(q, sub, M, op, ex, start_row=st, top=top)
+            res.append((b, i, c))
+        else:
+            b, i = sg_target_end(q, sub, M, op, ex, ends, start_row=st, top=top)
+            res.append((b, i, Q - 1))
+        k += 1
+    # largest score, then first row, then smallest column; rows of -1 (no
+    # improvement) only when every window has the initial score
+    best = max(res, key=lambda x: (x[0], -x[1] if x[1] >= 0 else -(10 ** 12), -x[2]))
+    return best
+
+
+@pytest.mark.parametrize("local,ends", [(False, 12), (False, 13), (True, 0)])
+def test_window_fold_equals_whole_record(local, ends):
+    rng = np.random.default_rng(7 + ends + local)
+    M = blosum_like(rng)
+    for trial in range(8):
+        op, ex = [(10, 1), (5, 2), (30, 10)][trial % 3]
+        q = rng.integers(0, 20, 8)
+        r = rng.integers(0, 20, int(rng.integers(150, 400)))
+        O = window_overlap(len(q), int(M.max()), int(M.min()), op, ex, local)
+        W = max(O + 1, 40)
+        if local:
+            whole = sw_best(q, r, M, op, ex)
+        else:
+            b, i = sg_target_end(q, r, M, op, ex, ends)
+            whole = (b, i, len(q) - 1)
+        assert windowed(q, r, M, op, ex, ends, W, O, local) == whole, (trial, op, ex, W, O)
+
+
+def test_free_query_start_windows_would_invent_alignments():
+    # the counterexample behind the fixed-start rule: with a free query start,
+    # windows past row 0 that also start freely report scores the whole record
+    # does not have (large gap penalties keep the true best small)
+    rng = np.random.default_rng(3)
+    M = blosum_like(rng)
+    op, ex = 207, 200
+    found = False
+    for _ in range(40):
+        q = rng.integers(0, 20, 10)
+        r = rng.integers(0, 20, 300)
+        O = window_overlap(len(q), int(M.max()), int(M.min()), op, ex, False)
+        W = max(O + 1, 40)
+        b, i = sg_target_end(q, r, M, op, ex, 13)
+        whole = (b, i, len(q) - 1)
+        assert windowed(q, r, M, op, ex, 13, W, O, False, fixed_start_past_row0=True) == whole
+        if windowed(q, r, M, op, ex, 13, W, O, False, fixed_start_past_row0=False) != whole:
+            found = True
+    assert found
