@@ -139,6 +139,7 @@ extern "C" int ish_gpu_match_starts(ish_ctx *ctx, int32_t query_id, int32_t set_
     DevBuf *b[] = {&d_hits, &d_tend, &rlen, &slot, &poff, &orig, &rev_end, &d_start, &scan};
     for (DevBuf *x : b) x->release();
     rev.codes.release();
+    rev.windows.release();
   };
   int rc = ISH_OK;
   do {
@@ -209,7 +210,19 @@ extern "C" int ish_gpu_match_starts(ish_ctx *ctx, int32_t query_id, int32_t set_
     rev.orig_s.p = orig.p;
     SCU(cudaMemsetAsync(rev_end.p, 0, (size_t)n_hits * 4, s));
     OutDev out{nullptr, nullptr, rev_end.as<int32_t>(), nullptr};
-    if (rq.Q > 0) rc = fast ? launch_range(ctx, rq, rev, 0, n_hits, out, s) : launch_exact(ctx, rq, rev, 0, n_hits, out, s);
+    if (rq.Q > 0 && fast) {
+      // long prefixes (hits in long records) go through the window view like
+      // a forward pass; it needs the longest prefix
+      std::vector<uint32_t> hl(n_hits);
+      SCU(cudaMemcpy(hl.data(), rlen.p, (size_t)n_hits * 4, cudaMemcpyDeviceToHost));
+      rev.max_len = *std::max_element(hl.begin(), hl.end());
+      bool windowed = false;
+      rc = launch_windows(ctx, rq, rev, n_hits, out, s, &windowed);
+      if (!rc && !windowed) rc = launch_range(ctx, rq, rev, 0, n_hits, out, s);
+      if (!rc) SCU(cudaStreamSynchronize(s));
+    } else if (rq.Q > 0) {
+      rc = launch_exact(ctx, rq, rev, 0, n_hits, out, s);
+    }
     rev.off_s.p = rev.len_s.p = rev.orig_s.p = nullptr;  // owned by poff / rlen / orig
     if (rc) break;
     k_starts<<<hb, 256, 0, s>>>(rlen.as<uint32_t>(), rev_end.as<int32_t>(), n_hits, d_start.as<int64_t>());

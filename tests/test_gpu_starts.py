@@ -129,3 +129,22 @@ def test_matchers_report_match_results(ctx):
                 want.append((i, m[0], m[1]))
         assert res.matches() == want
         assert len(want) >= 30
+
+
+@pytest.mark.parametrize("ends", [12, 13])
+def test_starts_in_long_records(ctx, ends):
+    # hits deep inside long records: the reverse pass over their prefixes is
+    # windowed like a forward pass, starts must still be the CPU matcher's
+    rng = np.random.default_rng(950 + ends)
+    q = rng.integers(0, 5, 80, dtype=np.uint8)
+    recs = planted(rng, 5, q, 60, 50, 400, frac=0.3)
+    for L in (150_000, 90_000, 40_000):
+        r = rng.integers(0, 5, L, dtype=np.uint8)
+        for pos in (int(L * 0.9), int(L * 0.4)):
+            cp = q.copy()
+            mut = rng.random(len(cp)) < 0.05
+            cp[mut] = rng.integers(0, 5, int(mut.sum()), dtype=np.uint8)
+            r[pos:pos + len(cp)] = cp
+        recs.append(r)
+    n = check(ctx, native.ALGO_SEMI_GLOBAL, O.ACTGN, q, recs, 3, 1, ends, 0.5)
+    assert n >= 3
