@@ -413,6 +413,27 @@ def _roofline(ctx, gcups, instr=INSTR_SG):
                            f"{instr:.3g} instr per cell pair"}
 
 
+def _h2d_rate(pin):
+    """GB/s of a plain host-to-device copy of the e2e input buffer (torch,
+    outside the library): tells a slow host buffer from a slow load path."""
+    try:
+        import torch
+
+        src = torch.from_numpy(pin)
+        dst = torch.empty(len(pin), dtype=torch.uint8, device="cuda")
+        dst.copy_(src, non_blocking=True)
+        torch.cuda.synchronize()
+        t = time.perf_counter()
+        dst.copy_(src, non_blocking=True)
+        torch.cuda.synchronize()
+        dt = time.perf_counter() - t
+        del dst
+        torch.cuda.empty_cache()
+        return round(len(pin) / dt / 1e9, 1)
+    except Exception:
+        return None
+
+
 def _pinned(wl):
     try:
         import torch
@@ -482,6 +503,9 @@ def run_workload(args):
 
     native.load(build_if_missing=True)
     m = ScoringMatrix(wl.kind)
+    # pinned host copy of the batch for the end-to-end arm, allocated before
+    # the library's context exists
+    pin, pin_off = _pinned(wl)
     ctx = native.Context(local)
     qids = [ctx.set_query(q, wl.kind, m.values, native.ALGO_SEMI_GLOBAL, gap_open, gap_ext,
                           native.FREE_TARGET_START | native.FREE_TARGET_END, mx, thr) for q, _, _, mx in queries]
@@ -545,7 +569,7 @@ def run_workload(args):
     extra["speedup_vs_plain"] = round(value / world / plain, 1)
 
     # end to end from pinned host memory: upload + pack + score + results
-    pin, pin_off = _pinned(wl)
+    h2d_gbs = _h2d_rate(pin)
     e2e = []
     phases = []
     nh = 0
@@ -570,7 +594,7 @@ def run_workload(args):
     ph = np.mean(np.array(phases), axis=0)
     extra["e2e_phases_ms"] = {"load": round(float(ph[0]), 2), "score": round(float(ph[1]), 2),
                               "score_device": round(float(ph[2]), 2), "free": round(float(ph[3]), 2),
-                              "pinned": bool(getattr(_pinned, "ok", False))}
+                              "pinned": bool(getattr(_pinned, "ok", False)), "h2d_gbs_torch": h2d_gbs}
     d2h = 4 * nh + (0 if name == "batched" else 12 * wl.n) + 8 * (len(qids) + 1)
     if name == "line":
         # from raw text, as a line runner holds a file: upload, split into
