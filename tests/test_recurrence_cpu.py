@@ -213,3 +213,73 @@ def test_free_query_start_windows_would_invent_alignments():
         if windowed(q, r, M, op, ex, 13, W, O, False, fixed_start_past_row0=False) != whole:
             found = True
     assert found
+
+
+def sw_matrix(q, r, M, op, ex):
+    """All H rows of plain local Gotoh."""
+    return [list(H) for _, H in gotoh_rows(q, r, M, op, ex, 0, local=True)]
+
+
+def sw_reference_end(Hrows):
+    """The reference's rule: first row whose maximum strictly beats every
+    earlier cell, smallest column of that maximum in that row."""
+    best, br, bc = 0, -1, 0
+    for i, H in enumerate(Hrows):
+        m = max(H)
+        if m > best:
+            best, br, bc = m, i, H.index(m)
+    return (best, br, bc) if best > 0 else (0, -1, 0)
+
+
+def sw_filtered_end(Hrows, G, K):
+    """The wavefront kernel's local-alignment end logic on the same H values:
+    thread t owns columns [t*K, (t+1)*K); per row it records its row only when
+    its column maximum beats max(its recorded best, the running best of all
+    columns to its left for this row), then the threads' (score, row, column)
+    are folded left to right with the (score, earlier row, smaller column)
+    order."""
+    Q = len(Hrows[0]) if Hrows else 0
+    best = [0] * G
+    row_of = [-1] * G
+    saved = [None] * G
+    for i, H in enumerate(Hrows):
+        left = 0
+        for t in range(G):
+            cols = H[t * K:min(Q, (t + 1) * K)]
+            cm = max(cols) if cols else 0
+            thr = max(best[t], left)
+            nb = max(thr, cm)
+            if cm > thr:
+                best[t], row_of[t], saved[t] = cm, i, list(cols)
+            left = nb
+    acc = None
+    for t in range(G):
+        b, r = best[t], row_of[t]
+        c = 0x7FFF
+        if b > 0 and saved[t] is not None:
+            c = t * K + saved[t].index(b)
+        mine = (b, r, c)
+        if acc is not None:
+            lb, lr, lc = acc
+            if lb > b or (lb == b and (lr < r or (lr == r and lc < c))):
+                mine = acc
+        acc = mine
+    b, r, c = acc
+    return (b, r, c) if b > 0 else (0, -1, 0)
+
+
+@pytest.mark.parametrize("G", [1, 2, 4, 8])
+def test_local_end_filter_and_fold_equal_reference_rule(G):
+    rng = np.random.default_rng(40 + G)
+    M = blosum_like(rng, 6)  # a small alphabet: many equal maxima
+    for trial in range(60):
+        Q = int(rng.integers(1, 30))
+        K = (Q + G - 1) // G
+        q = rng.integers(0, 6, Q)
+        r = rng.integers(0, 6, int(rng.integers(0, 60)))
+        if trial % 3 == 0 and len(r) > Q:  # a copy of the query: a clear maximum
+            pos = int(rng.integers(0, len(r) - Q + 1))
+            r[pos:pos + Q] = q
+        op, ex = [(3, 1), (5, 2), (2, 1)][trial % 3]
+        Hrows = sw_matrix(q, r, M, op, ex)
+        assert sw_filtered_end(Hrows, G, K) == sw_reference_end(Hrows), (G, trial)
