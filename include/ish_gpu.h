@@ -93,6 +93,8 @@ ISH_API void ish_gpu_close(ish_ctx *ctx);
 /* Text of the last failure on this context ("" if none).  Valid until the
  * next call on the context.  ctx may be NULL (then: the last open failure). */
 ISH_API const char *ish_gpu_last_error(const ish_ctx *ctx);
+/* Sets one of the ISH_OPT_* options.  Refused (ISH_EINVAL) while the serving
+ * loop runs: its thread reads them. */
 ISH_API int ish_gpu_set_option(ish_ctx *ctx, int option, int64_t value);
 
 /* Register a query: the matcher state of StripedSemiGlobalMatcher.__init__

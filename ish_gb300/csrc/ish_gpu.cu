@@ -907,6 +907,8 @@ const char *ish_gpu_last_error(const ish_ctx *ctx) { return ctx ? ctx->err.c_str
 
 int ish_gpu_set_option(ish_ctx *ctx, int option, int64_t value) {
   if (!ctx) return ISH_EINVAL;
+  // the serving thread reads the options for every step
+  if (ctx->server) return fail(ctx, ISH_EINVAL, "options cannot change while the serving loop runs");
   switch (option) {
   case ISH_OPT_KERNEL:
     if (value < ISH_KERNEL_AUTO || value > ISH_KERNEL_EXACT) return fail(ctx, ISH_EINVAL, "bad kernel %lld", (long long)value);

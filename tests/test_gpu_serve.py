@@ -161,6 +161,8 @@ def test_serving_errors_stay_with_their_request(ctx):
         try:
             with pytest.raises(native.IshGpuError):
                 ctx.records_free(sid)  # in use by the serving loop
+            with pytest.raises(native.IshGpuError):
+                ctx.set_option(native.OPT_WAVE_LEAN, 1)  # the serving thread reads the options
             tb = ctx.submit(bad)
             t0, t1 = ctx.submit(ids[0]), ctx.submit(ids[1])
             with pytest.raises(native.IshGpuError) as ei:
