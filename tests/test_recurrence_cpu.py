@@ -283,3 +283,73 @@ def test_local_end_filter_and_fold_equal_reference_rule(G):
         op, ex = [(3, 1), (5, 2), (2, 1)][trial % 3]
         Hrows = sw_matrix(q, r, M, op, ex)
         assert sw_filtered_end(Hrows, G, K) == sw_reference_end(Hrows), (G, trial)
+
+
+def sg_kernel_fold(Hrows, Q, G, K, ends, neg_limit):
+    """The wavefront kernel's semi-global end logic on plain-Gotoh H rows:
+    the target-end running maximum (strict, first row wins), the last-row
+    query-end scan split over G threads of K columns (front padding d; each
+    thread keeps its first maximum, columns to the left win ties) and the
+    combination rule of the two."""
+    T = len(Hrows)
+    d = G * K - Q
+    te, qe = bool(ends & 8), bool(ends & 2)
+    best, row_a = neg_limit, -1
+    for i, H in enumerate(Hrows):
+        if H[Q - 1] > best:
+            best, row_a = H[Q - 1], i
+    mx = mq = None
+    if qe:
+        last = Hrows[T - 1]
+        for t in range(G):
+            b, c = -32768, 0x7FFF
+            for j in range(K):
+                col = t * K - d + j
+                if col >= 0 and last[col] > b:
+                    b, c = last[col], col
+            if t > 0 and not (b > mx):
+                b, c = mx, mq
+            mx, mq = b, c
+    eq = Q - 1
+    if not te and not qe:
+        return Hrows[T - 1][Q - 1], eq, T - 1
+    score = best if te else neg_limit
+    er = row_a if te else -1
+    if qe:
+        if mx > score:
+            score, er, eq = mx, T - 1, mq
+        elif mx == score and er == T - 1 and mq < eq:
+            eq = mq
+    return score, eq, er
+
+
+@pytest.mark.parametrize("kind", ["actgn", "blosum62"])
+def test_semi_global_fold_equals_oracle(kind):
+    import oracle as O
+    from ish_gb300 import native
+    from ish_gb300.scoring import ScoringMatrix
+
+    k = O.ACTGN if kind == "actgn" else O.BLOSUM62
+    alpha = 5 if kind == "actgn" else 20
+    m = ScoringMatrix(k)
+    M = m.values.astype(int)
+    rng = np.random.default_rng(91 + alpha)
+    for trial in range(12):
+        Q = int(rng.integers(1, 25))
+        q = rng.integers(0, alpha, Q, dtype=np.uint8)
+        recs = [rng.integers(0, alpha, int(rng.integers(1, 50)), dtype=np.uint8) for _ in range(6)]
+        op, ex = (3, 1) if kind == "actgn" else (10, 1)
+        mx_score = int(m.values[q, q].astype(np.int64).sum())
+        buf, off = native.pack_records(recs)
+        for ends in range(16):
+            om = O.Matcher(O.SEMI_GLOBAL, k, q, mx_score, 0.5, gap_open=op, gap_extend=ex, ends=ends)
+            o = om.batch(buf, off, threads=1)
+            min_score = int(M.min())
+            neg_limit = -32768 + op + 1 if -op < min_score else -32768 - min_score + 1
+            for n, r in enumerate(recs):
+                Hrows = [list(H) for _, H in gotoh_rows(q, r, M, op, ex, ends)]
+                want = (int(o["score"][n]), int(o["qend"][n]), int(o["tend"][n]))
+                for G in (1, 2, 4):
+                    K = (Q + 1 + G - 1) // G
+                    got = sg_kernel_fold(Hrows, Q, G, K, ends, neg_limit)
+                    assert got == want, (kind, trial, ends, n, G, got, want)
