@@ -353,3 +353,31 @@ def test_semi_global_fold_equals_oracle(kind):
                     K = (Q + 1 + G - 1) // G
                     got = sg_kernel_fold(Hrows, Q, G, K, ends, neg_limit)
                     assert got == want, (kind, trial, ends, n, G, got, want)
+
+
+@pytest.mark.parametrize("kind", ["actgn", "blosum62"])
+def test_local_end_logic_equals_oracle(kind):
+    import oracle as O
+    from ish_gb300 import native
+    from ish_gb300.scoring import ScoringMatrix
+
+    k = O.ACTGN if kind == "actgn" else O.BLOSUM62
+    alpha = 5 if kind == "actgn" else 20
+    m = ScoringMatrix(k)
+    M = m.values.astype(int)
+    rng = np.random.default_rng(97 + alpha)
+    for trial in range(20):
+        Q = int(rng.integers(1, 30))
+        q = rng.integers(0, alpha, Q, dtype=np.uint8)
+        recs = [rng.integers(0, alpha, int(rng.integers(0, 60)), dtype=np.uint8) for _ in range(8)]
+        op, ex = (3, 1) if kind == "actgn" else (10, 1)
+        mx_score = int(m.values[q, q].astype(np.int64).sum())
+        buf, off = native.pack_records(recs)
+        o = O.Matcher(O.LOCAL, k, q, mx_score, 0.5, gap_open=op, gap_extend=ex, ends=0).batch(buf, off, threads=1)
+        for n, r in enumerate(recs):
+            Hrows = sw_matrix(q, r, M, op, ex)
+            want = (int(o["score"][n]), int(o["tend"][n]), int(o["qend"][n]))
+            for G in (1, 2, 4):
+                K = (Q + G - 1) // G
+                got = sw_filtered_end(Hrows, G, K) if Hrows else (0, -1, 0)
+                assert got == want, (kind, trial, n, G, got, want)
