@@ -15,9 +15,13 @@ seconds / 1e9 (ish's own definition, benchmarking/ish_bench_aligner.mojo:740-750
   e2e       the same step through the C ABI from pinned host buffers: upload
             records, score both passes, copy scores/ends/hits back.
   roofline  integer cell-update roofline: measured DPX add-max throughput x 2
-            cells per instruction / 5 instructions per cell pair.
+            cells per instruction / DPX instructions per cell pair (4 for
+            semi-global, 5 for local; 4.5 cell-weighted over the step).
   cpu_baseline / --impl reference: the CPU oracle (a restatement of ish's
             striped CPU matchers) on all host cores, on a bounded sample.
+  parity    the timed step's scores, ends and hit flags compared with the
+            oracle on the CPU sample's records (outside the timed region); the
+            run exits non-zero on any mismatch.
 """
 from __future__ import annotations
 
@@ -159,6 +163,49 @@ def cpu_sample(wl, seconds):
     k = int(min(wl.n, max(len(probe), len(probe) * seconds / max(dt, 1e-3))))
     idx = np.sort(rng.choice(wl.n, k, replace=False))
     return idx, threads
+
+
+def parity_check(wl, idx, passes, threads, gap_open, gap_ext, thr):
+    """Bit-exact comparison of GPU results with the oracle on records `idx`.
+
+    `passes` is a list of (label, oracle algo, ends, encoded query, gpu result)
+    where the gpu result holds full-length "score"/"qend"/"tend" arrays (or a
+    subset of them) and "hit_idx" in original record order.  Runs outside every
+    timed region.  Returns {"records", "passes", "mismatches", "fields", ...}."""
+    import oracle as O
+    from ish_gb300.scoring import ScoringMatrix
+
+    sub = wl.subset(idx)
+    m = ScoringMatrix(wl.kind)
+    total = 0
+    bad = 0
+    first = None
+    fields = set()
+    hits = 0
+    for label, algo, ends, q, g in passes:
+        mx = int(m.values[q, q].astype(np.int64).sum())
+        om = O.Matcher(algo, wl.kind, q, mx, thr, gap_open=gap_open, gap_extend=gap_ext, ends=ends)
+        o = om.batch(sub.records, sub.offsets, threads=threads, forward=True, matches=True)
+        ghit = np.zeros(wl.n, np.uint8)
+        ghit[np.asarray(g["hit_idx"], np.int64)] = 1
+        cmp = [("hit", ghit[idx], o["hit"])]
+        for k in ("score", "qend", "tend"):
+            if k in g:
+                cmp.append((k, np.asarray(g[k])[idx], o[k]))
+        for k, a, b in cmp:
+            fields.add(k)
+            d = np.nonzero(a != b)[0]
+            bad += len(d)
+            if len(d) and first is None:
+                i = int(d[0])
+                first = f"{label} {k} record {int(idx[i])}: gpu {int(a[i])} oracle {int(b[i])}"
+        hits += int(o["hit"].sum())
+        total += len(idx)
+    out = {"records": int(len(idx)), "passes": len(passes), "record_passes": total, "mismatches": int(bad),
+           "fields": sorted(fields), "oracle_hits": hits}
+    if first:
+        out["first_mismatch"] = first
+    return out
 
 
 def run_reference(args):
@@ -303,6 +350,7 @@ def run_ours(args):
             traffic = None
 
     cpu = None
+    parity = None
     if rank == 0 and not args.no_cpu:
         import oracle as O
 
@@ -316,6 +364,10 @@ def run_ours(args):
         cpu = {"value": round(2 * len(q) * int(sub.offsets[-1]) / dt / 1e9, 4), "unit": "GCUPS", "cores": threads,
                "kind": "port",
                "sample": f"{len(idx)} of {n} records, semi-global + local, {dt:.1f} s on {threads} threads"}
+        # the last timed step's own outputs against the oracle on the same
+        # records (outside the timed region)
+        parity = parity_check(wl, idx, [("semi-global", O.SEMI_GLOBAL, O.TS | O.TE, q, res[0]),
+                                        ("local", O.LOCAL, 0, q, res[1])], threads, 10, 1, 0.8)
 
     if rank == 0:
         lat = np.array(e2e_ms)
@@ -340,11 +392,15 @@ def run_ours(args):
             "plain_kernel_gcups": round(plain, 2) if plain else None,
             "wall_ms_per_step": round(wall_ms, 3),
             "hits": {"semi_global": hits[0], "local": hits[1]},
+            "parity": parity,
         }
         print(json.dumps(out))
     ctx.close()
     if dist is not None:
         dist.destroy_process_group()
+    if parity is not None and parity["mismatches"]:
+        print(f"bench: GPU results differ from the oracle: {parity.get('first_mismatch')}", file=sys.stderr)
+        sys.exit(3)
 
 
 # ---------------------------------------------------------------------------
@@ -381,7 +437,8 @@ def _cpu_sample(wl, queries, gap_open, gap_ext, thr, seconds, max_queries=8):
     import oracle as O
 
     threads = os.cpu_count() or 1
-    qs = queries[:: max(1, len(queries) // max_queries)][:max_queries]
+    qsel = list(range(len(queries)))[:: max(1, len(queries) // max_queries)][:max_queries]
+    qs = [queries[i] for i in qsel]
     rng = np.random.default_rng(123)
 
     def timed(idx):
@@ -398,6 +455,7 @@ def _cpu_sample(wl, queries, gap_open, gap_ext, thr, seconds, max_queries=8):
     idx = np.sort(rng.choice(wl.n, k, replace=False))
     sub, dt = timed(idx)
     cells = sum(len(q) for q, *_ in qs) * int(sub.offsets[-1])
+    _cpu_sample.last = (idx, qsel, threads)
     return {"value": round(cells / dt / 1e9, 4), "unit": "GCUPS", "cores": threads, "kind": "port",
             "sample": f"{len(qs)} of {len(queries)} queries x {k} of {wl.n} records, {dt:.1f} s on {threads} threads"}
 
@@ -616,8 +674,23 @@ def run_workload(args):
                                   "h2d_bytes_per_step": len(text), "lines": nl,
                                   "hits_equal": bool(len(r["hit_idx"]) == nh)}
     cpu = None
+    parity = None
     if rank == 0 and not args.no_cpu:
         cpu = _cpu_sample(wl, queries, gap_open, gap_ext, thr, args.cpu_seconds)
+        pidx, qsel, threads = _cpu_sample.last
+        if name == "batched":
+            # the timed step fetched hit lists only; one more batched launch
+            # (untimed) returns the scores and ends of the same queries
+            full = ctx.score_multi(qids, sid, want=("score", "qend", "tend", "hit_idx"))
+            gres = [{"score": full["score"][i], "qend": full["qend"][i], "tend": full["tend"][i],
+                     "hit_idx": res["hit_idx"][i]} for i in qsel]
+            for i in qsel:
+                if not np.array_equal(full["hit_idx"][i], res["hit_idx"][i]):
+                    raise SystemExit(f"bench: batched hit lists differ between two launches (query {i})")
+        else:
+            gres = [res]
+        parity = parity_check(wl, pidx, [(f"query {i}", queries[i][1], queries[i][2], queries[i][0], g)
+                                         for i, g in zip(qsel, gres)], threads, gap_open, gap_ext, thr)
     if rank == 0:
         line = _base_line(args, world, value, step_ms, config)
         line.update({
@@ -627,12 +700,15 @@ def run_workload(args):
                     "h2d_bytes_per_step": int(len(wl.records) + 8 * len(wl.offsets)), "d2h_bytes_per_step": int(d2h),
                     "latency_ms": {"p50": round(float(np.percentile(e2e, 50)), 3),
                                    "p99": round(float(np.percentile(e2e, 99)), 3)}},
-            "gpu_launches": launches, "clocks": clk, "hits": int(nh), **extra,
+            "gpu_launches": launches, "clocks": clk, "hits": int(nh), "parity": parity, **extra,
         })
         print(json.dumps(line))
     ctx.close()
     if dist is not None:
         dist.destroy_process_group()
+    if parity is not None and parity["mismatches"]:
+        print(f"bench: GPU results differ from the oracle: {parity.get('first_mismatch')}", file=sys.stderr)
+        sys.exit(3)
 
 
 def run_serving(args, rank, world, local, dist):

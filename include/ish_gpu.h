@@ -81,6 +81,18 @@ extern "C" {
 #define ISH_OPT_WAVE_BLOCKS 8 /* cap wavefront blocks per SM (0 = as many as fit) */
 #define ISH_OPT_WINDOWS 10    /* 1 (default): window long records when they would bound the pass; 0: never */
 #define ISH_OPT_WAVE_LEAN 9   /* 34 <= K <= 48: -1 measured default, 0 128x3 blocks, 1 128x2 (more registers) */
+/* Fault injection for testing a caller's error paths (no counterpart in the
+ * reference).  ISH_OPT_STEP_BUDGET: 0 (default) lets every wavefront and
+ * batched launch of this context run to the end of its work; n > 0 caps each
+ * warp at n pipeline steps, so a launch with more work stops early and the call
+ * (or, in the serving loop, the queries of that step) fails with
+ * ISH_ETIMEDOUT -- the device-side bound every wavefront launch carries, made
+ * to run out.  ISH_OPT_FAULT_ALLOC: n >= 0 makes the (n+1)-th device allocation
+ * the library attempts from now on fail as if device memory were exhausted
+ * (ISH_ENOMEM); it applies to every context of the process and disarms after
+ * firing; -1 disarms it.  Neither changes results when left at its default. */
+#define ISH_OPT_STEP_BUDGET 11
+#define ISH_OPT_FAULT_ALLOC 12
 
 typedef struct ish_ctx ish_ctx;
 

@@ -97,6 +97,7 @@ struct BatchParams {
   uint32_t *tile_counter;     // one pair counter per tile, zeroed before launch
   uint32_t prof_area;         // shared-memory bytes reserved for the largest profile (16-byte multiple)
   uint32_t slot_words;        // slot words per block: 32 per group at the class's smallest G
+  uint64_t step_cap;          // nonzero: pipeline steps per warp and tile (ISH_OPT_STEP_BUDGET)
 };
 
 struct PlainParams {

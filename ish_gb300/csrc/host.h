@@ -18,6 +18,14 @@
 namespace ish {
 namespace host {
 
+// Injected allocation failure (ISH_OPT_FAULT_ALLOC): -1 disarmed, else the
+// number of device allocations still to succeed before one fails.
+extern std::atomic<int64_t> g_alloc_fault;
+inline bool alloc_fault_fires() {
+  if (g_alloc_fault.load(std::memory_order_relaxed) < 0) return false;
+  return g_alloc_fault.fetch_sub(1) == 0;
+}
+
 struct DevBuf {
   void *p = nullptr;
   size_t cap = 0;
@@ -26,6 +34,7 @@ struct DevBuf {
     if (p) cudaFree(p);
     p = nullptr;
     cap = 0;
+    if (alloc_fault_fires()) return cudaErrorMemoryAllocation;
     size_t want = bytes < 256 ? 256 : bytes;
     cudaError_t e = cudaMalloc(&p, want);
     if (e == cudaSuccess) cap = want;
@@ -170,6 +179,7 @@ struct ish_ctx {
   int force_blocks = 0;  // cap on wavefront blocks per SM (0: occupancy limit)
   int force_lean = -1;   // lean kernel variant: -1 per (K, mode) default, 0 off, 1 on
   int windows_on = 1;    // window long records (windows.cu)
+  uint64_t step_budget = 0;  // ISH_OPT_STEP_BUDGET: cap on pipeline steps per warp (0: the launch's own bound)
   std::map<int32_t, ish::host::Query> queries;
   int32_t next_query = 1;
   std::map<int32_t, ish::host::RecordSet> sets;

@@ -23,6 +23,7 @@ namespace ish {
 namespace host {
 
 thread_local std::string g_open_error;
+std::atomic<int64_t> g_alloc_fault{-1};
 
 int fail(ish_ctx *c, int code, const char *fmt, ...) {
   char buf[512];
@@ -413,11 +414,17 @@ int pack_set(ish_ctx *ctx, uint32_t n, uint64_t raw_bytes, const uint64_t *end, 
   CU(ctx->len_tmp.ensure((size_t)n * 4));
   CU(ctx->slot_tmp.ensure((size_t)n * 8));
   CU(ctx->poff_tmp.ensure((size_t)n * 8));
-  CU(ctx->hist.ensure((size_t)NBUCKETS * 4 * 2));
-  CU(cudaMemsetAsync(ctx->hist.p, 0, (size_t)NBUCKETS * 4, s));
+  // counts [NBUCKETS], descending cursors [NBUCKETS], per-block sums
+  CU(ctx->hist.ensure((size_t)NBUCKETS * 4 * 2 + BUCKET_BLOCKS * 4));
+  uint32_t *counts = ctx->hist.as<uint32_t>(), *cursor = counts + NBUCKETS, *bsums = cursor + NBUCKETS;
+  // max_code[0]: largest record code, [1]: largest length bucket
+  CU(ctx->max_code.ensure(16));
+  uint32_t *max_code = ctx->max_code.as<uint32_t>();
+  CU(cudaMemsetAsync(ctx->max_code.p, 0, 8, s));
+  CU(cudaMemsetAsync(counts, 0, (size_t)NBUCKETS * 4, s));
   const uint32_t nb = std::min<uint32_t>(ceil_div(n, 256), (uint32_t)ctx->num_sms * 16);
   k_lengths<<<nb, 256, 0, s>>>(ctx->off_in.as<uint64_t>(), end, n, ctx->len_tmp.as<uint32_t>(),
-                                ctx->slot_tmp.as<uint64_t>(), ctx->hist.as<uint32_t>());
+                                ctx->slot_tmp.as<uint64_t>(), counts, max_code + 1);
   ++ctx->launches;
   // exclusive scan of slot sizes -> packed offsets
   const uint32_t tiles = ceil_div(n, SCAN_TILE);
@@ -433,17 +440,17 @@ int pack_set(ish_ctx *ctx, uint32_t n, uint64_t raw_bytes, const uint64_t *end, 
     k_scan64_add<<<tiles, 1024, 0, s>>>(ctx->poff_tmp.as<uint64_t>(), n, boff);
     ++ctx->launches;
   }
-  // host copy of the histogram, then turn it into descending bucket cursors
-  rs.hist.assign(NBUCKETS, 0);
-  CU(cudaMemcpyAsync(rs.hist.data(), ctx->hist.p, (size_t)NBUCKETS * 4, cudaMemcpyDeviceToHost, s));
-  k_bucket_scan<<<1, 1024, 0, s>>>(ctx->hist.as<uint32_t>());
+  // descending bucket cursors (the counts stay for the host copy below)
+  k_bucket_sums<<<BUCKET_BLOCKS, 1024, 0, s>>>(counts, max_code + 1, bsums);
+  ++ctx->launches;
+  k_bucket_cursors<<<BUCKET_BLOCKS, 1024, 0, s>>>(counts, max_code + 1, bsums, cursor);
   ++ctx->launches;
   const uint64_t packed = rs.total + 16ull * n + 16;
   take_spare_set(ctx, rs, packed);
   CU(rs.len_s.ensure((size_t)n * 4));
   CU(rs.off_s.ensure((size_t)n * 8));
   CU(rs.orig_s.ensure((size_t)n * 4));
-  k_scatter<<<nb, 256, 0, s>>>(ctx->len_tmp.as<uint32_t>(), ctx->poff_tmp.as<uint64_t>(), n, ctx->hist.as<uint32_t>(),
+  k_scatter<<<nb, 256, 0, s>>>(ctx->len_tmp.as<uint32_t>(), ctx->poff_tmp.as<uint64_t>(), n, cursor,
                                rs.len_s.as<uint32_t>(), rs.off_s.as<uint64_t>(), rs.orig_s.as<uint32_t>());
   ++ctx->launches;
   {
@@ -457,21 +464,28 @@ int pack_set(ish_ctx *ctx, uint32_t n, uint64_t raw_bytes, const uint64_t *end, 
     CU(e);
   }
   const uint32_t pb = std::min<uint32_t>(ceil_div((uint64_t)n * 32, 256), (uint32_t)ctx->num_sms * 32);
-  CU(ctx->max_code.ensure(16));
-  CU(cudaMemsetAsync(ctx->max_code.p, 0, 4, s));
   k_pack<<<pb, 256, 0, s>>>(ctx->raw.as<uint8_t>(), raw_bytes, ctx->off_in.as<uint64_t>(), end,
-                            ctx->poff_tmp.as<uint64_t>(), n, enc, rs.codes.as<uint8_t>(), ctx->max_code.as<uint32_t>());
+                            ctx->poff_tmp.as<uint64_t>(), n, enc, rs.codes.as<uint8_t>(), max_code);
   ++ctx->launches;
   CU(cudaGetLastError());
-  CU(cudaMemcpyAsync(&rs.max_code, ctx->max_code.p, 4, cudaMemcpyDeviceToHost, s));
+  // host copy of the histogram: the buckets of lengths up to HIST_HEAD in the
+  // same round trip as the largest code and bucket, the rest (long records
+  // only) after it
+  constexpr uint32_t HIST_HEAD = 8192;
+  uint32_t mc[2] = {0, 0};
+  rs.hist.assign(NBUCKETS, 0);
+  CU(cudaMemcpyAsync(mc, ctx->max_code.p, 8, cudaMemcpyDeviceToHost, s));
+  CU(cudaMemcpyAsync(rs.hist.data(), counts, (size_t)HIST_HEAD * 4, cudaMemcpyDeviceToHost, s));
   CU(cudaStreamSynchronize(s));
+  rs.max_code = mc[0];
+  const uint32_t maxb = std::min<uint32_t>(mc[1], NBUCKETS - 1);
+  if (maxb >= HIST_HEAD) {
+    CU(cudaMemcpyAsync(rs.hist.data() + HIST_HEAD, counts + HIST_HEAD, (size_t)(maxb + 1 - HIST_HEAD) * 4,
+                       cudaMemcpyDeviceToHost, s));
+    CU(cudaStreamSynchronize(s));
+  }
   rs.n_empty = rs.hist[0];
-  rs.max_len = 0;
-  for (int b = NBUCKETS - 1; b >= 0; --b)
-    if (rs.hist[b]) {
-      rs.max_len = b < 32768 ? (uint32_t)b : (uint32_t)(32768 + ((uint64_t)(b - 32768) << 5) + 31);
-      break;
-    }
+  rs.max_len = maxb < 32768 ? maxb : (uint32_t)(32768 + ((uint64_t)(maxb - 32768) << 5) + 31);
   return ISH_OK;
 }
 
@@ -656,7 +670,7 @@ int launch_wave_range(ish_ctx *ctx, Query &q, RecordSet &rs, uint32_t first, uin
   p.first = first;
   p.count = count;
   p.counter = ctx->counter.as<uint32_t>();
-  p.max_steps = rs.total + 2ull * count + 1024;
+  p.max_steps = ctx->step_budget ? ctx->step_budget : rs.total + 2ull * count + 1024;
   CU(cudaMemsetAsync(ctx->counter.p, 0, 4, s));
   fn<<<grid, threads, smem, s>>>(p);
   ++ctx->launches;
@@ -946,6 +960,15 @@ int ish_gpu_set_option(ish_ctx *ctx, int option, int64_t value) {
     if (value < -1 || value > 1) return fail(ctx, ISH_EINVAL, "lean variant must be -1, 0 or 1");
     ctx->force_lean = (int)value;
     drop_plans(ctx, 0, 0);
+    return ISH_OK;
+  case ISH_OPT_STEP_BUDGET:
+    if (value < 0) return fail(ctx, ISH_EINVAL, "step budget must be >= 0");
+    ctx->step_budget = (uint64_t)value;
+    drop_plans(ctx, 0, 0);
+    return ISH_OK;
+  case ISH_OPT_FAULT_ALLOC:
+    if (value < -1) return fail(ctx, ISH_EINVAL, "allocation fault countdown must be >= -1");
+    g_alloc_fault.store(value);
     return ISH_OK;
   case ISH_OPT_WAVE_BLOCKS:
     if (value < 0 || value > 32) return fail(ctx, ISH_EINVAL, "blocks per SM must be in 0..32");

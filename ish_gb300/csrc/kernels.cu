@@ -28,38 +28,81 @@ __device__ __forceinline__ uint64_t rec_len(const uint64_t *off, const uint64_t 
 }
 
 __global__ void k_lengths(const uint64_t *off, const uint64_t *end, uint32_t n, uint32_t *len, uint64_t *slot_bytes,
-                          uint32_t *hist) {
+                          uint32_t *hist, uint32_t *max_bucket) {
+  uint32_t mb = 0;
   for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
     const uint64_t l = rec_len(off, end, i);
     len[i] = (uint32_t)l;
     slot_bytes[i] = (l + 15) & ~(uint64_t)15;
-    atomicAdd(&hist[len_bucket(l)], 1u);
+    const uint32_t b = len_bucket(l);
+    atomicAdd(&hist[b], 1u);
+    mb = max(mb, b);
+  }
+  for (int o = 16; o > 0; o >>= 1) mb = max(mb, __shfl_xor_sync(0xffffffffu, mb, o));
+  if ((threadIdx.x & 31) == 0 && mb) atomicMax(max_bucket, mb);
+}
+
+// Exclusive scan of the bucket histogram in DESCENDING bucket order, in two
+// passes of BUCKET_BLOCKS blocks: block b covers the descending positions
+// [b*1024, b*1024 + 1024), i.e. buckets NBUCKETS-1-(b*1024+t), so every load
+// is coalesced.  Blocks whose buckets all lie above the set's largest bucket
+// hold no records and skip their loads.
+__device__ __forceinline__ bool bucket_block_empty(uint32_t b, const uint32_t *max_bucket) {
+  return NBUCKETS - 1024 * (b + 1) > *max_bucket;  // the block's smallest bucket is above the largest used
+}
+
+__global__ void __launch_bounds__(1024) k_bucket_sums(const uint32_t *hist, const uint32_t *max_bucket,
+                                                      uint32_t *sums) {
+  __shared__ uint32_t warp_sum[32];
+  const uint32_t b = blockIdx.x;
+  if (bucket_block_empty(b, max_bucket)) {
+    if (threadIdx.x == 0) sums[b] = 0;
+    return;
+  }
+  uint32_t v = hist[NBUCKETS - 1 - (b * 1024 + threadIdx.x)];
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  if ((threadIdx.x & 31) == 0) warp_sum[threadIdx.x >> 5] = v;
+  __syncthreads();
+  if (threadIdx.x < 32) {
+    uint32_t w = warp_sum[threadIdx.x];
+    for (int o = 16; o > 0; o >>= 1) w += __shfl_xor_sync(0xffffffffu, w, o);
+    if (threadIdx.x == 0) sums[b] = w;
   }
 }
 
-// Exclusive scan of the bucket histogram in DESCENDING bucket order (one block).
-__global__ void k_bucket_scan(uint32_t *hist) {
-  __shared__ uint32_t part[1024];
-  const int tid = threadIdx.x;
-  const int per = NBUCKETS / 1024;
-  // thread tid owns descending buckets [tid*per, (tid+1)*per) counted from the top
-  uint32_t s = 0;
-  for (int k = 0; k < per; ++k) s += hist[NBUCKETS - 1 - (tid * per + k)];
-  part[tid] = s;
+__global__ void __launch_bounds__(1024) k_bucket_cursors(const uint32_t *hist, const uint32_t *max_bucket,
+                                                         const uint32_t *sums, uint32_t *cursor) {
+  __shared__ uint32_t warp_incl[32];
+  __shared__ uint32_t base;
+  const uint32_t b = blockIdx.x;
+  if (bucket_block_empty(b, max_bucket)) return;  // no record lands in these buckets
+  const uint32_t tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  if (warp == 0) {  // records in the blocks before this one (BUCKET_BLOCKS <= 64)
+    uint32_t s = 0;
+    for (uint32_t k = lane; k < b; k += 32) s += sums[k];
+    for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+    if (lane == 0) base = s;
+  }
+  const uint32_t bucket = NBUCKETS - 1 - (b * 1024 + tid);
+  const uint32_t c = hist[bucket];
+  uint32_t incl = c;
+  for (int o = 1; o < 32; o <<= 1) {
+    const uint32_t x = __shfl_up_sync(0xffffffffu, incl, o);
+    if (lane >= (uint32_t)o) incl += x;
+  }
+  if (lane == 31) warp_incl[warp] = incl;
   __syncthreads();
-  for (int off = 1; off < 1024; off <<= 1) {
-    uint32_t v = tid >= off ? part[tid - off] : 0;
-    __syncthreads();
-    part[tid] += v;
-    __syncthreads();
+  if (warp == 0) {
+    uint32_t w = warp_incl[lane];
+    for (int o = 1; o < 32; o <<= 1) {
+      const uint32_t x = __shfl_up_sync(0xffffffffu, w, o);
+      if (lane >= (uint32_t)o) w += x;
+    }
+    warp_incl[lane] = w;
   }
-  uint32_t run = part[tid] - s;
-  for (int k = 0; k < per; ++k) {
-    const int b = NBUCKETS - 1 - (tid * per + k);
-    const uint32_t c = hist[b];
-    hist[b] = run;
-    run += c;
-  }
+  __syncthreads();
+  const uint32_t before_warp = warp ? warp_incl[warp - 1] : 0u;
+  cursor[bucket] = base + before_warp + incl - c;
 }
 
 __global__ void k_scatter(const uint32_t *len, const uint64_t *poff, uint32_t n, uint32_t *cursor,

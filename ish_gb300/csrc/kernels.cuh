@@ -12,8 +12,11 @@ constexpr uint32_t HIT_TILE = 8192;      // records per block of the hit compact
 
 constexpr uint32_t LINE_TILE = 65536;    // text bytes per block of the line splitter
 __global__ void k_lengths(const uint64_t *off, const uint64_t *end, uint32_t n, uint32_t *len, uint64_t *slot_bytes,
-                          uint32_t *hist);
-__global__ void k_bucket_scan(uint32_t *hist);
+                          uint32_t *hist, uint32_t *max_bucket);
+constexpr uint32_t BUCKET_BLOCKS = NBUCKETS / 1024;  // blocks of the two-pass bucket scan
+__global__ void k_bucket_sums(const uint32_t *hist, const uint32_t *max_bucket, uint32_t *sums);
+__global__ void k_bucket_cursors(const uint32_t *hist, const uint32_t *max_bucket, const uint32_t *sums,
+                                 uint32_t *cursor);
 __global__ void k_scatter(const uint32_t *len, const uint64_t *poff, uint32_t n, uint32_t *cursor, uint32_t *len_s,
                           uint64_t *off_s, uint32_t *orig_s);
 __global__ void k_pack(const uint8_t *src, uint64_t src_bytes, const uint64_t *off, const uint64_t *end,

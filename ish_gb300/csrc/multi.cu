@@ -236,6 +236,7 @@ int enqueue_plan(ish_ctx *ctx, MultiPlan &P, RecordSet &rs, cudaStream_t s) {
     b.tile_counter = P.counters.as<uint32_t>() + c.counter_base;
     b.prof_area = c.prof_area;
     b.slot_words = (uint32_t)((c.threads / c.Gmin) * 32);
+    b.step_cap = ctx->step_budget;
     if (c.ntiles) c.fn<<<c.grid, c.threads, c.smem, cs>>>(b);
     if (c.ntiles) ++P.kernels;
     CU(cudaGetLastError());

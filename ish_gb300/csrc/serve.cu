@@ -314,6 +314,7 @@ int step(Server &S, char *msg) {
       b.tile_counter = S.step_counters.as<uint32_t>() + C.first;
       b.prof_area = C.prof_area;
       b.slot_words = (uint32_t)slot_words;
+      b.step_cap = S.ctx->step_budget;
       cudaStream_t cs = c == 0 ? s : S.side[c - 1];
       if (c > 0) SCU(cudaStreamWaitEvent(cs, S.fork, 0));
       fn<<<per_sm * S.ctx->num_sms, threads, smem, cs>>>(b);
@@ -483,7 +484,8 @@ void stop_server(ish_ctx *ctx) {
   }
   S->cv_work.notify_all();
   if (S->th.joinable()) S->th.join();
-  cudaStreamSynchronize(S->s);
+  // (a serve_start that failed part-way may have created only some of these)
+  if (S->s) cudaStreamSynchronize(S->s);
   for (Bundle *b : S->pool) {
     b->release();
     delete b;
@@ -491,10 +493,10 @@ void stop_server(ish_ctx *ctx) {
   for (auto &kv : S->finished) delete kv.second;
   for (auto st : S->side) cudaStreamDestroy(st);
   for (auto e : S->join) cudaEventDestroy(e);
-  cudaEventDestroy(S->ev0);
-  cudaEventDestroy(S->ev1);
-  cudaEventDestroy(S->fork);
-  cudaStreamDestroy(S->s);
+  if (S->ev0) cudaEventDestroy(S->ev0);
+  if (S->ev1) cudaEventDestroy(S->ev1);
+  if (S->fork) cudaEventDestroy(S->fork);
+  if (S->s) cudaStreamDestroy(S->s);
   S->step_params.release();
   S->step_tiles.release();
   S->step_counters.release();
@@ -540,6 +542,7 @@ int ish_gpu_serve_start(ish_ctx *ctx, int32_t set_id, uint32_t max_active, uint6
   make_chunks(*S, chunks);
   for (const auto &ch : S->chunks) S->max_chunk = std::max(S->max_chunk, ch.second);
   auto bail = [&](cudaError_t e) {
+    (void)cudaGetLastError();
     ctx->server = S;
     stop_server(ctx);
     return fail(ctx, e == cudaErrorMemoryAllocation ? ISH_ENOMEM : ISH_EDEVICE, "serve_start: %s",

@@ -584,7 +584,7 @@ __global__ void __launch_bounds__(wave_threads_lean(K, MODE, LEAN), wave_blocks_
         // every group's steps are bounded by all pairs of the range at its
         // longest length (records are sorted, the first is longest)
         const uint64_t npairs = (tl.count + 1) / 2;
-        sp.max_steps = npairs * ((uint64_t)qp->rec.len[tl.first] + 2 * 32 + 8) + 1024;
+        sp.max_steps = b.step_cap ? b.step_cap : npairs * ((uint64_t)qp->rec.len[tl.first] + 2 * 32 + 8) + 1024;
       }
     }
     __syncthreads();

@@ -21,6 +21,8 @@ OPT_PROFILE_LAYOUT = 7
 OPT_WAVE_BLOCKS = 8
 OPT_WAVE_LEAN = 9
 OPT_WINDOWS = 10
+OPT_STEP_BUDGET = 11
+OPT_FAULT_ALLOC = 12
 PROF_AUTO, PROF_S16, PROF_PAIR, PROF_S32 = -1, 0, 1, 2
 
 # Entry points declared in include/ish_gpu.h (checked by the tests).
