@@ -70,6 +70,12 @@ extern "C" {
 #define ISH_KERNEL_AUTO 0  /* wavefront engine, exact fallback where needed */
 #define ISH_KERNEL_PLAIN 1 /* one thread per record (the reference GPU design) */
 #define ISH_KERNEL_EXACT 2 /* per-record emulation of the striped CPU algorithm */
+/* one thread per record with int16 per-thread H/E arrays, 15,000 threads in
+ * blocks of 32: the reference GPU kernel's storage and launch shape
+ * (ishlib/matcher/alignment/semi_global_aln/basic.mojo:305-306,
+ * ishlib/gpu/searcher_device.mojo:477-497); queries up to 2048 residues,
+ * longer ones run as ISH_KERNEL_PLAIN */
+#define ISH_KERNEL_PLAIN16 3
 
 #define ISH_OPT_KERNEL 1      /* value: ISH_KERNEL_* */
 #define ISH_OPT_SG_LANES 2    /* int16 lanes of the reference CPU build (default 8) */
@@ -250,7 +256,12 @@ ISH_API int ish_gpu_serve_stats(ish_ctx *ctx, uint64_t *completed, double *cells
  *   d_offsets: device uint64[n+1], record i = d_records[d_offsets[i] .. d_offsets[i+1]);
  *   enc_query, matrix: HOST arrays, as for ish_gpu_set_query;
  *   d_score, d_query_end, d_target_end, d_hit: device outputs (any may be NULL),
- *       same values as ish_gpu_score, in record order;
+ *       same values as ish_gpu_score, in record order, for every request it
+ *       accepts.  It has no lane-exact fallback: parameters outside the
+ *       exact-integer regime (gap_open <= gap_extend, scores that could leave
+ *       int16) and, with a fixed target start, records too long for the int16
+ *       boundary row are refused with ISH_EINVAL where ish_gpu_score would
+ *       switch to its exact kernels;
  *   stream: cudaStream_t to run on (NULL = the legacy default stream);
  *   err: optional buffer for a message (err_len bytes).
  * Working memory is a fixed 32 MiB __device__ array inside the library that
@@ -259,7 +270,10 @@ ISH_API int ish_gpu_serve_stats(ish_ctx *ctx, uint64_t *completed, double *cells
  * with ISH_EOVERFLOW.  All calls share that array: calls that overlap on the
  * GPU race and must be serialised by the caller.  The first call on a device
  * (with that device current) resolves the array's address; make it before
- * any stream capture.  Blocks until the work on `stream` is done. */
+ * any stream capture, and do not use the entry point after a cudaDeviceReset
+ * (or a release of the device's primary context) in the same process: the
+ * address kept from the first call would be stale.  Blocks until the work on
+ * `stream` is done. */
 ISH_API int ish_gpu_score_noalloc(const uint8_t *d_records, uint64_t records_bytes, const uint64_t *d_offsets,
                                   uint32_t n, const uint8_t *enc_query, uint32_t qlen, const int8_t *matrix,
                                   uint32_t alphabet, int algo, uint32_t gap_open, uint32_t gap_ext,

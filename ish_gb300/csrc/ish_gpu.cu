@@ -140,12 +140,12 @@ int matrix_alphabet_ok(uint32_t alphabet) { return alphabet >= 1 && alphabet <= 
 int wave_lean(const ish_ctx *ctx, int K, int mode) {
   if (!wave_has_lean(K)) return 0;
   if (ctx->force_lean >= 0) return ctx->force_lean;
-  if (K <= 32) return 0;
-  const int i = (K - 34) / 2;  //                         K = 34 36 38 40 42 44 46 48
-  if (i < 0 || i >= 8) return 0;
-  static const unsigned char lean[2][8] = {/* semi-global */ {1, 1, 1, 1, 0, 0, 0, 0},
-                                           /* local */ {1, 1, 1, 0, 0, 0, 0, 0}};
-  return lean[mode == SW][i];
+  // Measured per K (protein, 200k records, G = 8, Q = 8K - 2, the rows-per-step
+  // kernel): the 128 x 3 build beats 256 x 2 from K = 27 (semi-global) / 30
+  // (local) on, by up to 16 %; from K = 34 the 128 x 3 default build beats the
+  // 128 x 2 lean one by 3-19 % up to K = 44, and loses at 46-48.
+  if (K <= 32) return mode == SW ? K >= 30 : K >= 27;
+  return K >= 46;
 }
 
 // The same choice for the batched kernel (parameters in shared memory, one
@@ -177,7 +177,7 @@ Regime regime(const Query &q, int qpad) {
     return r;
   }
   if (q.open + q.ext > 10000) return r;
-  if (q.ext > 2048) return r;  // row frames (see frame_rows)
+  if (frame_rows(q.ext) < WAVE_RPS_SG) return r;  // row frames reset at step boundaries (see frame_rows)
   const long base = 2L * q.open + (long)q.ext * (qpad + 3) + std::abs(q.mmin) + 64;
   if (base > 30000) return r;
   r.fast = true;
@@ -682,10 +682,18 @@ int launch_plain(ish_ctx *ctx, Query &q, RecordSet &rs, uint32_t first, uint32_t
   if (count == 0) return ISH_OK;
   int rc = build_plain(ctx, q);
   if (rc) return rc;
-  const int threads = 128;
-  const uint32_t blocks = std::max<uint32_t>(1, std::min<uint32_t>(ceil_div(count, threads), (uint32_t)ctx->num_sms * 4));
-  const uint32_t nth = blocks * threads;
-  CU(ctx->plain_scratch.ensure((size_t)2 * q.Q * nth * 4 + 16));
+  // the int16 form (the reference kernel's per-thread arrays and launch shape)
+  // when asked for and the query fits its largest array; else int32 columns
+  int qmax = 0;
+  if (ctx->kernel == ISH_KERNEL_PLAIN16 && q.Q <= PLAIN16_QMAX)
+    for (qmax = 64; qmax < q.Q; qmax <<= 1) {
+    }
+  const int threads = qmax ? 32 : 128;
+  const uint32_t blocks =
+      qmax ? ceil_div(PLAIN16_THREADS, threads)
+           : std::max<uint32_t>(1, std::min<uint32_t>(ceil_div(count, threads), (uint32_t)ctx->num_sms * 4));
+  const uint32_t nth = qmax ? PLAIN16_THREADS : blocks * threads;
+  if (!qmax) CU(ctx->plain_scratch.ensure((size_t)2 * q.Q * nth * 4 + 16));
   PlainParams p{};
   p.prof = q.plain_prof.as<const int16_t>();
   p.prof_bytes = (uint32_t)(((size_t)q.alphabet * q.Q * 2 + 15) & ~(size_t)15);
@@ -707,7 +715,7 @@ int launch_plain(ish_ctx *ctx, Query &q, RecordSet &rs, uint32_t first, uint32_t
   p.out = out;
   p.dec = Decision{q.max_score, q.thr};
   const size_t smem = p.use_smem ? p.prof_bytes : 0;
-  PlainFn fn = plain_fn(q.algo == ISH_ALGO_LOCAL ? SW : SG);
+  PlainFn fn = plain_fn(q.algo == ISH_ALGO_LOCAL ? SW : SG, qmax);
   CU(cudaFuncSetAttribute((const void *)fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)std::max<size_t>(smem, 1)));
   fn<<<blocks, threads, smem, ctx->stream>>>(p);
   ++ctx->launches;
@@ -772,7 +780,7 @@ bool wave_fits(const Query &q, int G, int K, int layout) {
 int launch_range(ish_ctx *ctx, Query &q, RecordSet &rs, uint32_t first, uint32_t count, OutDev out, cudaStream_t s) {
   int G, K, layout;
   pick_shape(ctx, q, &G, &K, &layout);
-  if (ctx->kernel == ISH_KERNEL_PLAIN || !wave_fits(q, G, K, layout)) {
+  if (ctx->kernel == ISH_KERNEL_PLAIN || ctx->kernel == ISH_KERNEL_PLAIN16 || !wave_fits(q, G, K, layout)) {
     if (s != ctx->stream) return fail(ctx, ISH_EINVAL, "the plain kernel runs on the context stream only");
     return launch_plain(ctx, q, rs, first, count, out);
   }
@@ -925,7 +933,8 @@ int ish_gpu_set_option(ish_ctx *ctx, int option, int64_t value) {
   if (ctx->server) return fail(ctx, ISH_EINVAL, "options cannot change while the serving loop runs");
   switch (option) {
   case ISH_OPT_KERNEL:
-    if (value < ISH_KERNEL_AUTO || value > ISH_KERNEL_EXACT) return fail(ctx, ISH_EINVAL, "bad kernel %lld", (long long)value);
+    if (value < ISH_KERNEL_AUTO || value > ISH_KERNEL_PLAIN16)
+      return fail(ctx, ISH_EINVAL, "bad kernel %lld", (long long)value);
     ctx->kernel = (int)value;
     return ISH_OK;
   case ISH_OPT_SG_LANES:

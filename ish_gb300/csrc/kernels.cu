@@ -314,16 +314,23 @@ __global__ void k_trivial(RecordsDev rec, uint32_t first, uint32_t count, int mo
 }
 
 // ---------------------------------------------------------------------------
-// The plain kernel: one thread per record, scalar int32 Gotoh with the query
-// on the inner loop -- the design of the reference's GPU kernel
+// The plain kernels: one thread per record, scalar Gotoh with the query on the
+// inner loop -- the design of the reference's GPU kernel
 // (ishlib/gpu/kernels/semi_global.mojo:20-115 with
 // ishlib/matcher/alignment/semi_global_aln/basic.mojo:242-425) made exact:
-// it applies the end rules of the striped CPU matchers.  Its H and E columns
-// live in a global scratch buffer, interleaved by thread for coalescing.
-// It is the one-query-per-launch comparison for the wavefront kernel.
+// they apply the end rules of the striped CPU matchers.  Two storage forms of
+// the H and E columns:
+//   QMAX = 0:  int32 columns in a global scratch buffer, interleaved by thread
+//              for coalescing, 128-thread blocks (any query length);
+//   QMAX > 0:  int16 per-thread arrays sized for queries up to QMAX residues,
+//              as the reference keeps InlineArray[NUM, max_query_length]
+//              (basic.mojo:305-306), launched as 15,000 threads in blocks of 32
+//              like the reference's default (ishlib/gpu/searcher_device.mojo:
+//              477-497).  Exact in the fast regime, where every value fits int16.
+// They are the one-query-per-launch comparison for the wavefront kernel.
 // ---------------------------------------------------------------------------
-template <int MODE>
-__global__ void __launch_bounds__(128) plain_kernel(const PlainParams p) {
+template <int MODE, int QMAX>
+__global__ void __launch_bounds__(QMAX ? 32 : 128) plain_kernel(const PlainParams p) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const int16_t *prof = p.prof;
   if (p.use_smem) {
@@ -340,6 +347,23 @@ __global__ void __launch_bounds__(128) plain_kernel(const PlainParams p) {
   const bool ts = p.ends & 4, te = p.ends & 8, qe = p.ends & 2;
   int32_t *Hc = p.scratch + gt;
   int32_t *Ec = p.scratch + (size_t)Q * nth + gt;
+  int16_t Hl[QMAX ? QMAX : 1], El[QMAX ? QMAX : 1];
+  auto ldH = [&](int q) -> int {
+    if constexpr (QMAX > 0) return Hl[q];
+    else return Hc[(size_t)q * nth];
+  };
+  auto ldE = [&](int q) -> int {
+    if constexpr (QMAX > 0) return El[q];
+    else return Ec[(size_t)q * nth];
+  };
+  auto stH = [&](int q, int v) {
+    if constexpr (QMAX > 0) Hl[q] = (int16_t)v;
+    else Hc[(size_t)q * nth] = v;
+  };
+  auto stE = [&](int q, int v) {
+    if constexpr (QMAX > 0) El[q] = (int16_t)v;
+    else Ec[(size_t)q * nth] = v;
+  };
   for (uint32_t s = gt; s < p.count; s += nth) {
     const uint32_t idx = p.first + s;
     const int T = (int)p.rec.len[idx];
@@ -347,8 +371,8 @@ __global__ void __launch_bounds__(128) plain_kernel(const PlainParams p) {
     const uint32_t orig = p.rec.orig[idx];
     for (int q = 0; q < Q; ++q) {
       const int h0 = p.hinit[q];
-      Hc[(size_t)q * nth] = h0;
-      Ec[(size_t)q * nth] = MODE == SW ? 0 : h0 - open;
+      stH(q, h0);
+      stE(q, MODE == SW ? 0 : h0 - open);
     }
     int best = MODE == SW ? 0 : p.neg_limit, er = -1, eq = MODE == SW ? 0 : Q - 1;
     int hlast = 0;
@@ -370,14 +394,14 @@ __global__ void __launch_bounds__(128) plain_kernel(const PlainParams p) {
       int colmax = 0, colq = 0;
       int h = 0;
       for (int q = 0; q < Q; ++q) {
-        const int e = Ec[(size_t)q * nth];
-        const int hold = Hc[(size_t)q * nth];
+        const int e = ldE(q);
+        const int hold = ldH(q);
         h = max(hdiag + prow[q], max(e, F));
         hdiag = hold;
-        Hc[(size_t)q * nth] = h;
+        stH(q, h);
         int v = h - open;
         if (MODE == SW) v = max(v, 0);
-        Ec[(size_t)q * nth] = max(e - ext, v);
+        stE(q, max(e - ext, v));
         F = max(F - ext, v);
         if (MODE == SW && h > colmax) {
           colmax = h;
@@ -413,7 +437,7 @@ __global__ void __launch_bounds__(128) plain_kernel(const PlainParams p) {
       qend = Q - 1;
       if (qe) {
         for (int q = 0; q < Q; ++q) {
-          const int v = Hc[(size_t)q * nth];
+          const int v = ldH(q);
           if (v > score) {
             score = v;
             qend = q;
@@ -431,7 +455,23 @@ __global__ void __launch_bounds__(128) plain_kernel(const PlainParams p) {
   }
 }
 
-PlainFn plain_fn(int mode) { return mode == SW ? (PlainFn)plain_kernel<SW> : (PlainFn)plain_kernel<SG>; }
+PlainFn plain_fn(int mode, int qmax) {
+  switch (qmax) {
+#define ISH_PLAIN(QM) \
+  case QM:            \
+    return mode == SW ? (PlainFn)plain_kernel<SW, QM> : (PlainFn)plain_kernel<SG, QM>;
+    ISH_PLAIN(0)
+    ISH_PLAIN(64)
+    ISH_PLAIN(128)
+    ISH_PLAIN(256)
+    ISH_PLAIN(512)
+    ISH_PLAIN(1024)
+    ISH_PLAIN(2048)
+#undef ISH_PLAIN
+    default:
+      return nullptr;
+  }
+}
 
 // ---------------------------------------------------------------------------
 // Hit compaction: indices of hit[i] != 0 in ascending order.

@@ -29,13 +29,35 @@ __global__ void k_scan64_block(const uint64_t *in, uint64_t *out, uint32_t n, ui
 __global__ void k_scan64_add(uint64_t *out, uint32_t n, const uint64_t *block_offsets);
 __global__ void k_trivial(RecordsDev rec, uint32_t first, uint32_t count, int mode, int qlen, OutDev out, Decision dec);
 typedef void (*PlainFn)(const PlainParams);
-PlainFn plain_fn(int mode);  // plain_kernel<SG> / plain_kernel<SW>
+// plain_kernel<mode, qmax>: qmax 0 (int32 columns in global scratch) or a
+// power of two 64..2048 (int16 per-thread columns); nullptr otherwise
+PlainFn plain_fn(int mode, int qmax);
+constexpr int PLAIN16_QMAX = 2048;     // longest query of the int16 plain kernel
+constexpr int PLAIN16_THREADS = 15000; // its launch: 15,000 threads in blocks of 32
 __global__ void k_count_hits(const uint8_t *hit, uint32_t n, uint32_t *block_counts);
 __global__ void k_scan_counts(uint32_t *counts, uint32_t nb, uint32_t *total);
 __global__ void k_dpx_peak(uint32_t *out, int iters, uint32_t b, uint32_t c);
 __global__ void k_write_hits(const uint8_t *hit, uint32_t n, const uint32_t *block_offsets, uint32_t *idx);
 __global__ void k_gather_hits(const uint32_t *idx, const uint32_t *count, const int32_t *score, const int32_t *qend,
                               const int32_t *tend, int32_t *hit_score, int32_t *hit_qend, int32_t *hit_tend);
+
+// Rows a wavefront thread computes per pipeline step.  A record's codes arrive
+// four to a 32-bit word, and everything beside the recurrence itself -- the
+// pipeline shuffles and control word, thread 0's work grab, the code refill,
+// the frame reset, the end-of-record test and the target-end maximum -- runs
+// once per step instead of once per row.  A pair's rows are rounded up to a
+// multiple of the rows per step (the rows past both records' ends feed nothing).
+// Semi-global row frames reset only at step boundaries, so the fast regime
+// keeps R >= WAVE_RPS_SG rows per frame period (gap_extend <= 512 at 4).
+// Chosen per mode from measurements (protein, K = 38): semi-global 4, local 2
+// (local alignment's per-row maximum and dominance state make four rows per
+// step cost more registers than they save).
+#ifndef WAVE_RPS_SG
+#define WAVE_RPS_SG 4
+#endif
+#ifndef WAVE_RPS_SW
+#define WAVE_RPS_SW 2
+#endif
 
 // Wavefront kernels are instantiated for K = 2, 4, ..., WAVE_KMAX columns per
 // thread, both modes and both profile layouts.

@@ -56,10 +56,13 @@ namespace ish {
 template <int K, int MODE, int LAYOUT>
 __device__ __forceinline__ void wave_rows(const WaveParams &p, const unsigned char *prof, uint32_t *slots_all,
                                           uint32_t *save_all, uint32_t *counter) {
+  constexpr int RPS = (MODE == SG) ? WAVE_RPS_SG : WAVE_RPS_SW;
+  static_assert(RPS == 2 || RPS == 4, "rows per step: 2 or 4");
   const int tid = threadIdx.x;
   const int G = p.G;
   const int lane = tid & 31;
   const int t = lane & (G - 1);
+  const bool t0 = t == 0;
   uint32_t *slots = slots_all + (tid / G) * 32;
   // local alignment: per thread, the H row of the last improvement of each lane
   constexpr int KP8 = (K + 7) & ~7;
@@ -72,7 +75,7 @@ __device__ __forceinline__ void wave_rows(const WaveParams &p, const unsigned ch
   const uint32_t VFLOOR = (MODE == SW) ? 0u : dup16(-32768);
   const uint32_t FS_IN = dup16(p.fin + p.open);  // F + open entering the padding
   // semi-global row frames: row r is held raised by frame = (r mod R) * ext
-  const uint32_t EOPEN = dup16(p.ext - p.open);                   // E' = max(T + ext - open, E)
+  const uint32_t EOPEN = dup16(p.ext - p.open);  // E' = max(T + ext - open, E)
   const uint32_t NEGMIN = dup16(-32768);
   const int f0 = (MODE == SG) ? p.ext : 0;  // row -1 sits in frame -ext
   const bool te = (MODE == SG) && (p.ends & 8);
@@ -81,12 +84,15 @@ __device__ __forceinline__ void wave_rows(const WaveParams &p, const unsigned ch
   const uint16_t *prof16 = reinterpret_cast<const uint16_t *>(prof);
   const uint32_t *prof32 = reinterpret_cast<const uint32_t *>(prof);
   const int col0 = t * K - p.d;  // query column of register 0
-  // parameters read every row, held in registers (the batched kernel's
+  // parameters read every step, held in registers (the batched kernel's
   // parameters live in shared memory)
   const int kp = p.kp, alpha = p.alphabet, fmask = p.frame_mask, ext = p.ext, hleft = p.hleft;
   const uint32_t remap_off = p.remap_off, lane_mul = p.lane_mul;
   // the frame of a row (always 0 for local alignment)
   auto frame_of = [&](int r) { return (MODE == SG) ? (r & fmask) * ext : 0; };
+  // +ext in both 16-bit halves: added to a boundary value hleft + frame
+  // (hleft 0 or NEG_BIG, frames <= 2048), the low half never carries
+  const uint32_t EXT2 = (MODE == SG) ? (uint32_t)ext * 0x10001u : 0u;
 
   uint32_t H[K], E[K];
 #pragma unroll
@@ -94,9 +100,15 @@ __device__ __forceinline__ void wave_rows(const WaveParams &p, const unsigned ch
     H[j] = 0;
     E[j] = 0;
   }
-  uint32_t prevH = 0, outH = 0, outF = 0, outC = CTL_IDLE;
-  uint32_t outBest = 0;  // local alignment: best cell so far in this thread's and all earlier columns
-  int row = 0, lenA = 0, lenB = 0, lastA_row = -1, lastB_row = -1;
+  uint32_t prevH = 0;  // H(row above the step's first row, column col0 - 1)
+  // per row of the step, passed to thread t+1: H of the last column, F + open
+  // leaving it, and (local alignment) the running best of this thread's and
+  // all earlier columns
+  uint32_t outH[RPS], outF[RPS], outB[RPS];
+#pragma unroll
+  for (int k = 0; k < RPS; ++k) outH[k] = outF[k] = outB[k] = 0;
+  uint32_t outC = CTL_IDLE;
+  int q4 = 0, lenA = 0, lenB = 0, lastA_row = -1, lastB_row = -1;  // q4: row of the step's first row
   uint32_t pr = 0;
   // this thread's record streams: 4 codes per 32-bit word, one word ahead
   const uint8_t *pa = nullptr, *pb = nullptr;
@@ -105,9 +117,10 @@ __device__ __forceinline__ void wave_rows(const WaveParams &p, const unsigned ch
   uint32_t best = 0;         // SG: lane-wise running max of H(i, Q-1); SW: of this thread's cells
   int rowA = -1, rowB = -1;  // first row of the lane's maximum
   uint32_t oR0 = 0, oR1 = 0, oR2 = 0, oR3 = 0;  // last-row partials for thread t+1
+  uint32_t iR0 = 0, iR1 = 0, iR2 = 0, iR3 = 0;  // ... and those of thread t-1
   bool has_out = false;
-  // thread 0 of the group grabs record pairs: f_left rows of the current pair
-  // are still to start, f_ctl is the control word of the next row
+  // thread 0 of the group grabs record pairs: f_left steps of the current pair
+  // are still to start, f_ctl is the control word of the next step
   bool f_done = false;
   int f_left = 0;
   uint32_t f_ctl = CTL_IDLE;
@@ -116,16 +129,293 @@ __device__ __forceinline__ void wave_rows(const WaveParams &p, const unsigned ch
   int ev_row = -3;
   const bool remap = remap_off != 0;
   uint64_t steps = 0;
-  int chk = 8;
+  constexpr int CHK = 8 / RPS;  // steps between termination checks
+  int chk = CHK;
+
+  // One row of the pair with record codes cA, cB: `diag` is H of the row above
+  // at column col0 - 1, `fs` is F + open entering column col0.  Updates H and
+  // E in place and returns F + open leaving the thread's last column.
+  auto row_step = [&](uint32_t cA, uint32_t cB, uint32_t diag, uint32_t fs) -> uint32_t {
+    if (remap) {  // codes that score alike share a profile row
+      cA = prof[remap_off + cA];
+      cB = prof[remap_off + cB];
+    }
+    uint32_t P[K];
+    if (LAYOUT == PROF_PAIR) {
+      const uint4 *r4 = reinterpret_cast<const uint4 *>(prof32 + ((cA * alpha + cB) * G + t) * kp);
+#pragma unroll
+      for (int v = 0; v < (K + 3) / 4; ++v) {
+        const uint4 w = r4[v];
+        if (4 * v + 0 < K) P[4 * v + 0] = w.x;
+        if (4 * v + 1 < K) P[4 * v + 1] = w.y;
+        if (4 * v + 2 < K) P[4 * v + 2] = w.z;
+        if (4 * v + 3 < K) P[4 * v + 3] = w.w;
+      }
+    } else if (LAYOUT == PROF_S32) {
+      // 32-bit words holding the 16-bit score in the low half; the packed
+      // pair is b * 65536 + a, one integer multiply-add (the multiplier is a
+      // runtime value, so this stays an IMAD on the FMA pipe, which the DPX
+      // recurrence on the ALU pipe leaves idle)
+      const uint4 *ra = reinterpret_cast<const uint4 *>(prof32 + (cA * G + t) * kp);
+      const uint4 *rb = reinterpret_cast<const uint4 *>(prof32 + (cB * G + t) * kp);
+      const uint32_t mul = lane_mul;
+#pragma unroll
+      for (int v = 0; v < (K + 3) / 4; ++v) {
+        const uint4 a = ra[v], b = rb[v];
+        if (4 * v + 0 < K) P[4 * v + 0] = b.x * mul + a.x;
+        if (4 * v + 1 < K) P[4 * v + 1] = b.y * mul + a.y;
+        if (4 * v + 2 < K) P[4 * v + 2] = b.z * mul + a.z;
+        if (4 * v + 3 < K) P[4 * v + 3] = b.w * mul + a.w;
+      }
+    } else {
+      // 16-bit words (profiles too large for the 32-bit layout): one PRMT
+      // per packed pair
+      const uint4 *ra = reinterpret_cast<const uint4 *>(prof16 + (cA * G + t) * kp);
+      const uint4 *rb = reinterpret_cast<const uint4 *>(prof16 + (cB * G + t) * kp);
+#pragma unroll
+      for (int v = 0; v < (K + 7) / 8; ++v) {
+        const uint4 a = ra[v], b = rb[v];
+        const uint32_t aw[4] = {a.x, a.y, a.z, a.w}, bw[4] = {b.x, b.y, b.z, b.w};
+#pragma unroll
+        for (int m = 0; m < 4; ++m) {
+          if (8 * v + 2 * m < K) P[8 * v + 2 * m] = __byte_perm(aw[m], bw[m], 0x5410);
+          if (8 * v + 2 * m + 1 < K) P[8 * v + 2 * m + 1] = __byte_perm(aw[m], bw[m], 0x7632);
+        }
+      }
+    }
+    // backward pass (columns independent), then the F chain
+#pragma unroll
+    for (int j = K - 1; j >= 0; --j) {
+      const uint32_t T = __viaddmax_s16x2(j == 0 ? diag : H[j - 1], P[j], E[j]);
+      if (MODE == SG) {
+        E[j] = __viaddmax_s16x2(T, EOPEN, E[j]);  // in the row frames (see the header)
+      } else {
+        const uint32_t u = __viaddmax_s16x2(T, NOPEN, VFLOOR);
+        E[j] = __viaddmax_s16x2(E[j], NEXT, u);
+      }
+      H[j] = T;
+    }
+#pragma unroll
+    for (int j = 0; j < K; ++j) {
+      const uint32_t T = H[j];
+      H[j] = __viaddmax_s16x2(fs, NOPEN, T);
+      fs = __viaddmax_s16x2(fs, NEXT, T);
+    }
+    return fs;
+  };
+
+  // Local alignment, after row `row`: only a row maximum above every cell so
+  // far in this thread AND in all columns to its left (`left`, their running
+  // best up to this row, passed along the pipeline) can be the first row of
+  // the record's maximum at its smallest column; anything else is dominated
+  // (smaller, or equal in an earlier row or a smaller column), so only those
+  // improvements are recorded.  Returns the running best passed on.
+  auto sw_track = [&](int row, uint32_t left) -> uint32_t {
+    uint32_t cm = H[0];
+#pragma unroll
+    for (int j = 1; j + 1 < K; j += 2) cm = __vimax3_s16x2(cm, H[j], H[j + 1]);
+    if ((K & 1) == 0 && K > 1) cm = __viaddmax_s16x2(cm, 0u, H[K - 1]);
+    const uint32_t thr = __viaddmax_s16x2(best, 0u, left);
+    const uint32_t nb = __viaddmax_s16x2(thr, 0u, cm);
+    if (nb != thr) {
+      // keep this row (shared-memory stores only); the column of the maximum
+      // is looked up once, at the record's last row
+      const bool upA = lo16(cm) > lo16(thr), upB = hi16(cm) > hi16(thr);
+      // the improving lane's halves of the row: one PRMT per two columns
+#define ISH_H(j) ((j) < K ? H[(j) < K ? (j) : 0] : 0u)
+      if (upA) {
+#pragma unroll
+        for (int v = 0; v < KP8 / 8; ++v)
+          reinterpret_cast<uint4 *>(saveA)[v] =
+              make_uint4(__byte_perm(ISH_H(8 * v), ISH_H(8 * v + 1), 0x5410),
+                         __byte_perm(ISH_H(8 * v + 2), ISH_H(8 * v + 3), 0x5410),
+                         __byte_perm(ISH_H(8 * v + 4), ISH_H(8 * v + 5), 0x5410),
+                         __byte_perm(ISH_H(8 * v + 6), ISH_H(8 * v + 7), 0x5410));
+      }
+      if (upB) {
+#pragma unroll
+        for (int v = 0; v < KP8 / 8; ++v)
+          reinterpret_cast<uint4 *>(saveB)[v] =
+              make_uint4(__byte_perm(ISH_H(8 * v), ISH_H(8 * v + 1), 0x7632),
+                         __byte_perm(ISH_H(8 * v + 2), ISH_H(8 * v + 3), 0x7632),
+                         __byte_perm(ISH_H(8 * v + 4), ISH_H(8 * v + 5), 0x7632),
+                         __byte_perm(ISH_H(8 * v + 6), ISH_H(8 * v + 7), 0x7632));
+      }
+#undef ISH_H
+      if (upA) rowA = row;
+      if (upB) rowB = row;
+      best = ((upA ? cm : best) & 0xffffu) | ((upB ? cm : best) & 0xffff0000u);
+    }
+    return nb;
+  };
+
+  // Semi-global, target end free, one row: the running max of column Q-1
+  // (register K-1 of thread G-1); a strict improvement records the row, so
+  // the FIRST row of the maximum wins.
+  auto te_row = [&](int row) {
+    const uint32_t nb = __viaddmax_s16x2(best, 0u, __viaddmax_s16x2(H[K - 1], dup16(-frame_of(row)), NEGMIN));
+    if (nb != best) {
+      if (lo16(nb) != lo16(best)) rowA = row;
+      if (hi16(nb) != hi16(best)) rowB = row;
+      best = nb;
+    }
+  };
+
+  // o takes v's 16-bit half of each lane whose record ends now
+  auto put_lanes = [](uint32_t &o, uint32_t v, bool a, bool b) {
+    o = (a ? (v & 0xffffu) : (o & 0xffffu)) | (b ? (v & 0xffff0000u) : (o & 0xffff0000u));
+  };
+
+  // The last row of one or both records of the pair (H holds it): fold the
+  // partial results left to right -- thread t-1's arrived as iR at the start
+  // of this step, this thread's leave as oR at the next -- and thread G-1
+  // writes the record's outputs.
+  auto on_event = [&](int row) {
+    const bool lastA = row == lastA_row, lastB = row == lastB_row;
+    {  // the other record's end, if it is still ahead
+      int nxt = lastA_row > row ? lastA_row : -3;
+      if (lastB_row > row && (nxt < 0 || lastB_row < nxt)) nxt = lastB_row;
+      ev_row = nxt;
+    }
+    if (MODE == SG) {
+      uint32_t mx = 0, mq = 0;
+      if (qe) {
+        int bA = -32768, bB = -32768, qA = 0x7fff, qB = 0x7fff;
+        uint32_t row_h[K];  // staged as in the local-alignment scan
+#pragma unroll
+        for (int j = 0; j < K; ++j) row_h[j] = H[j];
+#pragma unroll 1
+        for (int j = 0; j < K; ++j) {
+          if (col0 + j >= 0) {
+            const int a = lo16(row_h[j]), b = hi16(row_h[j]);
+            if (a > bA) {
+              bA = a;
+              qA = col0 + j;
+            }
+            if (b > bB) {
+              bB = b;
+              qB = col0 + j;
+            }
+          }
+        }
+        if (t > 0) {  // columns to the left win ties
+          if (!(bA > lo16(iR0))) {
+            bA = lo16(iR0);
+            qA = (int)(iR1 & 0xffffu);
+          }
+          if (!(bB > hi16(iR0))) {
+            bB = hi16(iR0);
+            qB = (int)(iR1 >> 16);
+          }
+        }
+        mx = (uint32_t)(bA & 0xffff) | ((uint32_t)bB << 16);
+        mq = (uint32_t)qA | ((uint32_t)qB << 16);
+        if (t < G - 1) {
+          put_lanes(oR0, mx, lastA, lastB);
+          put_lanes(oR1, mq, lastA, lastB);
+          has_out = true;
+        }
+      }
+      if (t == G - 1) {
+#pragma unroll
+        for (int x = 0; x < 2; ++x) {
+          if (!(x == 0 ? lastA : lastB)) continue;
+          const uint32_t orig = p.rec.orig[p.first + 2 * pr + x];
+          const int T = x == 0 ? lenA : lenB;
+          int score, er, eq = p.Q - 1;
+          if (!te && !qe) {
+            score = (x == 0 ? lo16(H[K - 1]) : hi16(H[K - 1])) - frame_of(row);  // this row's H(i, Q-1)
+            er = T - 1;
+          } else {
+            score = te ? (x == 0 ? lo16(best) : hi16(best)) : p.neg_limit;
+            er = x == 0 ? rowA : rowB;
+            if (qe) {
+              const int s1 = (x == 0 ? lo16(mx) : hi16(mx)) - frame_of(row);
+              const int t1 = x == 0 ? (int)(mq & 0xffffu) : (int)(mq >> 16);
+              if (s1 > score) {
+                score = s1;
+                er = T - 1;
+                eq = t1;
+              } else if (s1 == score && er == T - 1 && t1 < eq) {
+                eq = t1;
+              }
+            }
+          }
+          if (p.out.score) p.out.score[orig] = score;
+          if (p.out.qend) p.out.qend[orig] = eq;
+          if (p.out.tend) p.out.tend[orig] = er;
+          if (p.out.hit) p.out.hit[orig] = decide(SG, score, eq, er, p.dec);
+        }
+      }
+    } else {
+      int bA = lo16(best), bB = hi16(best), rA = rowA, rB = rowB, qA = 0x7fff, qB = 0x7fff;
+      // smallest column of this thread's maximum in its first row
+#pragma unroll 1
+      for (int j = K - 1; j >= 0; --j) {
+        if (bA > 0 && (int)(int16_t)saveA[j] == bA) qA = col0 + j;
+        if (bB > 0 && (int)(int16_t)saveB[j] == bB) qB = col0 + j;
+      }
+      if (t > 0) {
+        const int ia = lo16(iR0), ib = hi16(iR0), ira = (int)iR2, irb = (int)iR3;
+        const int iqa = (int)(int16_t)(iR1 & 0xffffu), iqb = (int)(int16_t)(iR1 >> 16);
+        if (ia > bA || (ia == bA && (ira < rA || (ira == rA && iqa < qA)))) {
+          bA = ia;
+          rA = ira;
+          qA = iqa;
+        }
+        if (ib > bB || (ib == bB && (irb < rB || (irb == rB && iqb < qB)))) {
+          bB = ib;
+          rB = irb;
+          qB = iqb;
+        }
+      }
+      if (t < G - 1) {
+        put_lanes(oR0, (uint32_t)(bA & 0xffff) | ((uint32_t)bB << 16), lastA, lastB);
+        put_lanes(oR1, (uint32_t)(qA & 0xffff) | ((uint32_t)qB << 16), lastA, lastB);
+        if (lastA) oR2 = (uint32_t)rA;
+        if (lastB) oR3 = (uint32_t)rB;
+        has_out = true;
+      } else {
+#pragma unroll
+        for (int x = 0; x < 2; ++x) {
+          if (!(x == 0 ? lastA : lastB)) continue;
+          const uint32_t orig = p.rec.orig[p.first + 2 * pr + x];
+          int score = x == 0 ? bA : bB, er = x == 0 ? rA : rB, eq = x == 0 ? qA : qB;
+          if (score == 0) {
+            er = -1;
+            eq = 0;
+          }
+          if (p.out.score) p.out.score[orig] = score;
+          if (p.out.qend) p.out.qend[orig] = eq;
+          if (p.out.tend) p.out.tend[orig] = er;
+          if (p.out.hit) p.out.hit[orig] = decide(SW, score, eq, er, p.dec);
+        }
+      }
+    }
+  };
 
   while (true) {
     __syncwarp();
-    const uint32_t msgH = __shfl_up_sync(FULL, outH, 1, G);
-    const uint32_t msgF = __shfl_up_sync(FULL, outF, 1, G);
+    uint32_t msgH[RPS], msgF[RPS], msgB[RPS];
+#pragma unroll
+    for (int k = 0; k < RPS; ++k) {
+      msgH[k] = __shfl_up_sync(FULL, outH[k], 1, G);
+      msgF[k] = __shfl_up_sync(FULL, outF[k], 1, G);
+      msgB[k] = (MODE == SW) ? __shfl_up_sync(FULL, outB[k], 1, G) : 0u;
+    }
     uint32_t msgC = __shfl_up_sync(FULL, outC, 1, G);
-    const uint32_t msgBest = (MODE == SW) ? __shfl_up_sync(FULL, outBest, 1, G) : 0u;
+    // partial results of records that ended in thread t-1's previous step
+    if (__any_sync(FULL, has_out)) {
+      iR0 = __shfl_up_sync(FULL, oR0, 1, G);
+      iR1 = __shfl_up_sync(FULL, oR1, 1, G);
+      if (MODE == SW) {
+        iR2 = __shfl_up_sync(FULL, oR2, 1, G);
+        iR3 = __shfl_up_sync(FULL, oR3, 1, G);
+      }
+      has_out = false;
+    }
 
-    if (t == 0) {
+    if (t0) {
       if (f_left <= 0 && !f_done) {
         const uint32_t np = atomicAdd(counter, 1u);
         if (np < npairs) {
@@ -134,7 +424,7 @@ __device__ __forceinline__ void wave_rows(const WaveParams &p, const unsigned ch
           const uint32_t sA = p.first + 2 * np;
           const int na = (int)p.rec.len[sA];
           const int nb = (2 * np + 1 < p.count) ? (int)p.rec.len[sA + 1] : 0;
-          f_left = max(max(na, nb), 1);
+          f_left = (max(max(na, nb), 1) + RPS - 1) / RPS;
           f_ctl = CTL_NEW | (f_seq << CTL_SEQ_SHIFT);
         } else {
           f_done = true;
@@ -173,16 +463,16 @@ __device__ __forceinline__ void wave_rows(const WaveParams &p, const unsigned ch
           H[j] = dup16(h0 - f0);
           E[j] = (MODE == SW) ? 0u : dup16(h0 - p.open);
         }
-        prevH = (t == 0) ? dup16(p.hleft - f0) : dup16(p.hinit[t * K - 1] - f0);
+        prevH = t0 ? dup16(p.hleft - f0) : dup16(p.hinit[t * K - 1] - f0);
         best = (MODE == SW) ? 0u : dup16(p.neg_limit);
         rowA = rowB = -1;
-        row = 0;
+        q4 = 0;
       } else {
-        ++row;
+        q4 += RPS;
         if (MODE == SG) {
-          if ((row & fmask) == 0) {
-            // frame R*ext -> 0: lower what this row takes from the row above
-            const uint32_t FRAME_DROP = dup16(-(p.frame_mask + 1) * p.ext);
+          if ((q4 & fmask) == 0) {
+            // frame R*ext -> 0: lower what this step takes from the row above
+            const uint32_t FRAME_DROP = dup16(-(fmask + 1) * ext);
 #pragma unroll
             for (int j = 0; j < K; ++j) {
               H[j] = __viaddmax_s16x2(H[j], FRAME_DROP, NEGMIN);
@@ -192,321 +482,119 @@ __device__ __forceinline__ void wave_rows(const WaveParams &p, const unsigned ch
           }
         }
       }
-
-      // ---- record codes of this row ----
+      // ---- record codes of this step ----
       // Codes were checked against the alphabet when the set was loaded and
       // every record slot is zero-padded to 16 bytes.  Past a record's end the
       // last word repeats: those rows only feed a lane whose result is final.
-      uint32_t P[K];
-      {
-        // A new code word every 4 rows.  The threads of a group sit on
-        // different rows, so a conditional block here diverges every row;
-        // for the shapes where it measured faster the refill is written as
-        // selects and guarded loads instead (semi-global K <= 24 and >= 34:
-        // +1 to +3.4 %; local K <= 24 and >= 50), elsewhere the extra live
-        // registers cost more than the branch saves.
-        constexpr bool SELECT_REFILL = (MODE == SG) ? (K <= 24 || K >= 34) : (K <= 24 || K >= 50);
+      if (RPS == 4 || (q4 & 3) == 0) {
+        wA = nA;
+        wB = nB;
+        if (q4 + 4 < lenA) nA = __ldg(reinterpret_cast<const uint32_t *>(pa + q4 + 4));
+        if (q4 + 4 < lenB) nB = __ldg(reinterpret_cast<const uint32_t *>(pb + q4 + 4));
         // long records: the codes 256 rows ahead are pulled into L1, so the
         // group's loads hit L1 even when few warps are left to hide latency
-        if constexpr (SELECT_REFILL) {
-          const bool refill = (row & 3) == 0;
-          wA = refill ? nA : wA;
-          wB = refill ? nB : wB;
-          if (refill && row + 4 < lenA) nA = __ldg(reinterpret_cast<const uint32_t *>(pa + row + 4));
-          if (refill && row + 4 < lenB) nB = __ldg(reinterpret_cast<const uint32_t *>(pb + row + 4));
-          const bool pf = (row & 127) == 0;
-          if (pf && row + 256 < lenA) asm volatile("prefetch.global.L1 [%0];" ::"l"(pa + row + 256));
-          if (pf && row + 256 < lenB) asm volatile("prefetch.global.L1 [%0];" ::"l"(pb + row + 256));
-        } else if ((row & 3) == 0) {
-          wA = nA;
-          wB = nB;
-          if (row + 4 < lenA) nA = __ldg(reinterpret_cast<const uint32_t *>(pa + row + 4));
-          if (row + 4 < lenB) nB = __ldg(reinterpret_cast<const uint32_t *>(pb + row + 4));
-          if ((row & 127) == 0) {
-            if (row + 256 < lenA) asm volatile("prefetch.global.L1 [%0];" ::"l"(pa + row + 256));
-            if (row + 256 < lenB) asm volatile("prefetch.global.L1 [%0];" ::"l"(pb + row + 256));
-          }
+        if ((q4 & 127) == 0) {
+          if (q4 + 256 < lenA) asm volatile("prefetch.global.L1 [%0];" ::"l"(pa + q4 + 256));
+          if (q4 + 256 < lenB) asm volatile("prefetch.global.L1 [%0];" ::"l"(pb + q4 + 256));
         }
-        uint32_t cA = wA & 0xffu, cB = wB & 0xffu;
-        if (remap) {  // codes that score alike share a profile row
-          cA = prof[remap_off + cA];
-          cB = prof[remap_off + cB];
+      } else {
+        wA >>= 16;
+        wB >>= 16;
+      }
+      // thread 0: what enters the padding from the left, H = hleft in the
+      // row's frame and F = -infinity (semi-global) / 0 (local)
+      if (t0) {
+        const uint32_t hf = dup16(hleft + frame_of(q4));
+#pragma unroll
+        for (int k = 0; k < RPS; ++k) {
+          msgH[k] = hf + (uint32_t)k * EXT2;
+          msgF[k] = FS_IN;
+          msgB[k] = 0u;
         }
-        wA >>= 8;
-        wB >>= 8;
-        if (LAYOUT == PROF_PAIR) {
-          const uint4 *r4 = reinterpret_cast<const uint4 *>(prof32 + ((cA * alpha + cB) * G + t) * kp);
+      }
+    }
+    // whether a record of the warp ends in this step's rows (warp-uniform)
+    const bool slow = __any_sync(FULL, busy && (unsigned)(ev_row - q4) < (unsigned)RPS);
+
+    if (busy) {
+      if (!slow) {
+        // ---- the step's rows, no record ending ----
 #pragma unroll
-          for (int v = 0; v < (K + 3) / 4; ++v) {
-            const uint4 w = r4[v];
-            if (4 * v + 0 < K) P[4 * v + 0] = w.x;
-            if (4 * v + 1 < K) P[4 * v + 1] = w.y;
-            if (4 * v + 2 < K) P[4 * v + 2] = w.z;
-            if (4 * v + 3 < K) P[4 * v + 3] = w.w;
-          }
-        } else if (LAYOUT == PROF_S32) {
-          // 32-bit words holding the 16-bit score in the low half; the packed
-          // pair is b * 65536 + a, one integer multiply-add (the multiplier is
-          // a runtime value, so this stays an IMAD on the FMA pipe, which the
-          // DPX recurrence on the ALU pipe leaves idle)
-          const uint4 *ra = reinterpret_cast<const uint4 *>(prof32 + (cA * G + t) * kp);
-          const uint4 *rb = reinterpret_cast<const uint4 *>(prof32 + (cB * G + t) * kp);
-          const uint32_t mul = lane_mul;
+        for (int k = 0; k < RPS; ++k) {
+          const uint32_t fs = row_step(__byte_perm(wA, 0u, 0x4440 + k), __byte_perm(wB, 0u, 0x4440 + k),
+                                       k == 0 ? prevH : msgH[k - 1], msgF[k]);
+          outH[k] = H[K - 1];
+          outF[k] = fs;
+          if (MODE == SW) outB[k] = sw_track(q4 + k, msgB[k]);
+        }
+        prevH = msgH[RPS - 1];
+        if (te) {
+          // the largest H(., Q-1) of the step's rows without their frames
+          // (frame(q4 + k) = frame(q4) + k * ext): m = max_k outH[k] - k * ext
+          uint32_t m = outH[RPS - 1];
 #pragma unroll
-          for (int v = 0; v < (K + 3) / 4; ++v) {
-            const uint4 a = ra[v], b = rb[v];
-            if (4 * v + 0 < K) P[4 * v + 0] = b.x * mul + a.x;
-            if (4 * v + 1 < K) P[4 * v + 1] = b.y * mul + a.y;
-            if (4 * v + 2 < K) P[4 * v + 2] = b.z * mul + a.z;
-            if (4 * v + 3 < K) P[4 * v + 3] = b.w * mul + a.w;
-          }
-        } else {
-          // 16-bit words (profiles too large for the 32-bit layout): one PRMT
-          // per packed pair
-          const uint4 *ra = reinterpret_cast<const uint4 *>(prof16 + (cA * G + t) * kp);
-          const uint4 *rb = reinterpret_cast<const uint4 *>(prof16 + (cB * G + t) * kp);
+          for (int k = RPS - 2; k >= 0; --k) m = __viaddmax_s16x2(m, NEXT, outH[k]);
+          const uint32_t nb = __viaddmax_s16x2(m, dup16(-frame_of(q4)), best);
+          if (nb != best) {
+            // the first row reaching the new maximum, per improved lane
+            bool dA = lo16(nb) == lo16(best), dB = hi16(nb) == hi16(best);
 #pragma unroll
-          for (int v = 0; v < (K + 7) / 8; ++v) {
-            const uint4 a = ra[v], b = rb[v];
-            const uint32_t aw[4] = {a.x, a.y, a.z, a.w}, bw[4] = {b.x, b.y, b.z, b.w};
-#pragma unroll
-            for (int m = 0; m < 4; ++m) {
-              if (8 * v + 2 * m < K) P[8 * v + 2 * m] = __byte_perm(aw[m], bw[m], 0x5410);
-              if (8 * v + 2 * m + 1 < K) P[8 * v + 2 * m + 1] = __byte_perm(aw[m], bw[m], 0x7632);
+            for (int k = 0; k < RPS; ++k) {
+              const uint32_t u = __viaddmax_s16x2(outH[k], dup16(-frame_of(q4 + k)), NEGMIN);
+              if (!dA && lo16(u) == lo16(nb)) {
+                rowA = q4 + k;
+                dA = true;
+              }
+              if (!dB && hi16(u) == hi16(nb)) {
+                rowB = q4 + k;
+                dB = true;
+              }
             }
+            best = nb;
           }
         }
-      }
-
-      // ---- the row: backward pass (columns independent), then the F chain ----
+      } else {
+        // ---- a record of the warp ends in these rows: one row at a time,
+        // with the end-of-record work after its last row ----
+        uint32_t d = prevH, sA = wA, sB = wB;
+#pragma unroll 1
+        for (int k = 0; k < RPS; ++k) {
+          const int row = q4 + k;
+          const uint32_t fs = row_step(sA & 0xffu, sB & 0xffu, d, msgF[0]);
+          sA >>= 8;
+          sB >>= 8;
+          d = msgH[0];
+          const uint32_t left = msgB[0];
 #pragma unroll
-      for (int j = K - 1; j >= 0; --j) {
-        const uint32_t T = __viaddmax_s16x2(j == 0 ? prevH : H[j - 1], P[j], E[j]);
-        if (MODE == SG) {
-          E[j] = __viaddmax_s16x2(T, EOPEN, E[j]);  // in the row frames (see the header)
-        } else {
-          const uint32_t u = __viaddmax_s16x2(T, NOPEN, VFLOOR);
-          E[j] = __viaddmax_s16x2(E[j], NEXT, u);
+          for (int j = 0; j + 1 < RPS; ++j) {
+            msgH[j] = msgH[j + 1];
+            msgF[j] = msgF[j + 1];
+            msgB[j] = msgB[j + 1];
+            outH[j] = outH[j + 1];
+            outF[j] = outF[j + 1];
+            outB[j] = outB[j + 1];
+          }
+          outH[RPS - 1] = H[K - 1];
+          outF[RPS - 1] = fs;
+          if (MODE == SW) outB[RPS - 1] = sw_track(row, left);
+          if (te) te_row(row);
+          if (row == ev_row) on_event(row);
         }
-        H[j] = T;
+        prevH = d;
       }
-      uint32_t Fs = (t == 0) ? FS_IN : msgF;
-#pragma unroll
-      for (int j = 0; j < K; ++j) {
-        const uint32_t T = H[j];
-        H[j] = __viaddmax_s16x2(Fs, NOPEN, T);
-        Fs = __viaddmax_s16x2(Fs, NEXT, T);
-      }
-      prevH = (t == 0) ? dup16(hleft + frame_of(row)) : msgH;  // this row's H left of column 0
-      outH = H[K - 1];
-      outF = Fs;
       outC = msgC;
-
-      if (MODE == SW) {
-        uint32_t cm = H[0];
-#pragma unroll
-        for (int j = 1; j + 1 < K; j += 2) cm = __vimax3_s16x2(cm, H[j], H[j + 1]);
-        if ((K & 1) == 0 && K > 1) cm = __viaddmax_s16x2(cm, 0u, H[K - 1]);
-        // Only a row maximum above every cell so far in this thread AND in
-        // all columns to its left (`left`, the running best passed along the
-        // pipeline for this row) can be the first row of the record's
-        // maximum at its smallest column; anything else is dominated
-        // (smaller, or equal in an earlier row or a smaller column), so only
-        // those improvements are recorded.
-        const uint32_t left = (t == 0) ? 0u : msgBest;
-        const uint32_t thr = __viaddmax_s16x2(best, 0u, left);
-        const uint32_t nb = __viaddmax_s16x2(thr, 0u, cm);
-        outBest = nb;
-        if (nb != thr) {
-          // keep this row (shared-memory stores only); the column of the
-          // maximum is looked up once, at the record's last row
-          const bool upA = lo16(cm) > lo16(thr), upB = hi16(cm) > hi16(thr);
-          // the improving lane's halves of the row: one PRMT per two columns
-#define ISH_H(j) ((j) < K ? H[(j) < K ? (j) : 0] : 0u)
-          if (upA) {
-#pragma unroll
-            for (int v = 0; v < KP8 / 8; ++v)
-              reinterpret_cast<uint4 *>(saveA)[v] =
-                  make_uint4(__byte_perm(ISH_H(8 * v), ISH_H(8 * v + 1), 0x5410),
-                             __byte_perm(ISH_H(8 * v + 2), ISH_H(8 * v + 3), 0x5410),
-                             __byte_perm(ISH_H(8 * v + 4), ISH_H(8 * v + 5), 0x5410),
-                             __byte_perm(ISH_H(8 * v + 6), ISH_H(8 * v + 7), 0x5410));
-          }
-          if (upB) {
-#pragma unroll
-            for (int v = 0; v < KP8 / 8; ++v)
-              reinterpret_cast<uint4 *>(saveB)[v] =
-                  make_uint4(__byte_perm(ISH_H(8 * v), ISH_H(8 * v + 1), 0x7632),
-                             __byte_perm(ISH_H(8 * v + 2), ISH_H(8 * v + 3), 0x7632),
-                             __byte_perm(ISH_H(8 * v + 4), ISH_H(8 * v + 5), 0x7632),
-                             __byte_perm(ISH_H(8 * v + 6), ISH_H(8 * v + 7), 0x7632));
-          }
-#undef ISH_H
-          if (upA) rowA = row;
-          if (upB) rowB = row;
-          best = ((upA ? cm : best) & 0xffffu) | ((upB ? cm : best) & 0xffff0000u);
-        }
-      }
-
-      if (MODE == SG && te) {
-        // running max of column Q-1 (register K-1 of thread G-1); a strict
-        // improvement records the row, so the FIRST row of the maximum wins
-        const uint32_t nb = __viaddmax_s16x2(best, 0u, __viaddmax_s16x2(H[K - 1], dup16(-frame_of(row)), NEGMIN));
-        if (nb != best) {
-          if (lo16(nb) != lo16(best)) rowA = row;
-          if (hi16(nb) != hi16(best)) rowB = row;
-          best = nb;
-        }
-      }
     } else {
       outC = CTL_IDLE;
     }
 
-    // ---- last row of a record: fold partial results left to right ----
-    // (a handled end moves ev_row on, so an idle thread never sees it again)
-    const bool ev = row == ev_row;
-    if (__any_sync(FULL, ev || has_out)) {
-      const bool lastA = ev && row == lastA_row, lastB = ev && row == lastB_row;
-      if (ev) {  // the other record's end, if it is still ahead
-        int nxt = lastA_row > row ? lastA_row : -3;
-        if (lastB_row > row && (nxt < 0 || lastB_row < nxt)) nxt = lastB_row;
-        ev_row = nxt;
-      }
-      const uint32_t iR0 = __shfl_up_sync(FULL, oR0, 1, G);
-      const uint32_t iR1 = __shfl_up_sync(FULL, oR1, 1, G);
-      uint32_t iR2 = 0, iR3 = 0;
-      if (MODE == SW) {
-        iR2 = __shfl_up_sync(FULL, oR2, 1, G);
-        iR3 = __shfl_up_sync(FULL, oR3, 1, G);
-      }
-      has_out = false;
-      if (lastA || lastB) {
-        if (MODE == SG) {
-          uint32_t mx = 0, mq = 0;
-          if (qe) {
-            int bA = -32768, bB = -32768, qA = 0x7fff, qB = 0x7fff;
-            uint32_t row_h[K];  // staged as in the local-alignment scan
-#pragma unroll
-            for (int j = 0; j < K; ++j) row_h[j] = H[j];
-#pragma unroll 1
-            for (int j = 0; j < K; ++j) {
-              if (col0 + j >= 0) {
-                const int a = lo16(row_h[j]), b = hi16(row_h[j]);
-                if (a > bA) {
-                  bA = a;
-                  qA = col0 + j;
-                }
-                if (b > bB) {
-                  bB = b;
-                  qB = col0 + j;
-                }
-              }
-            }
-            if (t > 0) {  // columns to the left win ties
-              if (!(bA > lo16(iR0))) {
-                bA = lo16(iR0);
-                qA = (int)(iR1 & 0xffffu);
-              }
-              if (!(bB > hi16(iR0))) {
-                bB = hi16(iR0);
-                qB = (int)(iR1 >> 16);
-              }
-            }
-            mx = (uint32_t)(bA & 0xffff) | ((uint32_t)bB << 16);
-            mq = (uint32_t)qA | ((uint32_t)qB << 16);
-            if (t < G - 1) {
-              oR0 = mx;
-              oR1 = mq;
-              has_out = true;
-            }
-          }
-          if (t == G - 1) {
-#pragma unroll
-            for (int x = 0; x < 2; ++x) {
-              if (!(x == 0 ? lastA : lastB)) continue;
-              const uint32_t orig = p.rec.orig[p.first + 2 * pr + x];
-              const int T = x == 0 ? lenA : lenB;
-              int score, er, eq = p.Q - 1;
-              if (!te && !qe) {
-                score = (x == 0 ? lo16(outH) : hi16(outH)) - frame_of(row);  // this row's H(i, Q-1)
-                er = T - 1;
-              } else {
-                score = te ? (x == 0 ? lo16(best) : hi16(best)) : p.neg_limit;
-                er = x == 0 ? rowA : rowB;
-                if (qe) {
-                  const int s1 = (x == 0 ? lo16(mx) : hi16(mx)) - frame_of(row);
-                  const int t1 = x == 0 ? (int)(mq & 0xffffu) : (int)(mq >> 16);
-                  if (s1 > score) {
-                    score = s1;
-                    er = T - 1;
-                    eq = t1;
-                  } else if (s1 == score && er == T - 1 && t1 < eq) {
-                    eq = t1;
-                  }
-                }
-              }
-              if (p.out.score) p.out.score[orig] = score;
-              if (p.out.qend) p.out.qend[orig] = eq;
-              if (p.out.tend) p.out.tend[orig] = er;
-              if (p.out.hit) p.out.hit[orig] = decide(SG, score, eq, er, p.dec);
-            }
-          }
-        } else {
-          int bA = lo16(best), bB = hi16(best), rA = rowA, rB = rowB, qA = 0x7fff, qB = 0x7fff;
-          // smallest column of this thread's maximum in its first row
-#pragma unroll 1
-          for (int j = K - 1; j >= 0; --j) {
-            if (bA > 0 && (int)(int16_t)saveA[j] == bA) qA = col0 + j;
-            if (bB > 0 && (int)(int16_t)saveB[j] == bB) qB = col0 + j;
-          }
-          if (t > 0) {
-            const int ia = lo16(iR0), ib = hi16(iR0), ira = (int)iR2, irb = (int)iR3;
-            const int iqa = (int)(int16_t)(iR1 & 0xffffu), iqb = (int)(int16_t)(iR1 >> 16);
-            if (ia > bA || (ia == bA && (ira < rA || (ira == rA && iqa < qA)))) {
-              bA = ia;
-              rA = ira;
-              qA = iqa;
-            }
-            if (ib > bB || (ib == bB && (irb < rB || (irb == rB && iqb < qB)))) {
-              bB = ib;
-              rB = irb;
-              qB = iqb;
-            }
-          }
-          if (t < G - 1) {
-            oR0 = (uint32_t)(bA & 0xffff) | ((uint32_t)bB << 16);
-            oR1 = (uint32_t)(qA & 0xffff) | ((uint32_t)qB << 16);
-            oR2 = (uint32_t)rA;
-            oR3 = (uint32_t)rB;
-            has_out = true;
-          } else {
-#pragma unroll
-            for (int x = 0; x < 2; ++x) {
-              if (!(x == 0 ? lastA : lastB)) continue;
-              const uint32_t orig = p.rec.orig[p.first + 2 * pr + x];
-              int score = x == 0 ? bA : bB, er = x == 0 ? rA : rB, eq = x == 0 ? qA : qB;
-              if (score == 0) {
-                er = -1;
-                eq = 0;
-              }
-              if (p.out.score) p.out.score[orig] = score;
-              if (p.out.qend) p.out.qend[orig] = eq;
-              if (p.out.tend) p.out.tend[orig] = er;
-              if (p.out.hit) p.out.hit[orig] = decide(SW, score, eq, er, p.dec);
-            }
-          }
-        }
-      }
-    }
-
-    // Every row thread 0 starts reaches thread G-1 within G-1 steps, so the
-    // group is done once thread 0 is and no row is in flight.  The step budget
+    // Every step thread 0 starts reaches thread G-1 within G-1 steps, so the
+    // group is done once thread 0 is and no step is in flight.  The step budget
     // (all rows of the range plus the pipeline depth) is a hard stop.
-    // (checked every 8 steps; idle extra steps do nothing)
+    // (checked every CHK steps; idle extra steps do nothing)
     if (--chk == 0) {
-      chk = 8;
-      steps += 8;
-      const bool more = busy || (t == 0 && !f_done);
+      chk = CHK;
+      steps += CHK * RPS;
+      const bool more = busy || (t0 && !f_done);
       if (!__any_sync(FULL, more)) break;
       if (steps > p.max_steps) {
         if (lane == 0) atomicOr(p.error, 2);

@@ -15,7 +15,7 @@ OK = 0
 EINVAL, ENOMEM, EOVERFLOW, ENODEV, EDEVICE, EAGAIN, ETIMEDOUT = -22, -12, -75, -19, -5, -11, -110
 ALGO_SEMI_GLOBAL, ALGO_LOCAL = 0, 1
 FREE_QUERY_START, FREE_QUERY_END, FREE_TARGET_START, FREE_TARGET_END = 1, 2, 4, 8
-KERNEL_AUTO, KERNEL_PLAIN, KERNEL_EXACT = 0, 1, 2
+KERNEL_AUTO, KERNEL_PLAIN, KERNEL_EXACT, KERNEL_PLAIN16 = 0, 1, 2, 3
 OPT_KERNEL, OPT_SG_LANES, OPT_SW_U8_LANES, OPT_SW_U16_LANES, OPT_WAVE_GROUP, OPT_WAVE_K = 1, 2, 3, 4, 5, 6
 OPT_PROFILE_LAYOUT = 7
 OPT_WAVE_BLOCKS = 8

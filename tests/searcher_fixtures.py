@@ -58,14 +58,21 @@ def records(case):
 
 
 def render(case, recs, hits, code_to_ascii, encoded):
-    """Output text of the runner: matched records, decoded, in input order."""
-    out = []
-    for (header, _), enc, hit in zip(recs, encoded, hits):
-        if not hit:
-            continue
-        body = bytes(code_to_ascii[enc]) if len(enc) else b""
-        if header is not None:
-            out.append(b">" + header + b"\n" + body + b"\n")
-        else:
-            out.append(body + b"\n")
-    return b"".join(out).decode("utf-8", errors="surrogateescape")
+    """Output text of the runner for these hits, through the library's own
+    writer (ish_gb300.output): matched records, decoded, in input order."""
+    import numpy as np
+
+    from ish_gb300 import output
+
+    enc = [np.asarray(e, np.uint8) for e in encoded]
+    off = np.zeros(len(enc) + 1, np.uint64)
+    np.cumsum([len(e) for e in enc], out=off[1:])
+    buf = np.concatenate(enc) if enc else np.zeros(0, np.uint8)
+    matches = [(i, 0, 0) for i, h in enumerate(hits) if h]
+    c2a = np.asarray(code_to_ascii, np.uint8)
+    parts = []
+    if case["record_type"] == "line":
+        output.write_line_matches(parts.append, buf, off, matches, c2a)
+    else:
+        output.write_fastx_matches(parts.append, [h for h, _ in recs], buf, off, matches, c2a)
+    return b"".join(parts).decode("utf-8", errors="surrogateescape")

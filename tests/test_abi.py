@@ -69,3 +69,30 @@ def test_product_matrices_match_oracle(kind):
     enc, score = m.encode_and_score(text)
     oenc, oscore = O.encode_and_score(kind, text)
     assert (enc == oenc).all() and score == oscore
+
+
+def test_output_writer_formats():
+    """ish_gb300.output writes what the runners write: decoded records in input
+    order, the line runner's tty prefix and colours, the fastx header and
+    quality lines (ishlib/parallel_line_search_runner.mojo:113-155,
+    ishlib/parallel_fastx_search_runner.mojo:136-177)."""
+    from ish_gb300 import output
+    from ish_gb300.scoring import ScoringMatrix
+
+    m = ScoringMatrix.from_str("actgn")
+    recs = [m.encode(b"acgtNx"), m.encode(b"GGG"), m.encode(b"tta")]
+    buf, off = native.pack_records(recs)
+    got = []
+    output.write_line_matches(got.append, buf, off, [(0, 1, 3), (2, 0, 2)], m.code_to_ascii)
+    assert b"".join(got) == b"ACGTNN\nTTA\n"
+    got = []
+    output.write_line_matches(got.append, buf, off, [(2, 1, 3)], m.code_to_ascii, file_name=b"f.txt",
+                              first_line=10, tty=True)
+    assert b"".join(got) == (b"\x1b[35mf.txt\x1b[0m:\x1b[32m13\x1b[0m: T\x1b[31mTA\x1b[0m\n")
+    got = []
+    output.write_fastx_matches(got.append, [b"r0", b"r1", b"r2"], buf, off, [(1, 0, 3)], m.code_to_ascii,
+                               quals=[b"!!!!!!", b"III", b"###"])
+    assert b"".join(got) == b">r1\nGGG\n+\nIII\n"
+    got = []
+    output.write_fastx_matches(got.append, [b"r0", b"r1", b"r2"], buf, off, [(0, 2, 4)], m.code_to_ascii, tty=True)
+    assert b"".join(got) == b">r0\nAC\x1b[1;31m\x1b[31mGT\x1b[0mNN\n"

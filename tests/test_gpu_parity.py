@@ -211,14 +211,20 @@ def test_register_lean_builds(ctx, K):
         ctx.set_option(native.OPT_WAVE_K, 0)
 
 
+@pytest.mark.parametrize("kernel", [native.KERNEL_PLAIN, native.KERNEL_PLAIN16])
 @pytest.mark.parametrize("algo", [native.ALGO_SEMI_GLOBAL, native.ALGO_LOCAL])
-def test_plain_kernel_parity(ctx, algo):
+def test_plain_kernel_parity(ctx, algo, kernel):
+    # both storage forms of the one-thread-per-record kernel: int32 columns in
+    # global scratch, and int16 per-thread arrays (queries of 1 .. 2048
+    # residues cover every array size, 2100 falls back to int32 columns)
     rng = np.random.default_rng(13)
-    q = rng.integers(0, 20, 150, dtype=np.uint8)
-    recs = random_records(rng, 20, 300, 0, 400, q)
-    for ends in ((12, 15, 0, 5) if algo == native.ALGO_SEMI_GLOBAL else (0,)):
-        g, o = run_both(ctx, algo, O.BLOSUM62, q, recs, 10, 1, ends, kernel=native.KERNEL_PLAIN)
-        assert_same(g, o, f"plain algo={algo} ends={ends}")
+    qlens = (150,) if kernel == native.KERNEL_PLAIN else (1, 64, 65, 150, 700, 2048, 2100)
+    for qlen in qlens:
+        q = rng.integers(0, 20, qlen, dtype=np.uint8)
+        recs = random_records(rng, 20, 300 if qlen < 1000 else 60, 0, 400, q)
+        for ends in ((12, 15, 0, 5) if algo == native.ALGO_SEMI_GLOBAL else (0,)):
+            g, o = run_both(ctx, algo, O.BLOSUM62, q, recs, 10, 1, ends, kernel=kernel)
+            assert_same(g, o, f"plain kernel={kernel} Q={qlen} algo={algo} ends={ends}")
 
 
 def test_edge_cases(ctx):
