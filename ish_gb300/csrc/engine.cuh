@@ -73,6 +73,15 @@ struct WaveParams {
   int neg_limit;           // v_neg_limit of the reference (semi_global_aln/striped.mojo:329-334)
   int hleft, fin;          // left boundary value and F entering the padding
   int frame_mask;          // semi-global: R - 1, rows between frame resets (R * ext <= 2048)
+  // packed 16-bit pairs of values used every row, precomputed on the host so
+  // that the kernel reads them as operands instead of deriving them
+  uint32_t pk_nopen;       // (-open, -open)
+  uint32_t pk_next;        // (-ext, -ext)
+  uint32_t pk_eopen;       // (ext - open, ext - open): the framed E update
+  uint32_t pk_fsin;        // (fin + open, fin + open): F + open entering the padding
+  uint32_t pk_ext;         // (ext, ext) for semi-global, 0 for local: one row's frame step
+  uint32_t pk_drop;        // (-R * ext, -R * ext): a frame reset
+  uint32_t row_bytes;      // profile bytes between consecutive codes' rows ((G * kp) words)
   const int16_t *hinit;    // H(-1, q) for q in [-d, Q), index q + d
   uint32_t first, count;   // sorted entries [first, first + count) are scored
   uint32_t *counter;       // work counter (record pairs), zeroed before launch
@@ -116,8 +125,10 @@ struct PlainParams {
 };
 
 // ---- packed 16-bit helpers (DPX on sm_90+) ----
-__device__ __forceinline__ uint32_t dup16(int v) {
-  uint32_t u = (uint32_t)(v & 0xffff);
+__device__ __forceinline__ uint32_t dup16(int v) { return __byte_perm((uint32_t)v, 0u, 0x1010); }
+// the same on the host
+inline uint32_t dup16_host(int v) {
+  const uint32_t u = (uint32_t)v & 0xffffu;
   return u | (u << 16);
 }
 __device__ __forceinline__ int lo16(uint32_t w) { return (int)(int16_t)(w & 0xffff); }

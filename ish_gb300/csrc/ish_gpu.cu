@@ -615,6 +615,13 @@ void wave_params(const Query &q, const WaveLayout &L, const RecordSet &rs, OutDe
   p.hleft = (sg && !(q.ends & ISH_FREE_TARGET_START)) ? NEG_BIG : 0;
   p.fin = sg ? NEG_BIG : 0;
   p.frame_mask = sg ? frame_rows(q.ext) - 1 : 0x3fffffff;
+  p.pk_nopen = dup16_host(-q.open);
+  p.pk_next = dup16_host(-q.ext);
+  p.pk_eopen = dup16_host(q.ext - q.open);
+  p.pk_fsin = dup16_host(p.fin + q.open);
+  p.pk_ext = sg ? (uint32_t)q.ext * 0x10001u : 0u;
+  p.pk_drop = sg ? dup16_host(-(p.frame_mask + 1) * q.ext) : 0u;
+  p.row_bytes = (uint32_t)(L.G * L.kp * (L.layout == PROF_S16 ? 2 : 4));
   p.hinit = L.hinit.as<const int16_t>();
   p.error = error;
   p.rec = RecordsDev{rs.codes.as<const uint8_t>(), rs.off_s.as<const uint64_t>(), rs.len_s.as<const uint32_t>(),

@@ -70,19 +70,17 @@ __device__ __forceinline__ void wave_rows(const WaveParams &p, const unsigned ch
   uint16_t *saveB = saveA + KP8;
 
   const unsigned FULL = 0xffffffffu;
-  const uint32_t NOPEN = dup16(-p.open);
-  const uint32_t NEXT = dup16(-p.ext);
-  const uint32_t VFLOOR = (MODE == SW) ? 0u : dup16(-32768);
-  const uint32_t FS_IN = dup16(p.fin + p.open);  // F + open entering the padding
+  const uint32_t NOPEN = p.pk_nopen;
+  const uint32_t NEXT = p.pk_next;
+  const uint32_t VFLOOR = (MODE == SW) ? 0u : 0x80008000u;
+  const uint32_t FS_IN = p.pk_fsin;  // F + open entering the padding
   // semi-global row frames: row r is held raised by frame = (r mod R) * ext
-  const uint32_t EOPEN = dup16(p.ext - p.open);  // E' = max(T + ext - open, E)
-  const uint32_t NEGMIN = dup16(-32768);
+  const uint32_t EOPEN = p.pk_eopen;  // E' = max(T + ext - open, E)
+  const uint32_t NEGMIN = 0x80008000u;
   const int f0 = (MODE == SG) ? p.ext : 0;  // row -1 sits in frame -ext
   const bool te = (MODE == SG) && (p.ends & 8);
   const bool qe = (MODE == SG) && (p.ends & 2);
   const uint32_t npairs = (p.count + 1) >> 1;
-  const uint16_t *prof16 = reinterpret_cast<const uint16_t *>(prof);
-  const uint32_t *prof32 = reinterpret_cast<const uint32_t *>(prof);
   const int col0 = t * K - p.d;  // query column of register 0
   // parameters read every step, held in registers (the batched kernel's
   // parameters live in shared memory)
@@ -92,7 +90,11 @@ __device__ __forceinline__ void wave_rows(const WaveParams &p, const unsigned ch
   auto frame_of = [&](int r) { return (MODE == SG) ? (r & fmask) * ext : 0; };
   // +ext in both 16-bit halves: added to a boundary value hleft + frame
   // (hleft 0 or NEG_BIG, frames <= 2048), the low half never carries
-  const uint32_t EXT2 = (MODE == SG) ? (uint32_t)ext * 0x10001u : 0u;
+  const uint32_t EXT2 = (MODE == SG) ? p.pk_ext : 0u;
+  // this thread's part of every profile row, and the bytes between the rows
+  // of consecutive codes: a row's address is one multiply-add
+  const unsigned char *prof_t = prof + (uint32_t)(t * kp) * (LAYOUT == PROF_S16 ? 2u : 4u);
+  const uint32_t row_bytes = p.row_bytes;
 
   uint32_t H[K], E[K];
 #pragma unroll
@@ -142,7 +144,7 @@ __device__ __forceinline__ void wave_rows(const WaveParams &p, const unsigned ch
     }
     uint32_t P[K];
     if (LAYOUT == PROF_PAIR) {
-      const uint4 *r4 = reinterpret_cast<const uint4 *>(prof32 + ((cA * alpha + cB) * G + t) * kp);
+      const uint4 *r4 = reinterpret_cast<const uint4 *>(prof_t + (cA * alpha + cB) * row_bytes);
 #pragma unroll
       for (int v = 0; v < (K + 3) / 4; ++v) {
         const uint4 w = r4[v];
@@ -156,8 +158,8 @@ __device__ __forceinline__ void wave_rows(const WaveParams &p, const unsigned ch
       // pair is b * 65536 + a, one integer multiply-add (the multiplier is a
       // runtime value, so this stays an IMAD on the FMA pipe, which the DPX
       // recurrence on the ALU pipe leaves idle)
-      const uint4 *ra = reinterpret_cast<const uint4 *>(prof32 + (cA * G + t) * kp);
-      const uint4 *rb = reinterpret_cast<const uint4 *>(prof32 + (cB * G + t) * kp);
+      const uint4 *ra = reinterpret_cast<const uint4 *>(prof_t + cA * row_bytes);
+      const uint4 *rb = reinterpret_cast<const uint4 *>(prof_t + cB * row_bytes);
       const uint32_t mul = lane_mul;
 #pragma unroll
       for (int v = 0; v < (K + 3) / 4; ++v) {
@@ -170,8 +172,8 @@ __device__ __forceinline__ void wave_rows(const WaveParams &p, const unsigned ch
     } else {
       // 16-bit words (profiles too large for the 32-bit layout): one PRMT
       // per packed pair
-      const uint4 *ra = reinterpret_cast<const uint4 *>(prof16 + (cA * G + t) * kp);
-      const uint4 *rb = reinterpret_cast<const uint4 *>(prof16 + (cB * G + t) * kp);
+      const uint4 *ra = reinterpret_cast<const uint4 *>(prof_t + cA * row_bytes);
+      const uint4 *rb = reinterpret_cast<const uint4 *>(prof_t + cB * row_bytes);
 #pragma unroll
       for (int v = 0; v < (K + 7) / 8; ++v) {
         const uint4 a = ra[v], b = rb[v];
@@ -472,7 +474,7 @@ __device__ __forceinline__ void wave_rows(const WaveParams &p, const unsigned ch
         if (MODE == SG) {
           if ((q4 & fmask) == 0) {
             // frame R*ext -> 0: lower what this step takes from the row above
-            const uint32_t FRAME_DROP = dup16(-(fmask + 1) * ext);
+            const uint32_t FRAME_DROP = p.pk_drop;
 #pragma unroll
             for (int j = 0; j < K; ++j) {
               H[j] = __viaddmax_s16x2(H[j], FRAME_DROP, NEGMIN);
