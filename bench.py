@@ -349,6 +349,11 @@ def run_ours(args):
 
     # ---- integer roofline ----
     dpx = ctx.calibrate()
+    # the lane-width choice: local-alignment rows in registers on 2 x 16-bit
+    # DPX lanes against 4 x 8-bit saturating SIMD byte lanes
+    lanes = {k: round(v / 1e9, 1) for k, v in ctx.calibrate_lanes().items()}
+    lanes = {"s16x2_gcups": lanes["s16x2_cells_per_s"], "u8x4_gcups": lanes["u8x4_cells_per_s"],
+             "what": "local-alignment rows, registers only, no memory traffic"}
     instr = (INSTR_SG + INSTR_SW) / 2  # equal cells in both passes of a step
     peak_gcups = dpx * 2 / instr / 1e9
     per_gpu = cells / (step_ms * 1e-3) / 1e9
@@ -406,6 +411,7 @@ def run_ours(args):
             "gpu_launches": launches,
             "clocks": clk,
             "plain_kernel_gcups": plain,
+            "lane_width": lanes,
             "wall_ms_per_step": round(wall_ms, 3),
             "hits": {"semi_global": hits[0], "local": hits[1]},
             "parity": parity,

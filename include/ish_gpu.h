@@ -292,6 +292,14 @@ ISH_API int ish_gpu_last_kernel_ms(ish_ctx *ctx, double *ms);
  * counterpart in the reference: measurement support for the engine. */
 ISH_API int ish_gpu_calibrate(ish_ctx *ctx, double *dpx_ops_per_s);
 
+/* Local-alignment cell updates per second on packed lanes, measured now with
+ * no memory traffic: two 16-bit lanes per word with DPX add-max (the
+ * wavefront kernel's form) and four 8-bit lanes per word with the saturating
+ * SIMD byte add/subtract/max on a biased profile (the form of the reference's
+ * uint8 pass, local_aln/striped.mojo:162-196).  No counterpart in the
+ * reference: it measures this engine's choice of lane width. */
+ISH_API int ish_gpu_calibrate_lanes(ish_ctx *ctx, double *s16x2_cells_per_s, double *u8x4_cells_per_s);
+
 /* Number of CUDA kernels the library has launched on this context (a batched
  * launch counts the kernel nodes of its graph).  No counterpart in the
  * reference: measurement support. */

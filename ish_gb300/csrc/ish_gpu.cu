@@ -1183,6 +1183,32 @@ int ish_gpu_calibrate(ish_ctx *ctx, double *dpx_ops_per_s) {
   return ISH_OK;
 }
 
+int ish_gpu_calibrate_lanes(ish_ctx *ctx, double *s16x2_cells_per_s, double *u8x4_cells_per_s) {
+  if (!ctx) return ISH_EINVAL;
+  if (!s16x2_cells_per_s || !u8x4_cells_per_s) return fail(ctx, ISH_EINVAL, "NULL output");
+  cudaSetDevice(ctx->device);
+  CU(ctx->counter.ensure(64));
+  const int blocks = ctx->num_sms * 8, threads = 256, rows = 4096;
+  cudaStream_t s = ctx->stream;
+  for (int u8 = 0; u8 < 2; ++u8) {
+    const LaneFn fn = lane_rows_fn(u8 != 0);
+    const uint32_t open = u8 ? 0x0a0a0a0au : 10u, ext = u8 ? 0x01010101u : 1u;
+    fn<<<blocks, threads, 0, s>>>(ctx->counter.as<uint32_t>(), 64, 0x03020104u, open, ext, 0x04040404u);  // warm-up
+    CU(cudaEventRecord(ctx->ev0, s));
+    fn<<<blocks, threads, 0, s>>>(ctx->counter.as<uint32_t>(), rows, 0x03020104u, open, ext, 0x04040404u);
+    CU(cudaEventRecord(ctx->ev1, s));
+    ctx->launches += 2;
+    CU(cudaGetLastError());
+    CU(cudaStreamSynchronize(s));
+    float ms = 0.f;
+    CU(cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1));
+    // 16 words per thread and row, 2 or 4 cells per word
+    const double cells = (double)blocks * threads * rows * 16 * (u8 ? 4 : 2);
+    (u8 ? *u8x4_cells_per_s : *s16x2_cells_per_s) = cells / (ms * 1e-3);
+  }
+  return ISH_OK;
+}
+
 int ish_gpu_launch_count(ish_ctx *ctx, uint64_t *count) {
   if (!ctx || !count) return ISH_EINVAL;
   *count = ctx->launches.load();

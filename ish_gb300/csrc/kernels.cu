@@ -581,4 +581,61 @@ __global__ void k_dpx_peak(uint32_t *out, int iters, uint32_t b, uint32_t c) {
   if (x == 0x12345678u) out[0] = x;
 }
 
+// Local-alignment cell updates on packed lanes, for the lane-width choice of
+// the wavefront kernel.  U8 = false: two 16-bit lanes per word and the
+// wavefront kernel's five DPX add-max per word.  U8 = true: four 8-bit lanes
+// per word with a biased unsigned byte profile, as the reference's u8 pass
+// keeps it (local_aln/striped.mojo:78-139), through the saturating SIMD byte
+// intrinsics (add, subtract, max: ten per word).  Sixteen words of columns
+// per thread in registers and no memory traffic in the loop; the row's
+// boundary changes every row, so nothing is hoisted out of it.
+template <bool U8>
+__global__ void k_lane_rows(uint32_t *out, int rows, uint32_t p0, uint32_t popen, uint32_t pext, uint32_t bias) {
+  constexpr int K = 16;
+  uint32_t H[K], E[K], P[K];
+#pragma unroll
+  for (int j = 0; j < K; ++j) {
+    H[j] = 0;
+    E[j] = 0;
+    P[j] = (p0 + (uint32_t)j * 0x01030107u) ^ (threadIdx.x * 0x00010001u);
+  }
+  // 16-bit lanes add the negated penalties; 8-bit lanes subtract them
+  const uint32_t n16o = (0u - popen) & 0xffffu, n16e = (0u - pext) & 0xffffu;
+  const uint32_t OPEN = U8 ? popen : (n16o | (n16o << 16));
+  const uint32_t EXT = U8 ? pext : (n16e | (n16e << 16));
+  for (int r = 0; r < rows; ++r) {
+    const uint32_t diag = (uint32_t)r * 0x00050005u;
+#pragma unroll
+    for (int j = K - 1; j >= 0; --j) {
+      const uint32_t hd = j ? H[j - 1] : diag;
+      uint32_t T;
+      if (U8) {
+        T = __vmaxu4(__vsubus4(__vaddus4(hd, P[j]), bias), E[j]);
+        E[j] = __vmaxu4(__vsubus4(E[j], EXT), __vsubus4(T, OPEN));
+      } else {
+        T = __viaddmax_s16x2(hd, P[j], E[j]);
+        E[j] = __viaddmax_s16x2(E[j], EXT, __viaddmax_s16x2(T, OPEN, 0u));
+      }
+      H[j] = T;
+    }
+    uint32_t fs = OPEN;
+#pragma unroll
+    for (int j = 0; j < K; ++j) {
+      const uint32_t T = H[j];
+      if (U8) {
+        H[j] = __vmaxu4(__vsubus4(fs, OPEN), T);
+        fs = __vmaxu4(__vsubus4(fs, EXT), T);
+      } else {
+        H[j] = __viaddmax_s16x2(fs, OPEN, T);
+        fs = __viaddmax_s16x2(fs, EXT, T);
+      }
+    }
+  }
+  uint32_t x = 0;
+#pragma unroll
+  for (int j = 0; j < K; ++j) x ^= H[j] ^ E[j];
+  if (x == 0x12345678u) out[0] = x;
+}
+LaneFn lane_rows_fn(bool u8) { return u8 ? (LaneFn)k_lane_rows<true> : (LaneFn)k_lane_rows<false>; }
+
 }  // namespace ish

@@ -37,6 +37,10 @@ constexpr int PLAIN16_THREADS = 15000; // its launch: 15,000 threads in blocks o
 __global__ void k_count_hits(const uint8_t *hit, uint32_t n, uint32_t *block_counts);
 __global__ void k_scan_counts(uint32_t *counts, uint32_t nb, uint32_t *total);
 __global__ void k_dpx_peak(uint32_t *out, int iters, uint32_t b, uint32_t c);
+// k_lane_rows<u8>: local-alignment rows on 2 x 16-bit or 4 x 8-bit lanes
+// (ish_gpu_calibrate_lanes)
+typedef void (*LaneFn)(uint32_t *out, int rows, uint32_t p0, uint32_t popen, uint32_t pext, uint32_t bias);
+LaneFn lane_rows_fn(bool u8);
 __global__ void k_write_hits(const uint8_t *hit, uint32_t n, const uint32_t *block_offsets, uint32_t *idx);
 __global__ void k_gather_hits(const uint32_t *idx, const uint32_t *count, const int32_t *score, const int32_t *qend,
                               const int32_t *tend, int32_t *hit_score, int32_t *hit_qend, int32_t *hit_tend);

@@ -695,3 +695,45 @@ __global__ void __launch_bounds__(wave_threads_lean(K, MODE, LEAN), wave_blocks_
 }
 
 }  // namespace ish
+
+namespace ish {
+
+// Kernel tables.  Each wave_X.cu instantiates the wavefront and batched
+// kernels of one K range (one translation unit per range, so the build
+// compiles them in parallel); wave_table / batch_table pick one at run time
+// by (K, mode, profile layout).
+template <int K, int LEAN>
+struct WaveEntry {
+  static WaveFn wave(int mode, int layout) {
+    static const WaveFn t[2][3] = {
+        {wave_kernel<K, SG, PROF_S16, LEAN>, wave_kernel<K, SG, PROF_PAIR, LEAN>, wave_kernel<K, SG, PROF_S32, LEAN>},
+        {wave_kernel<K, SW, PROF_S16, LEAN>, wave_kernel<K, SW, PROF_PAIR, LEAN>, wave_kernel<K, SW, PROF_S32, LEAN>}};
+    return t[mode == SW][layout];
+  }
+  static BatchFn batch(int mode, int layout) {
+    static const BatchFn t[2][3] = {
+        {batch_kernel<K, SG, PROF_S16, LEAN>, batch_kernel<K, SG, PROF_PAIR, LEAN>,
+         batch_kernel<K, SG, PROF_S32, LEAN>},
+        {batch_kernel<K, SW, PROF_S16, LEAN>, batch_kernel<K, SW, PROF_PAIR, LEAN>,
+         batch_kernel<K, SW, PROF_S32, LEAN>}};
+    return t[mode == SW][layout];
+  }
+};
+
+template <int LEAN, int... Ks>
+WaveFn wave_table(int K, int mode, int layout) {
+  if (layout < PROF_S16 || layout > PROF_S32) return nullptr;
+  WaveFn f = nullptr;
+  ((K == Ks ? (void)(f = WaveEntry<Ks, LEAN>::wave(mode, layout)) : (void)0), ...);
+  return f;
+}
+
+template <int LEAN, int... Ks>
+BatchFn batch_table(int K, int mode, int layout) {
+  if (layout < PROF_S16 || layout > PROF_S32) return nullptr;
+  BatchFn f = nullptr;
+  ((K == Ks ? (void)(f = WaveEntry<Ks, LEAN>::batch(mode, layout)) : (void)0), ...);
+  return f;
+}
+
+}  // namespace ish

@@ -33,6 +33,7 @@ EXPORTS = (
     "ish_gpu_score_noalloc", "ish_gpu_score_multi", "ish_gpu_autotune", "ish_gpu_serve_start", "ish_gpu_submit",
     "ish_gpu_poll", "ish_gpu_serve_stop", "ish_gpu_serve_stats", "ish_gpu_match_starts",
     "ish_gpu_launch_count", "ish_gpu_records_load_raw", "ish_gpu_records_load_lines", "ish_gpu_last_windows",
+    "ish_gpu_calibrate_lanes",
 )
 
 
@@ -88,6 +89,7 @@ def load(build_if_missing: bool = False):
     L.ish_gpu_score_set.argtypes = [vp, C.c_int32, C.c_int32, i32p, i32p, i32p, u8p, u32p, u32p]
     L.ish_gpu_last_kernel_ms.argtypes = [vp, C.POINTER(C.c_double)]
     L.ish_gpu_calibrate.argtypes = [vp, C.POINTER(C.c_double)]
+    L.ish_gpu_calibrate_lanes.argtypes = [vp, C.POINTER(C.c_double), C.POINTER(C.c_double)]
     L.ish_gpu_score_noalloc.argtypes = [vp, C.c_uint64, vp, C.c_uint32, u8p, C.c_uint32, i8p, C.c_uint32, C.c_int,
                                         C.c_uint32, C.c_uint32, C.c_uint32, C.c_int32, C.c_float, vp, vp, vp, vp,
                                         vp, C.c_char_p, C.c_size_t]
@@ -354,6 +356,13 @@ class Context:
         r = C.c_double()
         self._check(self._L.ish_gpu_calibrate(self._h, C.byref(r)))
         return r.value
+
+    def calibrate_lanes(self) -> dict:
+        """Local-alignment cell updates per second on 2 x 16-bit (DPX) and
+        4 x 8-bit (saturating SIMD byte) lanes, registers only."""
+        a, b = C.c_double(), C.c_double()
+        self._check(self._L.ish_gpu_calibrate_lanes(self._h, C.byref(a), C.byref(b)))
+        return {"s16x2_cells_per_s": a.value, "u8x4_cells_per_s": b.value}
 
     def launch_count(self) -> int:
         """CUDA kernels the library has launched on this context."""

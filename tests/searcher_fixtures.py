@@ -38,19 +38,11 @@ def line_records(text: str):
 
 
 def fasta_records(text: str):
-    recs = []
-    header, seq = None, []
-    for raw in text.encode().split(b"\n"):
-        line = raw.rstrip(b"\r")
-        if line.startswith(b">"):
-            if header is not None:
-                recs.append((header, b"".join(seq)))
-            header, seq = line[1:], []
-        elif header is not None:
-            seq.append(line)
-    if header is not None:
-        recs.append((header, b"".join(seq)))
-    return recs
+    """(name, sequence) of every record, through the oracle's restatement of
+    ish's FASTX reader (ishlib/vendor/kseq.mojo:370-461)."""
+    from oracle.fastx import read_records
+
+    return [(name, seq) for name, seq, _ in read_records(text.encode())]
 
 
 def records(case):

@@ -132,10 +132,10 @@ def test_forced_group_shapes(ctx, G):
 
 
 @pytest.mark.parametrize("G,K", [(2, 52), (2, 64), (4, 50), (4, 64), (16, 64)])
-def test_wide_rows_interleaved_schedule(ctx, G, K):
-    # from 49 columns per thread on, the next row's backward pass runs inside
-    # the current row's forward pass; every end rule, records of unequal
-    # lengths in a pair (one lane ends rows before the other) and empty ones
+def test_wide_rows(ctx, G, K):
+    # wide rows (K > 48: 128 x 2 blocks for semi-global, 256 x 1 for local):
+    # every end rule, records of unequal lengths in a pair (one lane ends rows
+    # before the other) and empty ones
     rng = np.random.default_rng(19 + K)
     q = rng.integers(0, 20, 100, dtype=np.uint8)
     recs = random_records(rng, 20, 160, 0, 500, q)
@@ -338,3 +338,12 @@ def test_ascii_long_queries(ctx, qlen):
     for algo, ends in ((native.ALGO_SEMI_GLOBAL, 12), (native.ALGO_SEMI_GLOBAL, 3), (native.ALGO_LOCAL, 0)):
         g, o = run_both(ctx, algo, O.ASCII, q, recs, 3, 1, ends, thr=0.6)
         assert_same(g, o, f"ascii Q={qlen} algo={algo} ends={ends}")
+
+
+def test_calibration_kernels_report_rates(ctx):
+    # the integer-roofline calibration and the lane-width microbenchmark run
+    # and report finite, positive rates
+    assert 1e11 < ctx.calibrate() < 1e15
+    lanes = ctx.calibrate_lanes()
+    for k in ("s16x2_cells_per_s", "u8x4_cells_per_s"):
+        assert 1e10 < lanes[k] < 1e16, lanes
