@@ -59,6 +59,14 @@ def parse():
     ap.add_argument("--cpu-seconds", type=float, default=12.0, help="target CPU time of the baseline sample")
     ap.add_argument("--no-plain", action="store_true", help="skip the plain-kernel comparison")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline")
+    ap.add_argument("--no-batched", action="store_true",
+                    help="protein line: skip the batched leg (64 nucleotide queries x 2M reads, one launch)")
+    ap.add_argument("--no-serving", action="store_true",
+                    help="protein line: skip the serving leg (Poisson query stream against a resident set)")
+    ap.add_argument("--serve-gb", type=float, default=None,
+                    help="resident set of the serving legs in GB (default: 1 in the protein line, 4 alone)")
+    ap.add_argument("--serve-queries", type=int, default=None,
+                    help="queries per arrival rate in the serving legs (default: 100 in the protein line)")
     return ap.parse_args()
 
 
@@ -205,6 +213,169 @@ def parity_check(wl, idx, passes, threads, gap_open, gap_ext, thr):
            "fields": sorted(fields), "oracle_hits": hits}
     if first:
         out["first_mismatch"] = first
+    return out
+
+
+def batched_leg(local):
+    """The batched configuration at full size beside the headline line: 64
+    nucleotide queries (U[50,1000], actgn, gap 3/1, semi-global FFTT,
+    threshold 0.8) against 2,000,000 reads of U[100,300] in one batched launch
+    per step, against the same queries one wavefront launch each and the
+    plain one-thread-per-record kernel in the reference GPU kernel's launch
+    shape; parity of the batched kernel with the oracle on a record sample."""
+    from ish_gb300 import native, workloads
+    from ish_gb300.scoring import ScoringMatrix
+
+    wl = workloads.nucleotide_multi(seed=2, n=2_000_000)
+    queries, gap_open, gap_ext, thr = _queries_of("batched", wl)
+    cells = sum(len(q) for q, *_ in queries) * int(wl.offsets[-1])
+    m = ScoringMatrix(wl.kind)
+    out = {"workload": "64 queries of U[50,1000] nt vs 2,000,000 reads of U[100,300] nt, actgn, gap 3/1, "
+                       "semi-global FFTT, threshold 0.8"}
+    with native.Context(local) as ctx:
+        qids = [ctx.set_query(q, wl.kind, m.values, native.ALGO_SEMI_GLOBAL, gap_open, gap_ext,
+                              native.FREE_TARGET_START | native.FREE_TARGET_END, mx, thr) for q, _, _, mx in queries]
+        sid = ctx.records_load(wl.records, wl.offsets)
+        ctx.autotune(sid, qids)
+        ctx.score_multi(qids, sid, want=("hit_idx",))  # warm-up (captures the graph)
+        ms = []
+        for _ in range(2):
+            ctx.score_multi(qids, sid, want=("hit_idx",))
+            ms.append(ctx.last_kernel_ms())
+        batched = cells / (float(np.mean(ms)) * 1e-3) / 1e9
+        per = 0.0
+        for qid in qids:
+            ctx.score_set(qid, sid, want=("hit_idx",))
+            per += ctx.last_kernel_ms()
+        per_query = cells / (per * 1e-3) / 1e9
+        # plain kernel (int16 per-thread arrays, 15,000 threads x 32) on a sample
+        sub = wl.subset(np.arange(200_000))
+        sid2 = ctx.records_load(sub.records, sub.offsets)
+        pq = qids[::8]
+        pcells = sum(len(queries[qids.index(q)][0]) for q in pq) * int(sub.offsets[-1])
+        ctx.set_option(native.OPT_KERNEL, native.KERNEL_PLAIN16)
+        pms = 0.0
+        for qid in pq:
+            ctx.score_set(qid, sid2, want=("hit_idx",))
+            pms += ctx.last_kernel_ms()
+        ctx.set_option(native.OPT_KERNEL, native.KERNEL_AUTO)
+        ctx.records_free(sid2)
+        plain = pcells / (pms * 1e-3) / 1e9
+        # the batched kernel on a record sample against the oracle
+        rng = np.random.default_rng(31)
+        idx = np.sort(rng.choice(wl.n, 3000, replace=False))
+        sample = wl.subset(idx)
+        sid3 = ctx.records_load(sample.records, sample.offsets)
+        full = ctx.score_multi(qids, sid3, want=("score", "qend", "tend", "hit_idx"))
+        ctx.records_free(sid3)
+        ctx.records_free(sid)
+    import oracle as O
+
+    bad = 0
+    for i, (q, algo, ends, mx) in enumerate(queries):
+        o = O.Matcher(algo, wl.kind, q, mx, thr, gap_open=gap_open, gap_extend=gap_ext, ends=ends).batch(
+            sample.records, sample.offsets, threads=os.cpu_count() or 1)
+        hit = np.zeros(len(idx), np.uint8)
+        hit[np.asarray(full["hit_idx"][i], np.int64)] = 1
+        bad += int(np.count_nonzero(full["score"][i] != o["score"]) + np.count_nonzero(full["qend"][i] != o["qend"])
+                   + np.count_nonzero(full["tend"][i] != o["tend"]) + np.count_nonzero(hit != o["hit"]))
+    out.update({"batched_gcups": round(batched, 1), "ms_per_step": round(float(np.mean(ms)), 2),
+                "per_query_launches_gcups": round(per_query, 1),
+                "batched_over_per_query": round(batched / per_query, 3),
+                "plain_int16_15000x32_gcups": round(plain, 2), "batched_over_plain": round(batched / plain, 1),
+                "parity": {"records": int(len(idx)), "queries": len(queries), "mismatches": bad}})
+    return out
+
+
+def serving_leg(local, gb, count, rates=None):
+    """Poisson query streams through the serving loop (ish_gpu_serve_*)
+    against a resident blosum62 protein set: per arrival rate the served rate
+    and p50/p99 latency of `count` queries (Q ~ U[20,2000], striped-local /
+    semi-global FFTT mix, gap 10/1, threshold 0.8); the device rate against
+    the same queries scored one launch each; and each query's result in the
+    mix against the same query alone."""
+    from ish_gb300 import native, workloads
+    from ish_gb300.scoring import ScoringMatrix
+
+    wl = workloads.serving_records(seed=4, total_bytes=int(gb * (1 << 30)))
+    residues = int(wl.offsets[-1])
+    m = ScoringMatrix(wl.kind)
+    out = {"workload": f"{gb:g} GB resident blosum62 set ({wl.n} records, lognormal median 350), Poisson arrivals, "
+                       f"{count} queries per rate, Q ~ U[20,2000], striped-local / semi-global FFTT mix, gap 10/1, "
+                       "threshold 0.8", "records": wl.n, "residues": residues}
+
+    def make(ctx, qs):
+        ids = []
+        for _, algo, q in qs:
+            a = native.ALGO_LOCAL if algo == "striped-local" else native.ALGO_SEMI_GLOBAL
+            ids.append(ctx.set_query(q, wl.kind, m.values, a, 10, 1,
+                                     native.FREE_TARGET_START | native.FREE_TARGET_END if a == 0 else 0,
+                                     int(m.values[q, q].sum()), 0.8))
+        return ids
+
+    with native.Context(local) as ctx:
+        sid = ctx.records_load(wl.records, wl.offsets)
+        # capacity from a few queries alone: their device time per query
+        probe = workloads.serving_queries(seed=9, count=12, rate=1.0)
+        pids = make(ctx, probe)
+        alone_ms = 0.0
+        alone = []
+        for qid in pids:
+            r = ctx.score_set(qid, sid, want=("hit_idx",))
+            alone_ms += ctx.last_kernel_ms()
+            alone.append(r["hit_idx"])
+        pcells = sum(len(q) for _, _, q in probe) * residues
+        single = pcells / (alone_ms * 1e-3) / 1e9
+        capacity = len(probe) / (alone_ms * 1e-3)
+        # the same queries through the serving loop, submitted at once: the
+        # results must equal each query alone
+        ctx.serve_start(sid, max_active=64, chunks=8)
+        tickets = [ctx.submit(q) for q in pids]
+        same = True
+        for t, want in zip(tickets, alone):
+            r = None
+            while r is None:
+                r = ctx.poll(t, wait_ms=200)
+            same = same and np.array_equal(r["hit_idx"], want)
+        st = ctx.serve_stats()
+        ctx.serve_stop()
+        sat = st["cells"] / st["device_ms"] / 1e6
+        for qid in pids:
+            ctx.free_query(qid)
+        per_rate = []
+        for frac in (rates or (0.5, 0.9, 2.0)):
+            rate = capacity * frac
+            qs = workloads.serving_queries(seed=5, count=count, rate=rate)
+            ids = make(ctx, qs)
+            ctx.serve_start(sid, max_active=64, chunks=8)
+            start = time.perf_counter()
+            tickets = []
+            for (arrival, _, _), qid in zip(qs, ids):
+                now = time.perf_counter() - start
+                if arrival > now:
+                    time.sleep(arrival - now)
+                tickets.append(ctx.submit(qid))
+            lat = []
+            for t in tickets:
+                r = None
+                while r is None:
+                    r = ctx.poll(t, wait_ms=200)
+                lat.append(r["latency_ms"])
+            span = time.perf_counter() - start
+            st = ctx.serve_stats()
+            ctx.serve_stop()
+            for qid in ids:
+                ctx.free_query(qid)
+            per_rate.append({"offered_per_s": round(rate, 3), "offered_over_capacity": frac,
+                             "served_per_s": round(count / span, 3),
+                             "p50_ms": round(float(np.percentile(lat, 50)), 1),
+                             "p99_ms": round(float(np.percentile(lat, 99)), 1),
+                             "device_gcups": round(st["cells"] / st["device_ms"] / 1e6, 1),
+                             "max_active": st["max_active"], "queries": count})
+        ctx.records_free(sid)
+    out.update({"single_query_launches_gcups": round(single, 1), "capacity_per_s": round(capacity, 3),
+                "saturated_device_gcups": round(sat, 1), "saturated_over_single": round(sat / single, 3),
+                "results_equal_alone": bool(same), "rates": per_rate})
     return out
 
 
@@ -390,6 +561,21 @@ def run_ours(args):
         parity = parity_check(wl, idx, [("semi-global", O.SEMI_GLOBAL, O.TS | O.TE, q, res[0]),
                                         ("local", O.LOCAL, 0, q, res[1])], threads, 10, 1, 0.8)
 
+    legs = {}
+    if rank == 0 and world == 1:
+        ctx.close()
+        ctx = None
+        if not args.no_batched:
+            try:
+                legs["batched"] = batched_leg(local)
+            except Exception as e:  # reported, not fatal: the headline line stands on its own
+                legs["batched"] = {"error": f"{type(e).__name__}: {e}"}
+        if not args.no_serving:
+            try:
+                legs["serving"] = serving_leg(local, args.serve_gb or 1.0, args.serve_queries or 100)
+            except Exception as e:
+                legs["serving"] = {"error": f"{type(e).__name__}: {e}"}
+
     if rank == 0:
         lat = np.array(e2e_ms)
         out = {
@@ -415,9 +601,11 @@ def run_ours(args):
             "wall_ms_per_step": round(wall_ms, 3),
             "hits": {"semi_global": hits[0], "local": hits[1]},
             "parity": parity,
+            **legs,
         }
         print(json.dumps(out))
-    ctx.close()
+    if ctx is not None:
+        ctx.close()
     if dist is not None:
         dist.destroy_process_group()
     if parity is not None and parity["mismatches"]:
@@ -701,6 +889,34 @@ def run_workload(args):
         extra["e2e_from_text"] = {"value": round(cells / (float(np.mean(tl)) * 1e-3) / 1e9, 2), "unit": "GCUPS",
                                   "h2d_bytes_per_step": len(text), "lines": nl,
                                   "hits_equal": bool(len(r["hit_idx"]) == nh)}
+    if name == "batched":
+        # from FASTQ text, as the FASTX runner holds a file: upload, split
+        # into records, encode and pack on the device, score, hits back
+        from ish_gb300.scoring import ScoringMatrix as _SM
+
+        dec = _SM(wl.kind).code_to_ascii
+        rngq = np.random.default_rng(44)
+        parts = []
+        for i in range(wl.n):
+            seq = dec[wl.records[int(wl.offsets[i]):int(wl.offsets[i + 1])]].tobytes()
+            parts.append(b"@read%d\n%s\n+\n%s\n" % (i, seq, bytes(rngq.integers(33, 75, len(seq), dtype=np.uint8))))
+        text = b"".join(parts)
+        del parts
+        tl, tload = [], []
+        for s in range(args.warmup + args.steps):
+            t = time.perf_counter()
+            sid4, nr, _ = ctx.records_load_fastx(text, wl.kind, bounds=False)
+            t1 = time.perf_counter()
+            r = ctx.score_multi(qids, sid4, want=("hit_idx",))
+            ctx.records_free(sid4)
+            if s >= args.warmup:
+                tl.append(1e3 * (time.perf_counter() - t))
+                tload.append(1e3 * (t1 - t))
+        same = nr == wl.n and all(np.array_equal(a, b) for a, b in zip(r["hit_idx"], res["hit_idx"]))
+        extra["e2e_from_fastq"] = {"value": round(cells / (float(np.mean(tl)) * 1e-3) / 1e9, 2), "unit": "GCUPS",
+                                   "h2d_bytes_per_step": len(text), "records": int(nr),
+                                   "load_ms": round(float(np.mean(tload)), 2), "hits_equal": bool(same)}
+        del text
     cpu = None
     parity = None
     if rank == 0 and not args.no_cpu:

@@ -165,6 +165,38 @@ ISH_API int ish_gpu_records_load_raw(ish_ctx *ctx, const uint8_t *raw, const uin
 ISH_API int ish_gpu_records_load_lines(ish_ctx *ctx, const uint8_t *text, uint64_t bytes, int matrix_kind,
                                        int32_t *set_id, uint32_t *n_records);
 
+/* Load the FASTA/FASTQ records of a text buffer as a resident set: split on
+ * the device exactly as ish's FASTX runners read a file
+ * (ishlib/vendor/kseq.mojo:370-461, FastxReader[read_comment=False].read, in
+ * the loop of ishlib/parallel_fastx_search_runner.mojo:93-121): text before
+ * the first '>' or '@' is skipped, a record's sequence lines are joined with
+ * one trailing '\r' dropped from each, an empty line appends a '\n' and the
+ * whole next line, and reading stops at the first record whose read returns
+ * 0 or less (an empty sequence, a FASTQ quality of another length, a missing
+ * quality line).  Sequences are encoded on the device as for
+ * ish_gpu_records_load_raw; record i is the i-th record of the text.
+ *   bounds (may be NULL): 4 entries per record, byte offsets into `text`:
+ *     name [bounds[4i], bounds[4i+1]) (the header line after its '>'/'@',
+ *     as the reader keeps it), quality [bounds[4i+2], bounds[4i+3]) (both 0
+ *     for a FASTA record).  If more than bounds_cap records are read the call
+ *     fails with ISH_EOVERFLOW and loads nothing.
+ * A FASTQ quality that continues on the next line (legal for kseq, which
+ * reads quality lines until the quality is as long as the sequence) is not
+ * split on the device: ISH_EINVAL. */
+ISH_API int ish_gpu_records_load_fastx(ish_ctx *ctx, const uint8_t *text, uint64_t bytes, int matrix_kind,
+                                       int32_t *set_id, uint32_t *n_records, uint64_t *bounds, uint64_t bounds_cap);
+
+/* Copy records [first, first + count) of a resident set back to the host, in
+ * record order, as the set holds them (encoded codes): codes receives them
+ * concatenated (capacity codes_cap bytes), offsets count + 1 entries
+ * (record i of the range is codes[offsets[i] .. offsets[i + 1])).  What a
+ * runner prints for a match when the device parsed the file (the FASTX
+ * runners keep every record's sequence for their output,
+ * ishlib/parallel_fastx_search_runner.mojo:306-331).  ISH_EOVERFLOW if the
+ * codes do not fit (offsets are still filled). */
+ISH_API int ish_gpu_records_get(ish_ctx *ctx, int32_t set_id, uint32_t first, uint32_t count, uint8_t *codes,
+                                uint64_t codes_cap, uint64_t *offsets);
+
 /* Score one query against a resident set; outputs as for ish_gpu_score. */
 ISH_API int ish_gpu_score_set(ish_ctx *ctx, int32_t query_id, int32_t set_id, int32_t *score,
                       int32_t *query_end, int32_t *target_end, uint8_t *hit, uint32_t *hit_idx,

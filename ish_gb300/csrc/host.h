@@ -157,6 +157,15 @@ struct ExactRes {
   }
 };
 
+// Scratch of the FASTA/FASTQ splitter (fastx.cu): per line, per record.
+struct FastxScratch {
+  DevBuf hc, len, src, hdr, pos, rec, role, tiles, scan, totals, rec_off, bounds, flags, seq;
+  void release() {
+    DevBuf *b[] = {&hc, &len, &src, &hdr, &pos, &rec, &role, &tiles, &scan, &totals, &rec_off, &bounds, &flags, &seq};
+    for (DevBuf *x : b) x->release();
+  }
+};
+
 struct MultiPlan;  // multi.cu
 struct Server;     // serve.cu
 struct Tuned {
@@ -192,6 +201,7 @@ struct ish_ctx {
   ish::host::DevBuf counter, error, out_score, out_qend, out_tend, out_hit, hit_idx, block_counts, nhits;
   ish::host::DevBuf plain_scratch;
   ish::host::DevBuf enc_tables, nl_pos, line_end;  // encoding tables; line splitting scratch
+  ish::host::FastxScratch fastx;                    // FASTA/FASTQ splitting scratch (fastx.cu)
   ish::host::ExactRes exact;                        // exact kernels (exact.cu)
   ish::host::WindowOut window_out;                  // windowed passes (windows.cu)
   uint32_t last_windows = 0;                        // windows of the last windowed pass

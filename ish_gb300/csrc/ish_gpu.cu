@@ -926,6 +926,7 @@ void ish_gpu_close(ish_ctx *ctx) {
   for (DevBuf *b : bufs) b->release();
   ctx->exact.release();
   ctx->window_out.release();
+  ctx->fastx.release();
   cudaEventDestroy(ctx->ev0);
   cudaEventDestroy(ctx->ev1);
   cudaStreamDestroy(ctx->stream);

@@ -33,7 +33,7 @@ EXPORTS = (
     "ish_gpu_score_noalloc", "ish_gpu_score_multi", "ish_gpu_autotune", "ish_gpu_serve_start", "ish_gpu_submit",
     "ish_gpu_poll", "ish_gpu_serve_stop", "ish_gpu_serve_stats", "ish_gpu_match_starts",
     "ish_gpu_launch_count", "ish_gpu_records_load_raw", "ish_gpu_records_load_lines", "ish_gpu_last_windows",
-    "ish_gpu_calibrate_lanes",
+    "ish_gpu_calibrate_lanes", "ish_gpu_records_load_fastx", "ish_gpu_records_get",
 )
 
 
@@ -99,6 +99,8 @@ def load(build_if_missing: bool = False):
     L.ish_gpu_last_windows.argtypes = [vp, C.POINTER(C.c_uint32)]
     L.ish_gpu_records_load_raw.argtypes = [vp, u8p, u64p, C.c_uint32, C.c_int, i32p]
     L.ish_gpu_records_load_lines.argtypes = [vp, u8p, C.c_uint64, C.c_int, i32p, u32p]
+    L.ish_gpu_records_load_fastx.argtypes = [vp, u8p, C.c_uint64, C.c_int, i32p, u32p, u64p, C.c_uint64]
+    L.ish_gpu_records_get.argtypes = [vp, C.c_int32, C.c_uint32, C.c_uint32, u8p, C.c_uint64, u64p]
     L.ish_gpu_match_starts.argtypes = [vp, C.c_int32, C.c_int32, u32p, i32p, C.c_uint32, C.POINTER(C.c_int64)]
     L.ish_gpu_serve_start.argtypes = [vp, C.c_int32, C.c_uint32, C.c_uint64, C.c_uint32]
     L.ish_gpu_submit.argtypes = [vp, C.c_int32, u64p]
@@ -238,6 +240,36 @@ class Context:
         self._check(self._L.ish_gpu_records_load_lines(self._h, _p(buf, C.c_uint8) if len(buf) else None, len(buf),
                                                        matrix_kind, C.byref(sid), C.byref(n)))
         return sid.value, n.value
+
+    def records_load_fastx(self, text, matrix_kind: int, bounds: bool = True):
+        """Resident set of the FASTA/FASTQ records of `text` (split and encoded
+        on the device as ish's FASTX runners read a file); returns (set id,
+        number of records, bounds), bounds an (n, 4) uint64 array of name
+        [start, end) and quality [start, end) byte offsets into `text` (None
+        if not asked for)."""
+        buf = np.frombuffer(bytes(text), np.uint8) if not isinstance(text, np.ndarray) else \
+            np.ascontiguousarray(text, np.uint8)
+        sid = C.c_int32()
+        n = C.c_uint32()
+        # every record needs a header line: at most one record per newline + 1
+        cap = int(np.count_nonzero(buf == 10)) + 1 if bounds else 0
+        bnd = np.zeros((cap, 4), np.uint64) if bounds else None
+        self._check(self._L.ish_gpu_records_load_fastx(
+            self._h, _p(buf, C.c_uint8) if len(buf) else None, len(buf), matrix_kind, C.byref(sid), C.byref(n),
+            _p(bnd, C.c_uint64) if bounds else None, cap))
+        return sid.value, n.value, (bnd[:n.value].copy() if bounds else None)
+
+    def records_get(self, sid: int, first: int = 0, count: int | None = None):
+        """Records [first, first + count) of a resident set, as stored
+        (encoded), in record order: (codes, offsets)."""
+        if count is None:
+            count = self.records_info(sid)[0] - first
+        off = np.zeros(count + 1, np.uint64)
+        total = self.records_info(sid)[1]
+        codes = np.zeros(max(1, int(total)), np.uint8)
+        self._check(self._L.ish_gpu_records_get(self._h, sid, first, count, _p(codes, C.c_uint8), len(codes),
+                                                _p(off, C.c_uint64)))
+        return codes[:int(off[-1])], off
 
     def records_free(self, sid: int):
         self._check(self._L.ish_gpu_records_free(self._h, sid))

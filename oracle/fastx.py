@@ -54,6 +54,7 @@ class FastxReader:
         self.qual = bytearray()
         self.last_char = 0
         self.fastq = False
+        self.qual_lines = 1
         # byte offsets of the last record's header line (after the '>'/'@')
         # and quality line, for the device loader's bounds
         self.name_start = 0
@@ -71,6 +72,7 @@ class FastxReader:
         self.qual.clear()
         self.name.clear()
         self.fastq = False
+        self.qual_lines = 1  # quality lines read (more than one: a continued quality)
         self.name_start = r.i
         if r.read_until_newline(self.name, 0) < 0:  # 416-421
             return -1
@@ -95,6 +97,8 @@ class FastxReader:
         rr = r.read_until_newline(self.qual, len(self.qual))  # 454-461
         while rr >= 0 and len(self.qual) < len(self.seq):
             rr = r.read_until_newline(self.qual, len(self.qual))
+            if rr >= 0:
+                self.qual_lines += 1
         if rr < 0:
             return -3
         self.last_char = 0
@@ -104,13 +108,18 @@ class FastxReader:
         return len(self.seq)
 
 
-def read_records(data: bytes):
+def read_records(data: bytes, with_continued=False):
     """The records a FASTX runner takes from a file: a list of
-    (name, seq, qual-or-None), stopping at the first read() <= 0."""
+    (name, seq, qual-or-None), stopping at the first read() <= 0.  With
+    `with_continued`, also whether the reader went past a record's first
+    quality line before it stopped (a quality continued on the next line)."""
     rd = FastxReader(data)
     out = []
+    continued = False
     while True:
+        rd.qual_lines = 1
         ret = rd.read()
+        continued = continued or rd.qual_lines > 1
         if ret <= 0:
-            return out
+            return (out, continued) if with_continued else out
         out.append((bytes(rd.name), bytes(rd.seq), bytes(rd.qual) if rd.fastq else None))
