@@ -478,12 +478,13 @@ def run_ours(args):
     pin[:] = wl.records
     pin_off[:] = wl.offsets
     e2e_ms = []
+    outs_sg, outs_sw = _pinned_outputs(wl.n), _pinned_outputs(wl.n)
     for s in range(args.warmup + args.steps):
         barrier(dist)
         t = time.perf_counter()
         sid2 = ctx.records_load(pin, pin_off)
-        ctx.score_set(q_sg, sid2, want=("score", "qend", "tend", "hit_idx"))
-        ctx.score_set(q_sw, sid2, want=("score", "qend", "tend", "hit_idx"))
+        ctx.score_set(q_sg, sid2, want=("score", "qend", "tend", "hit_idx"), out=outs_sg)
+        ctx.score_set(q_sw, sid2, want=("score", "qend", "tend", "hit_idx"), out=outs_sw)
         ctx.records_free(sid2)
         if s >= args.warmup:
             e2e_ms.append(1e3 * (time.perf_counter() - t))
@@ -723,6 +724,20 @@ def _pinned(wl):
     return pin, pin_off
 
 
+def _pinned_outputs(n):
+    """Pinned host arrays for one pass's outputs (score, ends, hit list),
+    reused by every end-to-end step: the caller's buffers, as a runner would
+    keep them."""
+    try:
+        import torch
+
+        mk = lambda dt: torch.empty(max(n, 1), dtype=dt, pin_memory=True).numpy()
+        return {"score": mk(torch.int32), "qend": mk(torch.int32), "tend": mk(torch.int32),
+                "hit_idx": mk(torch.int32).view(np.uint32)}
+    except Exception:
+        return None
+
+
 def run_workload(args):
     from ish_gb300 import native, workloads
     from ish_gb300.scoring import ScoringMatrix
@@ -847,26 +862,30 @@ def run_workload(args):
     e2e = []
     phases = []
     nh = 0
+    outs = _pinned_outputs(wl.n)
     for s in range(args.warmup + args.steps):
         barrier(dist)
         t = time.perf_counter()
         sid3 = ctx.records_load(pin, pin_off)
         t1 = time.perf_counter()
+        lp = ctx.last_load_ms()
         if name == "batched":
             r = ctx.score_multi(qids, sid3, want=("hit_idx",))
             nh = sum(len(h) for h in r["hit_idx"])
         else:
-            r = ctx.score_set(qids[0], sid3, want=("score", "qend", "tend", "hit_idx"))
+            r = ctx.score_set(qids[0], sid3, want=("score", "qend", "tend", "hit_idx"), out=outs)
             nh = len(r["hit_idx"])
         t2 = time.perf_counter()
         dev_ms = ctx.last_kernel_ms()
         ctx.records_free(sid3)
         if s >= args.warmup:
             e2e.append(1e3 * (time.perf_counter() - t))
-            phases.append((1e3 * (t1 - t), 1e3 * (t2 - t1), dev_ms, 1e3 * (time.perf_counter() - t2)))
+            phases.append((1e3 * (t1 - t), 1e3 * (t2 - t1), dev_ms, 1e3 * (time.perf_counter() - t2), lp["upload"],
+                           lp["pack"]))
     e2e_ms = reduce_max(dist, float(np.mean(e2e)))
     ph = np.mean(np.array(phases), axis=0)
-    extra["e2e_phases_ms"] = {"load": round(float(ph[0]), 2), "score": round(float(ph[1]), 2),
+    extra["e2e_phases_ms"] = {"load": round(float(ph[0]), 2), "load_upload_device": round(float(ph[4]), 2),
+                              "load_pack_device": round(float(ph[5]), 2), "score": round(float(ph[1]), 2),
                               "score_device": round(float(ph[2]), 2), "free": round(float(ph[3]), 2),
                               "pinned": bool(getattr(_pinned, "ok", False)), "h2d_gbs_torch": h2d_gbs}
     d2h = 4 * nh + (0 if name == "batched" else 12 * wl.n) + 8 * (len(qids) + 1)
@@ -878,11 +897,19 @@ def run_workload(args):
         dec = _SM(wl.kind).code_to_ascii
         text = b"\n".join(dec[wl.records[int(wl.offsets[i]):int(wl.offsets[i + 1])]].tobytes()
                            for i in range(wl.n)) + b"\n"
+        text_pin = np.frombuffer(text, np.uint8)
+        try:
+            import torch
+
+            text_pin = torch.empty(len(text), dtype=torch.uint8, pin_memory=True).numpy()
+            text_pin[:] = np.frombuffer(text, np.uint8)
+        except Exception:
+            pass
         tl = []
         for s in range(args.warmup + args.steps):
             t = time.perf_counter()
-            sid4, nl = ctx.records_load_lines(text, wl.kind)
-            r = ctx.score_set(qids[0], sid4, want=("score", "qend", "tend", "hit_idx"))
+            sid4, nl = ctx.records_load_lines(text_pin, wl.kind)
+            r = ctx.score_set(qids[0], sid4, want=("score", "qend", "tend", "hit_idx"), out=outs)
             ctx.records_free(sid4)
             if s >= args.warmup:
                 tl.append(1e3 * (time.perf_counter() - t))
@@ -900,8 +927,16 @@ def run_workload(args):
         for i in range(wl.n):
             seq = dec[wl.records[int(wl.offsets[i]):int(wl.offsets[i + 1])]].tobytes()
             parts.append(b"@read%d\n%s\n+\n%s\n" % (i, seq, bytes(rngq.integers(33, 75, len(seq), dtype=np.uint8))))
-        text = b"".join(parts)
+        text = np.frombuffer(b"".join(parts), np.uint8)
         del parts
+        try:
+            import torch
+
+            tp = torch.empty(len(text), dtype=torch.uint8, pin_memory=True).numpy()
+            tp[:] = text
+            text = tp
+        except Exception:
+            pass
         tl, tload = [], []
         for s in range(args.warmup + args.steps):
             t = time.perf_counter()
@@ -957,109 +992,54 @@ def run_workload(args):
 
 def run_serving(args, rank, world, local, dist):
     """Poisson query streams against a resident protein set through the
-    serving loop (ish_gpu_serve_*); one JSON line with p50/p99 per rate."""
-    from ish_gb300 import native, workloads
-    from ish_gb300.scoring import ScoringMatrix
+    serving loop (ish_gpu_serve_*): one JSON line whose value is the device
+    rate with the loop saturated, with p50/p99 latency per arrival rate."""
+    from ish_gb300 import workloads
 
-    gb = float(os.environ.get("ISH_SERVE_GB", "4"))
-    wl = workloads.serving_records(seed=4 + rank, total_bytes=int(gb * (1 << 30)))
-    residues = int(wl.offsets[-1])
-    m = ScoringMatrix(wl.kind)
-    count = max(args.steps, 4)
-    # 0.5/s is below the set's capacity (~0.85 queries/s at 4 GB), the
-    # configuration's own rates (10-2000/s) are far above it
-    rates = (0.5, 10.0, 100.0, 2000.0)
-    config = {"workload": f"serving: {gb:g} GB resident blosum62 protein set ({wl.n} records, lognormal median "
-                          f"350), Poisson arrivals at {', '.join(f'{r:g}' for r in rates)} queries/s, {count} "
-                          "queries per rate, Q ~ U[20,2000], striped-local / semi-global FFTT mix, gap 10/1, "
-                          "threshold 0.8", "records": wl.n, "residues": residues, "parallelism": "records"}
+    gb = args.serve_gb or float(os.environ.get("ISH_SERVE_GB", "4"))
+    count = args.serve_queries or max(args.steps, 20)
     if args.impl == "reference":
-        qs = workloads.serving_queries(count=4, rate=rates[0])
+        from ish_gb300.scoring import ScoringMatrix
         import oracle as O
 
+        wl = workloads.serving_records(seed=4, total_bytes=int(gb * (1 << 30)))
+        m = ScoringMatrix(wl.kind)
+        qs = workloads.serving_queries(count=4, rate=1.0)
         queries = [(q, O.LOCAL if a == "striped-local" else O.SEMI_GLOBAL,
                     0 if a == "striped-local" else O.TS | O.TE, int(m.values[q, q].sum())) for _, a, q in qs]
         cpu = _cpu_sample(wl, queries, 10, 1, 0.8, args.cpu_seconds)
+        config = {"workload": f"serving: {gb:g} GB resident blosum62 protein set, Q ~ U[20,2000], striped-local / "
+                              "semi-global FFTT mix, gap 10/1, threshold 0.8", "parallelism": "records"}
         line = _base_line(args, 1, cpu["value"], 0.0, config, "int16")
         line.update({"impl": "reference", "cpu_baseline": cpu,
                      "e2e": {"value": cpu["value"], "unit": "GCUPS", "h2d_bytes_per_step": 0,
                              "d2h_bytes_per_step": 0}})
         print(json.dumps(line))
         return
-    native.load(build_if_missing=True)
-    ctx = native.Context(local)
-    sid = ctx.records_load(wl.records, wl.offsets)
-    per_rate = []
     clocks = Clocks(local)
     clocks.start()
-    total_cells = total_ms = 0.0
-    launches0 = ctx.launch_count()
-    sg_cells = sw_cells = 0
-    for rate in rates:
-        qs = workloads.serving_queries(count=count, rate=rate)
-        for _, algo, q in qs:
-            if algo == "striped-local":
-                sw_cells += len(q)
-            else:
-                sg_cells += len(q)
-        ids = []
-        for _, algo, q in qs:
-            a = native.ALGO_LOCAL if algo == "striped-local" else native.ALGO_SEMI_GLOBAL
-            ids.append(ctx.set_query(q, wl.kind, m.values, a, 10, 1,
-                                     native.FREE_TARGET_START | native.FREE_TARGET_END if a == 0 else 0,
-                                     int(m.values[q, q].sum()), 0.8))
-        ctx.serve_start(sid, max_active=64, chunks=8)
-        start = time.perf_counter()
-        tickets = []
-        for (arrival, _, _), qid in zip(qs, ids):
-            now = time.perf_counter() - start
-            if arrival > now:
-                time.sleep(arrival - now)
-            tickets.append(ctx.submit(qid))
-        lat = []
-        for t in tickets:
-            r = None
-            while r is None:
-                r = ctx.poll(t, wait_ms=200)
-            lat.append(r["latency_ms"])
-        span = time.perf_counter() - start
-        st = ctx.serve_stats()
-        ctx.serve_stop()
-        for qid in ids:
-            ctx.free_query(qid)
-        cells = sum(len(q) for _, _, q in qs) * residues
-        total_cells += st["cells"]
-        total_ms += st["device_ms"]
-        per_rate.append({"offered_per_s": rate, "served_per_s": round(count / span, 3),
-                         "p50_ms": round(float(np.percentile(lat, 50)), 1),
-                         "p99_ms": round(float(np.percentile(lat, 99)), 1),
-                         "wall_gcups": round(cells / span / 1e9, 1),
-                         "device_gcups": round(st["cells"] / st["device_ms"] / 1e6, 1),
-                         "max_active": st["max_active"], "steps": st["steps"]})
+    leg = serving_leg(local, gb, count)
     clk = clocks.stop()
-    launches = ctx.launch_count() - launches0
-    value = total_cells / (total_ms * 1e-3) / 1e9
-    # the plain one-thread-per-record kernel, one query on a record sample
-    sub = wl.subset(np.arange(0, wl.n, max(1, wl.n // 100_000)))
-    sid2 = ctx.records_load(sub.records, sub.offsets)
-    q = workloads.serving_queries(count=1, rate=1.0, seed=11)[0][2]
-    pq = ctx.set_query(q, wl.kind, m.values, native.ALGO_SEMI_GLOBAL, 10, 1, 12, int(m.values[q, q].sum()), 0.8)
-    ctx.set_option(native.OPT_KERNEL, native.KERNEL_PLAIN)
-    ctx.score_set(pq, sid2, want=("hit_idx",))
-    plain = len(q) * int(sub.offsets[-1]) / (ctx.last_kernel_ms() * 1e-3) / 1e9
-    ctx.set_option(native.OPT_KERNEL, native.KERNEL_AUTO)
-    line = _base_line(args, world, value, total_ms / max(1, len(rates) * count), config)
-    instr = (INSTR_SG * sg_cells + INSTR_SW * sw_cells) / max(1, sg_cells + sw_cells)
-    line.update({"roofline": _roofline(ctx, value, instr), "cpu_baseline": None,
-                 "e2e": {"value": per_rate[-1]["wall_gcups"], "unit": "GCUPS",
-                         "h2d_bytes_per_step": int(np.mean([len(q) for _, _, q in qs])) + 8,
-                         "d2h_bytes_per_step": 0,
-                         "latency_ms": {"p50": per_rate[-1]["p50_ms"], "p99": per_rate[-1]["p99_ms"]}},
-                 "serving": per_rate, "plain_per_query_gcups": round(plain, 2),
-                 "gpu_launches": launches, "clocks": clk})
+    value = leg["saturated_device_gcups"]
+    config = {"workload": "serving: " + leg["workload"], "records": leg["records"], "residues": leg["residues"],
+              "parallelism": "records"}
+    line = _base_line(args, world, value, 0.0, config)
+    mean_q = 1010.0  # U[20,2000]
+    sat = leg["rates"][-1]
+    line.update({"roofline": _roofline_ctxless(local, value, (INSTR_SG + INSTR_SW) / 2), "cpu_baseline": None,
+                 "e2e": {"value": round(sat["served_per_s"] * mean_q * leg["residues"] / 1e9, 1), "unit": "GCUPS",
+                         "h2d_bytes_per_step": int(mean_q) + 8, "d2h_bytes_per_step": 0,
+                         "latency_ms": {"p50": sat["p50_ms"], "p99": sat["p99_ms"]}},
+                 "serving": leg, "clocks": clk})
     if rank == 0:
         print(json.dumps(line))
-    ctx.close()
+
+
+def _roofline_ctxless(local, gcups, instr):
+    from ish_gb300 import native
+
+    with native.Context(local) as ctx:
+        return _roofline(ctx, gcups, instr)
 
 
 def main():

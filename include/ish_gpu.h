@@ -136,7 +136,10 @@ ISH_API int ish_gpu_free_query(ish_ctx *ctx, int32_t query_id);
  *   score[i], query_end[i], target_end[i]: the forward pass of the matcher
  *       (semi_global_aln / the adaptive sw of ssw_align);
  *   hit[i]: 1 iff first_match() of the CPU matcher returns a match;
- *   hit_idx[0 .. *n_hits): the hits in ascending record order. */
+ *   hit_idx[0 .. *n_hits): the hits in ascending record order (room for n
+ *       entries: the call may write past *n_hits, those entries mean nothing).
+ * Outputs in pinned host memory (cudaHostAlloc) come back at full copy speed;
+ * pageable ones are staged by the CUDA driver. */
 ISH_API int ish_gpu_score(ish_ctx *ctx, int32_t query_id, const uint8_t *records, const uint64_t *offsets,
                   uint32_t n, int32_t *score, int32_t *query_end, int32_t *target_end, uint8_t *hit,
                   uint32_t *hit_idx, uint32_t *n_hits);
@@ -254,7 +257,8 @@ ISH_API int ish_gpu_match_starts(ish_ctx *ctx, int32_t query_id, int32_t set_id,
  * the context admits waiting queries while fewer than max_active run and the
  * device memory their outputs need (29 bytes per record of the set) fits
  * mem_budget (0: half of the free device memory), and runs steps: each step
- * scores the next of `chunks` equal-residue chunks of the set for every
+ * scores the next of `chunks` chunks of the set (chunk c: every chunks-th
+ * record pair of the set's longest-first order, from pair c) for every
  * admitted query in one batched launch, so queries that arrive while others
  * run join at the next step and share the device with them.  Results are
  * identical to ish_gpu_score_set.  submit and poll may be called from any
@@ -317,6 +321,14 @@ ISH_API int ish_gpu_score_noalloc(const uint8_t *d_records, uint64_t records_byt
  * from the first scoring kernel to the end of the hit compaction (CUDA events
  * on the engine's stream; excludes host<->device copies). */
 ISH_API int ish_gpu_last_kernel_ms(ish_ctx *ctx, double *ms);
+
+/* Phases of the last record load (ish_gpu_records_load*): upload_ms, device
+ * time from the start of the host-to-device copy to the start of packing
+ * (for text loads this includes the splitting kernels); pack_ms, device time
+ * of the sort and pack kernels; wall_ms, host time of the whole call.  Any
+ * pointer may be NULL.  No counterpart in the reference: measurement support
+ * for the engine. */
+ISH_API int ish_gpu_last_load_ms(ish_ctx *ctx, double *upload_ms, double *pack_ms, double *wall_ms);
 
 /* Throughput of the packed 16-bit DPX add-max instruction on this device,
  * measured now (instructions per second; each covers two 16-bit lanes).  The

@@ -84,6 +84,7 @@ struct WaveParams {
   uint32_t row_bytes;      // profile bytes between consecutive codes' rows ((G * kp) words)
   const int16_t *hinit;    // H(-1, q) for q in [-d, Q), index q + d
   uint32_t first, count;   // sorted entries [first, first + count) are scored
+  uint32_t pair_stride, pair_phase;  // of those, record pairs phase, phase + stride, ... (stride 0: every pair)
   uint32_t *counter;       // work counter (record pairs), zeroed before launch
   uint64_t max_steps;      // hard bound on pipeline steps per warp
   int *error;              // bit 0: record code >= alphabet; bit 1: step budget exceeded
@@ -93,10 +94,12 @@ struct WaveParams {
 };
 
 // One work range of the batched launch: sorted entries [first, first + count)
-// of the record set scored against query q of the launch, handed out pair by
-// pair by its own counter.
+// of the record set (every stride-th record pair from phase, if `pairs` says
+// so) scored against query q of the launch, handed out pair by pair by its own
+// counter.
 struct BatchTile {
-  uint32_t q, first, count, pad;
+  uint32_t q, first, count;
+  uint32_t pairs;  // (stride << 16) | phase: the tile's record pairs, as WaveParams (0: every pair)
 };
 
 struct BatchParams {

@@ -371,6 +371,7 @@ int load_fastx(ish_ctx *ctx, const uint8_t *text, uint64_t bytes, RecordSet &rs,
   cudaStream_t s = ctx->stream;
   FastxScratch &fx = ctx->fastx;
   CU(ctx->raw.ensure(bytes + 32));
+  CU(cudaEventRecord(ctx->load_ev[0], s));
   CU(cudaMemcpyAsync(ctx->raw.p, text, bytes, cudaMemcpyHostToDevice, s));
   const uint8_t *dtext = ctx->raw.as<uint8_t>();
   // ---- newlines, as for line records ----
@@ -498,6 +499,7 @@ int ish_gpu_records_load_fastx(ish_ctx *ctx, const uint8_t *text, uint64_t bytes
                                uint32_t *n_records, uint64_t *bounds, uint64_t bounds_cap) {
   if (!ctx) return ISH_EINVAL;
   if (!set_id) return fail(ctx, ISH_EINVAL, "set_id is NULL");
+  LoadTimer timer(ctx);
   cudaSetDevice(ctx->device);
   const uint8_t *enc = nullptr;
   int rc = device_encoding(ctx, matrix_kind, &enc);

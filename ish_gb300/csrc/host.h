@@ -6,6 +6,7 @@
 #include <cuda_runtime.h>
 
 #include <atomic>
+#include <chrono>
 #include <cstdint>
 #include <map>
 #include <memory>
@@ -181,6 +182,8 @@ struct ish_ctx {
   size_t mem_total = 0;  // device memory (bytes)
   cudaStream_t stream = nullptr;
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+  cudaEvent_t load_ev[3] = {nullptr, nullptr, nullptr};  // last load: start, packing start, end
+  double last_load_ms[3] = {0, 0, 0};                    // upload (+ splitting), packing, host wall
   std::string err;
   int kernel = ISH_KERNEL_AUTO;
   int sg_lanes = 8, sw_u8_lanes = 16, sw_u16_lanes = 8;
@@ -223,6 +226,17 @@ namespace host {
 
 int fail(ish_ctx *c, int code, const char *fmt, ...);
 extern thread_local std::string g_open_error;
+
+// Host wall time of a record-load call, kept for ish_gpu_last_load_ms.
+struct LoadTimer {
+  ish_ctx *ctx;
+  std::chrono::steady_clock::time_point t0 = std::chrono::steady_clock::now();
+  explicit LoadTimer(ish_ctx *c) : ctx(c) {}
+  ~LoadTimer() {
+    ctx->last_load_ms[2] =
+        std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+  }
+};
 
 // A failed runtime call also leaves the runtime's last-error state set;
 // it is cleared here so that the next call does not report it again.

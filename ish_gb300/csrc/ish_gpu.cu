@@ -423,6 +423,7 @@ int pack_set(ish_ctx *ctx, uint32_t n, uint64_t raw_bytes, const uint64_t *end, 
   CU(cudaMemsetAsync(ctx->max_code.p, 0, 8, s));
   CU(cudaMemsetAsync(counts, 0, (size_t)NBUCKETS * 4, s));
   const uint32_t nb = std::min<uint32_t>(ceil_div(n, 256), (uint32_t)ctx->num_sms * 16);
+  CU(cudaEventRecord(ctx->load_ev[1], s));
   k_lengths<<<nb, 256, 0, s>>>(ctx->off_in.as<uint64_t>(), end, n, ctx->len_tmp.as<uint32_t>(),
                                 ctx->slot_tmp.as<uint64_t>(), counts, max_code + 1);
   ++ctx->launches;
@@ -468,6 +469,7 @@ int pack_set(ish_ctx *ctx, uint32_t n, uint64_t raw_bytes, const uint64_t *end, 
                             ctx->poff_tmp.as<uint64_t>(), n, enc, rs.codes.as<uint8_t>(), max_code);
   ++ctx->launches;
   CU(cudaGetLastError());
+  CU(cudaEventRecord(ctx->load_ev[2], s));
   // host copy of the histogram: the buckets of lengths up to HIST_HEAD in the
   // same round trip as the largest code and bucket, the rest (long records
   // only) after it
@@ -486,6 +488,10 @@ int pack_set(ish_ctx *ctx, uint32_t n, uint64_t raw_bytes, const uint64_t *end, 
   }
   rs.n_empty = rs.hist[0];
   rs.max_len = maxb < 32768 ? maxb : (uint32_t)(32768 + ((uint64_t)(maxb - 32768) << 5) + 31);
+  float a = 0.f, b = 0.f;
+  if (cudaEventElapsedTime(&a, ctx->load_ev[0], ctx->load_ev[1]) == cudaSuccess) ctx->last_load_ms[0] = a;
+  if (cudaEventElapsedTime(&b, ctx->load_ev[1], ctx->load_ev[2]) == cudaSuccess) ctx->last_load_ms[1] = b;
+  (void)cudaGetLastError();
   return ISH_OK;
 }
 
@@ -506,6 +512,7 @@ int load_records(ish_ctx *ctx, const uint8_t *records, const uint64_t *offsets, 
   cudaStream_t s = ctx->stream;
   // raw bytes (+16 slack for the realigning pack loads)
   CU(ctx->raw.ensure(bytes + 32));
+  CU(cudaEventRecord(ctx->load_ev[0], s));
   if (bytes) CU(cudaMemcpyAsync(ctx->raw.p, records + base, bytes, cudaMemcpyHostToDevice, s));
   CU(ctx->off_in.ensure((size_t)(n + 1) * 8));
   if (base == 0) {
@@ -529,6 +536,7 @@ int load_lines(ish_ctx *ctx, const uint8_t *text, uint64_t bytes, RecordSet &rs,
   if (!text) return fail(ctx, ISH_EINVAL, "text is NULL");
   cudaStream_t s = ctx->stream;
   CU(ctx->raw.ensure(bytes + 32));
+  CU(cudaEventRecord(ctx->load_ev[0], s));
   CU(cudaMemcpyAsync(ctx->raw.p, text, bytes, cudaMemcpyHostToDevice, s));
   const uint64_t tiles64 = (bytes + LINE_TILE - 1) / LINE_TILE;
   if (tiles64 > 0x7fffffffull) return fail(ctx, ISH_EINVAL, "text too large");
@@ -859,9 +867,15 @@ int fetch_outputs(ish_ctx *ctx, uint32_t n, int32_t *score, int32_t *qend, int32
   uint32_t total = 0;
   CU(cudaMemcpyAsync(&herr, ctx->error.p, 4, cudaMemcpyDeviceToHost, s));
   if (compact) CU(cudaMemcpyAsync(&total, ctx->nhits.p, 4, cudaMemcpyDeviceToHost, s));
+  // the first hit indices travel with the count (hit_idx holds n entries, so
+  // the prefix fits whatever the count); the rest, if any, after it
+  constexpr uint32_t HIT_PREFIX = 4096;
+  const uint32_t prefix = std::min<uint32_t>(n, HIT_PREFIX);
+  if (hit_idx && compact) CU(cudaMemcpyAsync(hit_idx, ctx->hit_idx.p, (size_t)prefix * 4, cudaMemcpyDeviceToHost, s));
   CU(cudaStreamSynchronize(s));
-  if (hit_idx && total) {
-    CU(cudaMemcpyAsync(hit_idx, ctx->hit_idx.p, (size_t)total * 4, cudaMemcpyDeviceToHost, s));
+  if (hit_idx && total > prefix) {
+    CU(cudaMemcpyAsync(hit_idx + prefix, ctx->hit_idx.as<uint32_t>() + prefix, (size_t)(total - prefix) * 4,
+                       cudaMemcpyDeviceToHost, s));
     CU(cudaStreamSynchronize(s));
   }
   if (n_hits) *n_hits = total;
@@ -906,6 +920,8 @@ int ish_gpu_open(int device, ish_ctx **out) {
     return bail(e, "cudaStreamCreate");
   if ((e = cudaEventCreate(&ctx->ev0)) != cudaSuccess) return bail(e, "cudaEventCreate");
   if ((e = cudaEventCreate(&ctx->ev1)) != cudaSuccess) return bail(e, "cudaEventCreate");
+  for (cudaEvent_t &ev : ctx->load_ev)
+    if ((e = cudaEventCreate(&ev)) != cudaSuccess) return bail(e, "cudaEventCreate");
   *out = ctx;
   return ISH_OK;
 }
@@ -929,6 +945,7 @@ void ish_gpu_close(ish_ctx *ctx) {
   ctx->fastx.release();
   cudaEventDestroy(ctx->ev0);
   cudaEventDestroy(ctx->ev1);
+  for (cudaEvent_t ev : ctx->load_ev) cudaEventDestroy(ev);
   cudaStreamDestroy(ctx->stream);
   delete ctx;
 }
@@ -1058,6 +1075,7 @@ int ish_gpu_free_query(ish_ctx *ctx, int32_t query_id) {
 
 int ish_gpu_records_load(ish_ctx *ctx, const uint8_t *records, const uint64_t *offsets, uint32_t n, int32_t *set_id) {
   if (!ctx || !set_id) return ctx ? fail(ctx, ISH_EINVAL, "set_id is NULL") : ISH_EINVAL;
+  LoadTimer timer(ctx);
   cudaSetDevice(ctx->device);
   RecordSet rs;
   int rc = load_records(ctx, records, offsets, n, rs, nullptr);
@@ -1074,6 +1092,7 @@ int ish_gpu_records_load(ish_ctx *ctx, const uint8_t *records, const uint64_t *o
 int ish_gpu_records_load_raw(ish_ctx *ctx, const uint8_t *raw, const uint64_t *offsets, uint32_t n, int matrix_kind,
                              int32_t *set_id) {
   if (!ctx || !set_id) return ctx ? fail(ctx, ISH_EINVAL, "set_id is NULL") : ISH_EINVAL;
+  LoadTimer timer(ctx);
   cudaSetDevice(ctx->device);
   const uint8_t *enc = nullptr;
   int rc = device_encoding(ctx, matrix_kind, &enc);
@@ -1093,6 +1112,7 @@ int ish_gpu_records_load_raw(ish_ctx *ctx, const uint8_t *raw, const uint64_t *o
 int ish_gpu_records_load_lines(ish_ctx *ctx, const uint8_t *text, uint64_t bytes, int matrix_kind, int32_t *set_id,
                                uint32_t *n_records) {
   if (!ctx || !set_id) return ctx ? fail(ctx, ISH_EINVAL, "set_id is NULL") : ISH_EINVAL;
+  LoadTimer timer(ctx);
   cudaSetDevice(ctx->device);
   const uint8_t *enc = nullptr;
   int rc = device_encoding(ctx, matrix_kind, &enc);
@@ -1225,6 +1245,14 @@ int ish_gpu_last_windows(ish_ctx *ctx, uint32_t *windows) {
 int ish_gpu_last_kernel_ms(ish_ctx *ctx, double *ms) {
   if (!ctx || !ms) return ISH_EINVAL;
   *ms = ctx->last_ms;
+  return ISH_OK;
+}
+
+int ish_gpu_last_load_ms(ish_ctx *ctx, double *upload_ms, double *pack_ms, double *wall_ms) {
+  if (!ctx) return ISH_EINVAL;
+  if (upload_ms) *upload_ms = ctx->last_load_ms[0];
+  if (pack_ms) *pack_ms = ctx->last_load_ms[1];
+  if (wall_ms) *wall_ms = ctx->last_load_ms[2];
   return ISH_OK;
 }
 

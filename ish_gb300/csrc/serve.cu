@@ -5,9 +5,9 @@
 // admits waiting requests while an active slot is free and the device memory
 // their outputs need fits the budget (profiles live in shared memory and DP
 // rows in registers, so outputs are what a request costs).  A step scores the
-// next chunk of the record set (the set split into chunks of equal residue
-// count, in descending length order) for EVERY active request, in one batched
-// launch: one persistent batch_kernel per shape class, whose blocks steal
+// next chunk of the record set (chunk c of n: every n-th record pair of the
+// descending length order from pair c) for EVERY active request, in one
+// batched launch: one persistent batch_kernel per shape class, whose blocks steal
 // record pairs from per-(request, chunk) counters, so the work of all active
 // requests overlaps on the device.  A request that has run its last chunk is
 // compacted (hit list, scores and ends of the hits) and handed to poll; new
@@ -268,8 +268,14 @@ int step(Server &S, char *msg) {
     cls[c].first = k;
     for (Request *r : members[c]) {
       S.h_params[k] = r->params;
-      const auto &ch = S.chunks[r->next_chunk];
-      S.h_tiles[k] = BatchTile{k - cls[c].first, ch.first, ch.second, 0};
+      // the wavefront requests' chunk c is every nch-th record pair of the
+      // set from pair c: each step meets the whole length distribution
+      // (longest pairs first), so its kernels end as evenly as a pass over
+      // the whole set (contiguous chunks of the longest-first order made the
+      // steps of the long records end on a few long pairs)
+      const uint32_t nch = (uint32_t)S.chunks.size();
+      const uint32_t nonempty = rs.n - rs.n_empty;
+      S.h_tiles[k] = BatchTile{k - cls[c].first, 0, nonempty, nch > 1 ? (nch << 16) | r->next_chunk : 0u};
       ++k;
     }
     cls[c].count = k - cls[c].first;

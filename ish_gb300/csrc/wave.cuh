@@ -80,7 +80,10 @@ __device__ __forceinline__ void wave_rows(const WaveParams &p, const unsigned ch
   const int f0 = (MODE == SG) ? p.ext : 0;  // row -1 sits in frame -ext
   const bool te = (MODE == SG) && (p.ends & 8);
   const bool qe = (MODE == SG) && (p.ends & 2);
-  const uint32_t npairs = (p.count + 1) >> 1;
+  // record pairs of the range: every pair_stride-th from pair_phase
+  const uint32_t pstride = p.pair_stride ? p.pair_stride : 1u, pphase = p.pair_stride ? p.pair_phase : 0u;
+  const uint32_t npairs_all = (p.count + 1) >> 1;
+  const uint32_t npairs = npairs_all > pphase ? (npairs_all - pphase + pstride - 1) / pstride : 0u;
   const int col0 = t * K - p.d;  // query column of register 0
   // parameters read every step, held in registers (the batched kernel's
   // parameters live in shared memory)
@@ -419,8 +422,9 @@ __device__ __forceinline__ void wave_rows(const WaveParams &p, const unsigned ch
 
     if (t0) {
       if (f_left <= 0 && !f_done) {
-        const uint32_t np = atomicAdd(counter, 1u);
-        if (np < npairs) {
+        const uint32_t nt = atomicAdd(counter, 1u);
+        if (nt < npairs) {
+          const uint32_t np = nt * pstride + pphase;  // the pair's index in the range
           f_seq = (f_seq + 1) & 31;
           slots[f_seq] = np;
           const uint32_t sA = p.first + 2 * np;
@@ -666,11 +670,15 @@ __global__ void __launch_bounds__(wave_threads_lean(K, MODE, LEAN), wave_blocks_
     uint32_t *counter = b.tile_counter + tile;
     if (threadIdx.x == 0) {
       const uint32_t taken = *reinterpret_cast<volatile uint32_t *>(counter);
-      s_skip = taken >= (tl.count + 1) / 2;
+      const uint32_t stride = tl.pairs >> 16, phase = tl.pairs & 0xffffu, all = (tl.count + 1) / 2;
+      const uint32_t mine = stride ? (all > phase ? (all - phase + stride - 1) / stride : 0u) : all;
+      s_skip = taken >= mine;
       if (!s_skip) {
         sp = *qp;
         sp.first = tl.first;
         sp.count = tl.count;
+        sp.pair_stride = stride;
+        sp.pair_phase = phase;
         // every group's steps are bounded by all pairs of the range at its
         // longest length (records are sorted, the first is longest)
         const uint64_t npairs = (tl.count + 1) / 2;

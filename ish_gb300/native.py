@@ -33,7 +33,7 @@ EXPORTS = (
     "ish_gpu_score_noalloc", "ish_gpu_score_multi", "ish_gpu_autotune", "ish_gpu_serve_start", "ish_gpu_submit",
     "ish_gpu_poll", "ish_gpu_serve_stop", "ish_gpu_serve_stats", "ish_gpu_match_starts",
     "ish_gpu_launch_count", "ish_gpu_records_load_raw", "ish_gpu_records_load_lines", "ish_gpu_last_windows",
-    "ish_gpu_calibrate_lanes", "ish_gpu_records_load_fastx", "ish_gpu_records_get",
+    "ish_gpu_calibrate_lanes", "ish_gpu_records_load_fastx", "ish_gpu_records_get", "ish_gpu_last_load_ms",
 )
 
 
@@ -88,6 +88,7 @@ def load(build_if_missing: bool = False):
     L.ish_gpu_records_info.argtypes = [vp, C.c_int32, u32p, u64p]
     L.ish_gpu_score_set.argtypes = [vp, C.c_int32, C.c_int32, i32p, i32p, i32p, u8p, u32p, u32p]
     L.ish_gpu_last_kernel_ms.argtypes = [vp, C.POINTER(C.c_double)]
+    L.ish_gpu_last_load_ms.argtypes = [vp, C.POINTER(C.c_double), C.POINTER(C.c_double), C.POINTER(C.c_double)]
     L.ish_gpu_calibrate.argtypes = [vp, C.POINTER(C.c_double)]
     L.ish_gpu_calibrate_lanes.argtypes = [vp, C.POINTER(C.c_double), C.POINTER(C.c_double)]
     L.ish_gpu_score_noalloc.argtypes = [vp, C.c_uint64, vp, C.c_uint32, u8p, C.c_uint32, i8p, C.c_uint32, C.c_int,
@@ -183,17 +184,27 @@ class Context:
     def free_query(self, qid: int):
         self._check(self._L.ish_gpu_free_query(self._h, qid))
 
-    def _outputs(self, n, want):
+    def _outputs(self, n, want, out=None):
+        """Output arrays for n records: the caller's (`out`, e.g. pinned host
+        buffers reused across calls) where given and large enough, else new."""
+        given = out or {}
+        types = {"score": np.int32, "qend": np.int32, "tend": np.int32, "hit": np.uint8, "hit_idx": np.uint32}
         out = {}
-        if "score" in want:
+        for k in want:
+            a = given.get(k)
+            if a is not None:
+                if a.dtype != types[k] or len(a) < max(n, 1) or not a.flags.c_contiguous:
+                    raise ValueError(f"output {k}: needs a contiguous {np.dtype(types[k])} array of {max(n, 1)}")
+                out[k] = a
+        if "score" in want and "score" not in out:
             out["score"] = np.empty(max(n, 1), np.int32)
-        if "qend" in want:
+        if "qend" in want and "qend" not in out:
             out["qend"] = np.empty(max(n, 1), np.int32)
-        if "tend" in want:
+        if "tend" in want and "tend" not in out:
             out["tend"] = np.empty(max(n, 1), np.int32)
-        if "hit" in want:
+        if "hit" in want and "hit" not in out:
             out["hit"] = np.empty(max(n, 1), np.uint8)
-        if "hit_idx" in want:
+        if "hit_idx" in want and "hit_idx" not in out:
             out["hit_idx"] = np.empty(max(n, 1), np.uint32)
         return out
 
@@ -279,9 +290,12 @@ class Context:
         self._check(self._L.ish_gpu_records_info(self._h, sid, C.byref(n), C.byref(b)))
         return n.value, b.value
 
-    def score_set(self, qid: int, sid: int, want=("score", "qend", "tend", "hit", "hit_idx")) -> dict:
+    def score_set(self, qid: int, sid: int, want=("score", "qend", "tend", "hit", "hit_idx"), out=None) -> dict:
+        """Scores query `qid` against set `sid`.  `out` may hold the caller's
+        output arrays (any of score/qend/tend/hit/hit_idx, at least n long);
+        the results are views of them."""
         n, _ = self.records_info(sid)
-        out = self._outputs(n, want)
+        out = self._outputs(n, want, out)
         nh = C.c_uint32()
         self._check(self._L.ish_gpu_score_set(self._h, qid, sid, _p(out.get("score"), C.c_int32),
                                               _p(out.get("qend"), C.c_int32), _p(out.get("tend"), C.c_int32),
@@ -382,6 +396,13 @@ class Context:
                                                 C.byref(steps)))
         return {"completed": done.value, "cells": cells.value, "device_ms": ms.value, "max_active": mx.value,
                 "steps": steps.value}
+
+    def last_load_ms(self) -> dict:
+        """Phases of the last record load: device upload (+ splitting),
+        device packing, host wall time of the call (ms)."""
+        a, b, c = C.c_double(), C.c_double(), C.c_double()
+        self._check(self._L.ish_gpu_last_load_ms(self._h, C.byref(a), C.byref(b), C.byref(c)))
+        return {"upload": a.value, "pack": b.value, "wall": c.value}
 
     def calibrate(self) -> float:
         """Packed 16-bit DPX add-max instructions per second on this device."""

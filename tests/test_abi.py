@@ -96,3 +96,23 @@ def test_output_writer_formats():
     got = []
     output.write_fastx_matches(got.append, [b"r0", b"r1", b"r2"], buf, off, [(0, 2, 4)], m.code_to_ascii, tty=True)
     assert b"".join(got) == b">r0\nAC\x1b[1;31m\x1b[31mGT\x1b[0mNN\n"
+
+
+def test_caller_output_buffers_are_checked():
+    # score_set(out=...) writes into the caller's arrays (e.g. pinned host
+    # buffers reused across calls) only when they fit the contract
+    import numpy as np
+
+    from ish_gb300 import native
+
+    good = {"score": np.zeros(10, np.int32), "hit_idx": np.zeros(10, np.uint32)}
+    out = native.Context._outputs(None, 10, ("score", "hit_idx", "tend"), good)
+    assert out["score"] is good["score"] and out["hit_idx"] is good["hit_idx"]
+    assert out["tend"].dtype == np.int32 and len(out["tend"]) == 10
+    for bad in ({"score": np.zeros(9, np.int32)}, {"score": np.zeros(10, np.int64)},
+                {"score": np.zeros(20, np.int32)[::2]}):
+        try:
+            native.Context._outputs(None, 10, ("score",), bad)
+        except ValueError:
+            continue
+        raise AssertionError(f"accepted {bad}")
