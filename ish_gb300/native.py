@@ -209,11 +209,13 @@ class Context:
         return out
 
     def score(self, qid: int, records: np.ndarray, offsets: np.ndarray,
-              want=("score", "qend", "tend", "hit", "hit_idx")) -> dict:
+              want=("score", "qend", "tend", "hit", "hit_idx"), out=None) -> dict:
+        """One-shot scoring of host records (ish_gpu_score): upload, pack,
+        score, results back in one call.  `out` as for score_set."""
         records = np.ascontiguousarray(records, np.uint8)
         offsets = np.ascontiguousarray(offsets, np.uint64)
         n = len(offsets) - 1
-        out = self._outputs(n, want)
+        out = self._outputs(n, want, out)
         nh = C.c_uint32()
         self._check(self._L.ish_gpu_score(self._h, qid, _p(records, C.c_uint8), _p(offsets, C.c_uint64), n,
                                           _p(out.get("score"), C.c_int32), _p(out.get("qend"), C.c_int32),
