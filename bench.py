@@ -13,7 +13,11 @@ seconds / 1e9 (ish's own definition, benchmarking/ish_bench_aligner.mojo:740-750
             resident in HBM (CUDA events on the engine stream); the record
             stream (~419 MB) is larger than L2, so every pass reads HBM.
   e2e       the same step through the C ABI from pinned host buffers: upload
-            records, score both passes, copy scores/ends/hits back.
+            records, score both passes, copy scores/ends/hits back.  Before
+            each step (untimed) the batch is written into the pinned buffer,
+            as a runner fills its batch buffer from a file: a pinned buffer
+            left untouched by the CPU for 0.1-1 s was measured to upload at
+            30-110 GB/s instead of 211 GB/s on some GB300 hosts.
   roofline  integer cell-update roofline: measured DPX add-max throughput x 2
             cells per instruction / DPX instructions per cell pair (4 for
             semi-global, 5 for local; 4.5 cell-weighted over the step).
@@ -304,6 +308,16 @@ def serving_leg(local, gb, count, rates=None):
                        f"{count} queries per rate, Q ~ U[20,2000], striped-local / semi-global FFTT mix, gap 10/1, "
                        "threshold 0.8", "records": wl.n, "residues": residues}
 
+    deadline = time.perf_counter() + 900.0  # the whole leg; a stuck query fails it instead of hanging the run
+
+    def wait(ctx, t):
+        r = None
+        while r is None:
+            if time.perf_counter() > deadline:
+                raise TimeoutError("serving leg: a query did not complete within the leg's 900 s")
+            r = ctx.poll(t, wait_ms=200)
+        return r
+
     def make(ctx, qs):
         ids = []
         for _, algo, q in qs:
@@ -333,9 +347,7 @@ def serving_leg(local, gb, count, rates=None):
         tickets = [ctx.submit(q) for q in pids]
         same = True
         for t, want in zip(tickets, alone):
-            r = None
-            while r is None:
-                r = ctx.poll(t, wait_ms=200)
+            r = wait(ctx, t)
             same = same and np.array_equal(r["hit_idx"], want)
         st = ctx.serve_stats()
         ctx.serve_stop()
@@ -355,12 +367,7 @@ def serving_leg(local, gb, count, rates=None):
                 if arrival > now:
                     time.sleep(arrival - now)
                 tickets.append(ctx.submit(qid))
-            lat = []
-            for t in tickets:
-                r = None
-                while r is None:
-                    r = ctx.poll(t, wait_ms=200)
-                lat.append(r["latency_ms"])
+            lat = [wait(ctx, t)["latency_ms"] for t in tickets]
             span = time.perf_counter() - start
             st = ctx.serve_stats()
             ctx.serve_stop()
@@ -480,6 +487,7 @@ def run_ours(args):
     e2e_ms = []
     outs_sg, outs_sw = _pinned_outputs(wl.n), _pinned_outputs(wl.n)
     for s in range(args.warmup + args.steps):
+        pin[:] = wl.records  # the step's batch, written as a runner fills its buffer (untimed)
         barrier(dist)
         t = time.perf_counter()
         sid2 = ctx.records_load(pin, pin_off)
@@ -493,6 +501,56 @@ def run_ours(args):
     n = wl.n
     h2d = int(len(wl.records) + 8 * len(wl.offsets))
     d2h = int(2 * (12 * n + 4 * 8 + 4 * sum(hits)))
+
+    # ---- streamed: the step's records as 4 batches; each batch's upload and
+    # packing run on the load stream while the previous batch is scored
+    # (ish_gpu_records_load_async), as a runner streams batches of a file ----
+    streamed = None
+    try:
+        import torch
+
+        nbat = 4
+        cut = np.linspace(0, wl.n, nbat + 1).astype(np.int64)
+        bats = []
+        for b in range(nbat):
+            lo, hi = int(cut[b]), int(cut[b + 1])
+            o0, o1 = int(wl.offsets[lo]), int(wl.offsets[hi])
+            br = torch.empty(max(1, o1 - o0), dtype=torch.uint8, pin_memory=True).numpy()[: o1 - o0]
+            bo = torch.empty(hi - lo + 1, dtype=torch.int64, pin_memory=True).numpy().view(np.uint64)
+            bo[:] = wl.offsets[lo:hi + 1] - wl.offsets[lo]
+            bats.append((br, bo, lo, hi, o0, o1))
+        bout_sg, bout_sw = _pinned_outputs(int(max(c[3] - c[2] for c in bats))), _pinned_outputs(
+            int(max(c[3] - c[2] for c in bats)))
+        st_ms, st_seq_ms = [], []
+        for mode in ("async", "sync"):
+            for s in range(args.warmup + args.steps):
+                for br, bo, lo, hi, o0, o1 in bats:
+                    br[:] = wl.records[o0:o1]  # the batches, freshly written (untimed)
+                barrier(dist)
+                t = time.perf_counter()
+                nh_st = 0
+                if mode == "async":
+                    sid_b = ctx.records_load_async(bats[0][0], bats[0][1])
+                for b in range(nbat):
+                    if mode == "async":
+                        nxt = ctx.records_load_async(bats[b + 1][0], bats[b + 1][1]) if b + 1 < nbat else None
+                    else:
+                        sid_b = ctx.records_load(bats[b][0], bats[b][1])
+                    r1 = ctx.score_set(q_sg, sid_b, want=("score", "qend", "tend", "hit_idx"), out=bout_sg)
+                    r2 = ctx.score_set(q_sw, sid_b, want=("score", "qend", "tend", "hit_idx"), out=bout_sw)
+                    nh_st += len(r1["hit_idx"]) + len(r2["hit_idx"])
+                    ctx.records_free(sid_b)
+                    if mode == "async":
+                        sid_b = nxt
+                if s >= args.warmup:
+                    (st_ms if mode == "async" else st_seq_ms).append(1e3 * (time.perf_counter() - t))
+        streamed = {"value": round(world * cells / (reduce_max(dist, float(np.mean(st_ms))) * 1e-3) / 1e9, 2),
+                    "unit": "GCUPS", "batches": nbat,
+                    "same_records_loaded_one_by_one_gcups": round(
+                        world * cells / (reduce_max(dist, float(np.mean(st_seq_ms))) * 1e-3) / 1e9, 2),
+                    "hits_equal": bool(nh_st == sum(hits))}
+    except Exception as e:  # reported, not fatal
+        streamed = {"error": f"{type(e).__name__}: {e}"}
 
     # ---- plain one-thread-per-record kernels (the in-GPU comparison), on a
     # random tenth of the records: int32 columns in global scratch, and int16
@@ -598,6 +656,7 @@ def run_ours(args):
             "gpu_launches": launches,
             "clocks": clk,
             "plain_kernel_gcups": plain,
+            "e2e_streamed": streamed,
             "lane_width": lanes,
             "wall_ms_per_step": round(wall_ms, 3),
             "hits": {"semi_global": hits[0], "local": hits[1]},
@@ -864,6 +923,9 @@ def run_workload(args):
     nh = 0
     outs = _pinned_outputs(wl.n)
     for s in range(args.warmup + args.steps):
+        # the step's batch is written into the pinned buffer first, as a
+        # runner fills its batch buffer from a file (untimed)
+        pin[:] = wl.records
         barrier(dist)
         t = time.perf_counter()
         if name == "line":
@@ -948,20 +1010,28 @@ def run_workload(args):
             text = tp
         except Exception:
             pass
-        tl, tload = [], []
+        text_src = text.copy()
+        tl, tload, tphase = [], [], []
         for s in range(args.warmup + args.steps):
+            text[:] = text_src  # the file's bytes, freshly read (untimed)
             t = time.perf_counter()
             sid4, nr, _ = ctx.records_load_fastx(text, wl.kind, bounds=False)
             t1 = time.perf_counter()
+            lp = ctx.last_load_ms()
             r = ctx.score_multi(qids, sid4, want=("hit_idx",))
             ctx.records_free(sid4)
             if s >= args.warmup:
                 tl.append(1e3 * (time.perf_counter() - t))
                 tload.append(1e3 * (t1 - t))
+                tphase.append((lp["upload"], lp["pack"]))
+        del text_src
         same = nr == wl.n and all(np.array_equal(a, b) for a, b in zip(r["hit_idx"], res["hit_idx"]))
         extra["e2e_from_fastq"] = {"value": round(cells / (float(np.mean(tl)) * 1e-3) / 1e9, 2), "unit": "GCUPS",
                                    "h2d_bytes_per_step": len(text), "records": int(nr),
-                                   "load_ms": round(float(np.mean(tload)), 2), "hits_equal": bool(same)}
+                                   "load_ms": round(float(np.mean(tload)), 2),
+                                   "load_upload_and_split_device_ms": round(float(np.mean([x[0] for x in tphase])), 2),
+                                   "load_pack_device_ms": round(float(np.mean([x[1] for x in tphase])), 2),
+                                   "hits_equal": bool(same)}
         del text
     cpu = None
     parity = None

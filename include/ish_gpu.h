@@ -87,6 +87,8 @@ extern "C" {
 #define ISH_OPT_WAVE_BLOCKS 8 /* cap wavefront blocks per SM (0 = as many as fit) */
 #define ISH_OPT_WINDOWS 10    /* 1 (default): window long records when they would bound the pass; 0: never */
 #define ISH_OPT_WAVE_LEAN 9   /* 34 <= K <= 48: -1 measured default, 0 128x3 blocks, 1 128x2 (more registers) */
+#define ISH_OPT_SERVE_STEP_CELLS 13 /* serving: cells a step aims at per query (default 1.25e11); a query takes
+                                    * cells/that steps, 1..chunks; 0: every query takes `chunks` steps */
 /* Fault injection for testing a caller's error paths (no counterpart in the
  * reference).  ISH_OPT_STEP_BUDGET: 0 (default) lets every wavefront and
  * batched launch of this context run to the end of its work; n > 0 caps each
@@ -148,6 +150,17 @@ ISH_API int ish_gpu_score(ish_ctx *ctx, int32_t query_id, const uint8_t *records
 ISH_API int ish_gpu_records_load(ish_ctx *ctx, const uint8_t *records, const uint64_t *offsets, uint32_t n,
                          int32_t *set_id);
 ISH_API int ish_gpu_records_free(ish_ctx *ctx, int32_t set_id);
+/* As ish_gpu_records_load, but returns as soon as the upload and packing are
+ * queued on the context's load stream, so that they overlap the scoring of
+ * another set: load batch k + 1 with this call, then score batch k.  One load
+ * is in flight per context: it completes (the call waits for it) when its set
+ * is first used, when another load starts, and in ish_gpu_close.  `records`
+ * and `offsets` must stay valid and unchanged until then (pinned host memory
+ * is read by the copy engine while the call has already returned).  Replaces
+ * the synchronous per-batch upload of ishlib/gpu/process_batch.mojo:112-132,
+ * where the CPU packs the next batch while the device scores. */
+ISH_API int ish_gpu_records_load_async(ish_ctx *ctx, const uint8_t *records, const uint64_t *offsets, uint32_t n,
+                                       int32_t *set_id);
 /* Number of records and total residue bytes of a resident set. */
 ISH_API int ish_gpu_records_info(ish_ctx *ctx, int32_t set_id, uint32_t *n, uint64_t *total_bytes);
 
@@ -257,10 +270,11 @@ ISH_API int ish_gpu_match_starts(ish_ctx *ctx, int32_t query_id, int32_t set_id,
  * the context admits waiting queries while fewer than max_active run and the
  * device memory their outputs need (29 bytes per record of the set) fits
  * mem_budget (0: half of the free device memory), and runs steps: each step
- * scores the next of `chunks` chunks of the set (chunk c: every chunks-th
- * record pair of the set's longest-first order, from pair c) for every
- * admitted query in one batched launch, so queries that arrive while others
- * run join at the next step and share the device with them.  Results are
+ * scores the next chunk of the set for every admitted query in one batched
+ * launch, so queries that arrive while others run join at the next step and
+ * share the device with them.  A query takes between 1 and `chunks` steps,
+ * as many as keep a step near ISH_OPT_SERVE_STEP_CELLS cells (its chunk c of
+ * m: every m-th record pair of the set's longest-first order, from pair c).  Results are
  * identical to ish_gpu_score_set.  submit and poll may be called from any
  * thread; the other calls on the context stay on one thread. */
 ISH_API int ish_gpu_serve_start(ish_ctx *ctx, int32_t set_id, uint32_t max_active, uint64_t mem_budget,

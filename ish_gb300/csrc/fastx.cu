@@ -34,9 +34,6 @@
 #include "host.h"
 
 namespace ish {
-namespace host {
-int pack_set(ish_ctx *ctx, uint32_t n, uint64_t raw_bytes, const uint64_t *end, const uint8_t *enc, RecordSet &rs);
-}
 
 namespace {
 
@@ -299,19 +296,22 @@ __global__ void k_fx_check(uint32_t nrec, const uint64_t *rec_off, const uint64_
   }
 }
 
-// Sequence bytes of every line into their records' places.
+// Sequence bytes of every line into their records' places: one warp per
+// line, lane k copying bytes k, k + 32, ... (coalesced on both sides).
 __global__ void k_fx_gather(const uint8_t *text, uint32_t n, const uint8_t *role, const uint64_t *len,
                             const uint64_t *src, const uint64_t *pos, uint8_t *out) {
-  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+  const uint32_t lane = threadIdx.x & 31;
+  const uint32_t warps = (gridDim.x * blockDim.x) >> 5;
+  for (uint32_t i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; i < n; i += warps) {
     const uint64_t ln = len[i];
     if (!ln) continue;
     uint8_t *d = out + pos[i];
     if (role[i] == R_EMPTY) {
-      d[0] = '\n';
+      if (lane == 0) d[0] = '\n';
       continue;
     }
     const uint8_t *s = text + src[i];
-    for (uint64_t k = 0; k < ln; ++k) d[k] = s[k];
+    for (uint64_t k = lane; k < ln; k += 32) d[k] = s[k];
   }
 }
 
@@ -473,7 +473,8 @@ int load_fastx(ish_ctx *ctx, const uint8_t *text, uint64_t bytes, RecordSet &rs,
   uint64_t used = 0;
   if (nr) CU(cudaMemcpyAsync(&used, fx.rec_off.as<uint64_t>() + nr, 8, cudaMemcpyDeviceToHost, s));
   CU(fx.seq.ensure(seq_bytes + 32));
-  k_fx_gather<<<gb, 256, 0, s>>>(dtext, n, fx.role.as<uint8_t>(), fx.len.as<uint64_t>(), fx.src.as<uint64_t>(),
+  const uint32_t gw = std::max<uint32_t>(1, std::min<uint32_t>(ceil_div((uint64_t)n * 32, 256), (uint32_t)ctx->num_sms * 32));
+  k_fx_gather<<<gw, 256, 0, s>>>(dtext, n, fx.role.as<uint8_t>(), fx.len.as<uint64_t>(), fx.src.as<uint64_t>(),
                                  fx.pos.as<uint64_t>(), fx.seq.as<uint8_t>());
   ++ctx->launches;
   CU(cudaGetLastError());
@@ -499,6 +500,7 @@ int ish_gpu_records_load_fastx(ish_ctx *ctx, const uint8_t *text, uint64_t bytes
                                uint32_t *n_records, uint64_t *bounds, uint64_t bounds_cap) {
   if (!ctx) return ISH_EINVAL;
   if (!set_id) return fail(ctx, ISH_EINVAL, "set_id is NULL");
+  if (int rc0 = finish_pending_load(ctx)) return rc0;
   LoadTimer timer(ctx);
   cudaSetDevice(ctx->device);
   const uint8_t *enc = nullptr;

@@ -130,6 +130,7 @@ struct WindowOut {
 };
 
 struct RecordSet {
+  bool pending = false;  // loaded asynchronously: its host-side summary is not read back yet
   uint32_t n = 0;
   uint64_t total = 0;
   uint32_t max_len = 0;
@@ -181,6 +182,10 @@ struct ish_ctx {
   int num_sms = 0;
   size_t mem_total = 0;  // device memory (bytes)
   cudaStream_t stream = nullptr;
+  cudaStream_t load_stream = nullptr;  // asynchronous record loads (ish_gpu_records_load_async)
+  cudaEvent_t load_done = nullptr;     // end of the asynchronous load in flight
+  uint32_t *h_summary = nullptr;       // pinned: its largest code, largest bucket, then the histogram
+  int32_t pending_set = 0;             // the set whose asynchronous load is in flight (0: none)
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
   cudaEvent_t load_ev[3] = {nullptr, nullptr, nullptr};  // last load: start, packing start, end
   double last_load_ms[3] = {0, 0, 0};                    // upload (+ splitting), packing, host wall
@@ -191,6 +196,7 @@ struct ish_ctx {
   int force_blocks = 0;  // cap on wavefront blocks per SM (0: occupancy limit)
   int force_lean = -1;   // lean kernel variant: -1 per (K, mode) default, 0 off, 1 on
   int windows_on = 1;    // window long records (windows.cu)
+  double serve_step_cells = 1.25e11;  // ISH_OPT_SERVE_STEP_CELLS
   uint64_t step_budget = 0;  // ISH_OPT_STEP_BUDGET: cap on pipeline steps per warp (0: the launch's own bound)
   std::map<int32_t, ish::host::Query> queries;
   int32_t next_query = 1;
@@ -257,6 +263,14 @@ int wave_lean(const ish_ctx *ctx, int K, int mode);
 int batch_lean(const ish_ctx *ctx, int K, int mode);
 uint64_t window_overlap(const Query &q);
 int launch_windows(ish_ctx *ctx, Query &q, RecordSet &rs, uint32_t nonempty, OutDev out, cudaStream_t s, bool *done);
+uint64_t window_stride(const ish_ctx *ctx, const RecordSet &rs, uint64_t O, int G, int K, int mode);
+int build_window_view(ish_ctx *ctx, const RecordSet &rs, uint32_t nonempty, uint64_t W, uint64_t O, WindowView &V,
+                      cudaStream_t s);
+RecordSet window_set(const RecordSet &rs, const WindowView &V);
+int merge_windows(ish_ctx *ctx, const RecordSet &rs, uint32_t nonempty, const WindowView &V, const Query &q,
+                  const int32_t *ws, const int32_t *wq, const int32_t *wt, OutDev out, cudaStream_t s,
+                  uint32_t *kernels);
+bool windowable_whole(const Query &q);  // the query runs windows past row 0 as it is (no fixed-start twin)
 Regime regime(const Query &q, int qpad);
 void release_query(Query &q);
 void release_set(RecordSet &rs);
@@ -273,7 +287,18 @@ size_t layout_bytes(int layout, int alphabet, int G, int K);
 int choose_layout(int alphabet, int G, int K, int mode);
 int build_wave_layout(ish_ctx *ctx, Query &q, int G, int K, int layout, WaveLayout **out);
 int load_records(ish_ctx *ctx, const uint8_t *records, const uint64_t *offsets, uint32_t n, RecordSet &rs,
-                 const uint8_t *enc);
+                 const uint8_t *enc, cudaStream_t s = nullptr, bool defer = false);
+// Sorts and packs the n records in ctx->raw ([off_in[i], end[i]) or, with end
+// NULL, [off_in[i], off_in[i + 1])) into rs on stream s (NULL: the context's
+// stream).  defer: the host-side summary of the set (histogram, largest code)
+// is read back when the set is first used (finish_pending_load), not now.
+int pack_set(ish_ctx *ctx, uint32_t n, uint64_t raw_bytes, const uint64_t *end, const uint8_t *enc, RecordSet &rs,
+             cudaStream_t s = nullptr, bool defer = false);
+// Completes an asynchronous load in flight (ish_gpu_records_load_async), if any.
+int finish_pending_load(ish_ctx *ctx);
+// The set, with its asynchronous load completed; nullptr (and the error) if
+// the id is unknown or the load failed.
+RecordSet *use_set(ish_ctx *ctx, int32_t set_id, int *rc);
 int load_lines(ish_ctx *ctx, const uint8_t *text, uint64_t bytes, RecordSet &rs, const uint8_t *enc, uint32_t *n_out);
 int device_encoding(ish_ctx *ctx, int kind, const uint8_t **out);
 void encoding_table(int kind, uint8_t t[256]);

@@ -408,8 +408,9 @@ int device_encoding(ish_ctx *ctx, int kind, const uint8_t **out) {
 // raw[off_in[i] .. end[i]) with `end` on the device, or raw[off_in[i] ..
 // off_in[i + 1]) without; `enc` (device, may be null) encodes bytes on the way
 // (see k_lengths .. k_pack in kernels.cu).  rs.total must hold the residue count.
-int pack_set(ish_ctx *ctx, uint32_t n, uint64_t raw_bytes, const uint64_t *end, const uint8_t *enc, RecordSet &rs) {
-  cudaStream_t s = ctx->stream;
+int pack_set(ish_ctx *ctx, uint32_t n, uint64_t raw_bytes, const uint64_t *end, const uint8_t *enc, RecordSet &rs,
+             cudaStream_t s, bool defer) {
+  if (!s) s = ctx->stream;
   rs.n = n;
   CU(ctx->len_tmp.ensure((size_t)n * 4));
   CU(ctx->slot_tmp.ensure((size_t)n * 8));
@@ -470,6 +471,14 @@ int pack_set(ish_ctx *ctx, uint32_t n, uint64_t raw_bytes, const uint64_t *end, 
   ++ctx->launches;
   CU(cudaGetLastError());
   CU(cudaEventRecord(ctx->load_ev[2], s));
+  if (defer) {
+    // the summary the host needs, read back when the set is first used
+    CU(cudaMemcpyAsync(ctx->h_summary, max_code, 8, cudaMemcpyDeviceToHost, s));
+    CU(cudaMemcpyAsync(ctx->h_summary + 2, counts, (size_t)NBUCKETS * 4, cudaMemcpyDeviceToHost, s));
+    CU(cudaEventRecord(ctx->load_done, s));
+    rs.pending = true;
+    return ISH_OK;
+  }
   // host copy of the histogram: the buckets of lengths up to HIST_HEAD in the
   // same round trip as the largest code and bucket, the rest (long records
   // only) after it
@@ -497,7 +506,7 @@ int pack_set(ish_ctx *ctx, uint32_t n, uint64_t raw_bytes, const uint64_t *end, 
 
 // Upload and pack a record set given as concatenated records + n+1 offsets.
 int load_records(ish_ctx *ctx, const uint8_t *records, const uint64_t *offsets, uint32_t n, RecordSet &rs,
-                 const uint8_t *enc) {
+                 const uint8_t *enc, cudaStream_t stream, bool defer) {
   if (n == 0) {
     rs.n = 0;
     rs.total = 0;
@@ -509,7 +518,7 @@ int load_records(ish_ctx *ctx, const uint8_t *records, const uint64_t *offsets, 
   const uint64_t bytes = end - base;
   if (bytes && !records) return fail(ctx, ISH_EINVAL, "records is NULL");
   rs.total = bytes;
-  cudaStream_t s = ctx->stream;
+  cudaStream_t s = stream ? stream : ctx->stream;
   // raw bytes (+16 slack for the realigning pack loads)
   CU(ctx->raw.ensure(bytes + 32));
   CU(cudaEventRecord(ctx->load_ev[0], s));
@@ -523,7 +532,52 @@ int load_records(ish_ctx *ctx, const uint8_t *records, const uint64_t *offsets, 
     CU(cudaMemcpyAsync(ctx->off_in.p, rebased.data(), (size_t)(n + 1) * 8, cudaMemcpyHostToDevice, s));
     CU(cudaStreamSynchronize(s));
   }
-  return pack_set(ctx, n, bytes, nullptr, enc, rs);
+  return pack_set(ctx, n, bytes, nullptr, enc, rs, s, defer);
+}
+
+// Completes the asynchronous load in flight: waits for its stream's work and
+// fills the set's host-side summary from the pinned staging copy.
+int finish_pending_load(ish_ctx *ctx) {
+  if (!ctx->pending_set) return ISH_OK;
+  const int32_t id = ctx->pending_set;
+  ctx->pending_set = 0;
+  auto it = ctx->sets.find(id);
+  const cudaError_t e = cudaEventSynchronize(ctx->load_done);
+  if (it == ctx->sets.end()) return ISH_OK;
+  RecordSet &rs = it->second;
+  rs.pending = false;
+  if (e != cudaSuccess) {
+    (void)cudaGetLastError();
+    release_set(rs);
+    ctx->sets.erase(it);
+    return fail(ctx, ISH_EDEVICE, "asynchronous load of record set %d failed: %s (the set is gone)", id,
+                cudaGetErrorString(e));
+  }
+  const uint32_t *h = ctx->h_summary;
+  rs.max_code = h[0];
+  const uint32_t maxb = std::min<uint32_t>(h[1], NBUCKETS - 1);
+  rs.hist.assign(h + 2, h + 2 + NBUCKETS);
+  rs.n_empty = rs.hist[0];
+  rs.max_len = maxb < 32768 ? maxb : (uint32_t)(32768 + ((uint64_t)(maxb - 32768) << 5) + 31);
+  float a = 0.f, b = 0.f;
+  if (cudaEventElapsedTime(&a, ctx->load_ev[0], ctx->load_ev[1]) == cudaSuccess) ctx->last_load_ms[0] = a;
+  if (cudaEventElapsedTime(&b, ctx->load_ev[1], ctx->load_ev[2]) == cudaSuccess) ctx->last_load_ms[1] = b;
+  (void)cudaGetLastError();
+  return ISH_OK;
+}
+
+RecordSet *use_set(ish_ctx *ctx, int32_t set_id, int *rc) {
+  auto it = ctx->sets.find(set_id);
+  if (it == ctx->sets.end()) {
+    *rc = fail(ctx, ISH_EINVAL, "unknown record set %d", set_id);
+    return nullptr;
+  }
+  if (it->second.pending) {
+    *rc = finish_pending_load(ctx);
+    if (*rc) return nullptr;
+  }
+  *rc = ISH_OK;
+  return &it->second;
 }
 
 // Upload a text buffer, split it into lines on the device and pack the lines
@@ -922,6 +976,12 @@ int ish_gpu_open(int device, ish_ctx **out) {
   if ((e = cudaEventCreate(&ctx->ev1)) != cudaSuccess) return bail(e, "cudaEventCreate");
   for (cudaEvent_t &ev : ctx->load_ev)
     if ((e = cudaEventCreate(&ev)) != cudaSuccess) return bail(e, "cudaEventCreate");
+  if ((e = cudaStreamCreateWithFlags(&ctx->load_stream, cudaStreamNonBlocking)) != cudaSuccess)
+    return bail(e, "cudaStreamCreate");
+  if ((e = cudaEventCreateWithFlags(&ctx->load_done, cudaEventDisableTiming)) != cudaSuccess)
+    return bail(e, "cudaEventCreate");
+  if ((e = cudaHostAlloc((void **)&ctx->h_summary, (size_t)(2 + NBUCKETS) * 4, cudaHostAllocDefault)) != cudaSuccess)
+    return bail(e, "cudaHostAlloc");
   *out = ctx;
   return ISH_OK;
 }
@@ -930,6 +990,7 @@ void ish_gpu_close(ish_ctx *ctx) {
   if (!ctx) return;
   cudaSetDevice(ctx->device);
   stop_server(ctx);
+  (void)finish_pending_load(ctx);
   cudaStreamSynchronize(ctx->stream);
   free_plans(ctx);
   for (auto &kv : ctx->queries) release_query(kv.second);
@@ -945,6 +1006,9 @@ void ish_gpu_close(ish_ctx *ctx) {
   ctx->fastx.release();
   cudaEventDestroy(ctx->ev0);
   cudaEventDestroy(ctx->ev1);
+  cudaEventDestroy(ctx->load_done);
+  cudaStreamDestroy(ctx->load_stream);
+  cudaFreeHost(ctx->h_summary);
   for (cudaEvent_t ev : ctx->load_ev) cudaEventDestroy(ev);
   cudaStreamDestroy(ctx->stream);
   delete ctx;
@@ -988,6 +1052,7 @@ int ish_gpu_set_option(ish_ctx *ctx, int option, int64_t value) {
     return ISH_OK;
   case ISH_OPT_WINDOWS:
     if (value != 0 && value != 1) return fail(ctx, ISH_EINVAL, "windows must be 0 or 1");
+    if (ctx->windows_on != (int)value) free_plans(ctx);  // batched plans window the set or not
     ctx->windows_on = (int)value;
     return ISH_OK;
   case ISH_OPT_WAVE_LEAN:
@@ -999,6 +1064,10 @@ int ish_gpu_set_option(ish_ctx *ctx, int option, int64_t value) {
     if (value < 0) return fail(ctx, ISH_EINVAL, "step budget must be >= 0");
     ctx->step_budget = (uint64_t)value;
     drop_plans(ctx, 0, 0);
+    return ISH_OK;
+  case ISH_OPT_SERVE_STEP_CELLS:
+    if (value < 0) return fail(ctx, ISH_EINVAL, "serving step cells must be >= 0");
+    ctx->serve_step_cells = (double)value;
     return ISH_OK;
   case ISH_OPT_FAULT_ALLOC:
     if (value < -1) return fail(ctx, ISH_EINVAL, "allocation fault countdown must be >= -1");
@@ -1075,6 +1144,7 @@ int ish_gpu_free_query(ish_ctx *ctx, int32_t query_id) {
 
 int ish_gpu_records_load(ish_ctx *ctx, const uint8_t *records, const uint64_t *offsets, uint32_t n, int32_t *set_id) {
   if (!ctx || !set_id) return ctx ? fail(ctx, ISH_EINVAL, "set_id is NULL") : ISH_EINVAL;
+  if (int rc0 = finish_pending_load(ctx)) return rc0;
   LoadTimer timer(ctx);
   cudaSetDevice(ctx->device);
   RecordSet rs;
@@ -1089,9 +1159,36 @@ int ish_gpu_records_load(ish_ctx *ctx, const uint8_t *records, const uint64_t *o
   return ISH_OK;
 }
 
+int ish_gpu_records_load_async(ish_ctx *ctx, const uint8_t *records, const uint64_t *offsets, uint32_t n,
+                               int32_t *set_id) {
+  if (!ctx || !set_id) return ctx ? fail(ctx, ISH_EINVAL, "set_id is NULL") : ISH_EINVAL;
+  // one load in flight: the previous one completes first (its scratch is reused)
+  if (int rc0 = finish_pending_load(ctx)) return rc0;
+  LoadTimer timer(ctx);
+  cudaSetDevice(ctx->device);
+  RecordSet rs;
+  // the load stream starts after the work already queued on the context's
+  // stream (a set freed just before may still be read there)
+  CU(cudaEventRecord(ctx->load_ev[0], ctx->stream));
+  CU(cudaStreamWaitEvent(ctx->load_stream, ctx->load_ev[0], 0));
+  int rc = load_records(ctx, records, offsets, n, rs, nullptr, ctx->load_stream, true);
+  if (rc) {
+    cudaStreamSynchronize(ctx->load_stream);
+    release_set(rs);
+    return rc;
+  }
+  const int32_t id = ctx->next_set++;
+  const bool pending = rs.pending;
+  ctx->sets.emplace(id, std::move(rs));
+  if (pending) ctx->pending_set = id;
+  *set_id = id;
+  return ISH_OK;
+}
+
 int ish_gpu_records_load_raw(ish_ctx *ctx, const uint8_t *raw, const uint64_t *offsets, uint32_t n, int matrix_kind,
                              int32_t *set_id) {
   if (!ctx || !set_id) return ctx ? fail(ctx, ISH_EINVAL, "set_id is NULL") : ISH_EINVAL;
+  if (int rc0 = finish_pending_load(ctx)) return rc0;
   LoadTimer timer(ctx);
   cudaSetDevice(ctx->device);
   const uint8_t *enc = nullptr;
@@ -1112,6 +1209,7 @@ int ish_gpu_records_load_raw(ish_ctx *ctx, const uint8_t *raw, const uint64_t *o
 int ish_gpu_records_load_lines(ish_ctx *ctx, const uint8_t *text, uint64_t bytes, int matrix_kind, int32_t *set_id,
                                uint32_t *n_records) {
   if (!ctx || !set_id) return ctx ? fail(ctx, ISH_EINVAL, "set_id is NULL") : ISH_EINVAL;
+  if (int rc0 = finish_pending_load(ctx)) return rc0;
   LoadTimer timer(ctx);
   cudaSetDevice(ctx->device);
   const uint8_t *enc = nullptr;
@@ -1133,9 +1231,11 @@ int ish_gpu_records_load_lines(ish_ctx *ctx, const uint8_t *text, uint64_t bytes
 
 int ish_gpu_records_free(ish_ctx *ctx, int32_t set_id) {
   if (!ctx) return ISH_EINVAL;
-  auto it = ctx->sets.find(set_id);
-  if (it == ctx->sets.end()) return fail(ctx, ISH_EINVAL, "unknown record set %d", set_id);
+  int urc = ISH_OK;
+  RecordSet *it_set = use_set(ctx, set_id, &urc);
+  if (!it_set) return urc;
   if (server_uses_set(ctx, set_id)) return fail(ctx, ISH_EINVAL, "record set %d is used by the serving loop", set_id);
+  auto it = ctx->sets.find(set_id);
   cudaStreamSynchronize(ctx->stream);
   drop_plans(ctx, 0, set_id);
   recycle_set(ctx, it->second);
@@ -1145,10 +1245,11 @@ int ish_gpu_records_free(ish_ctx *ctx, int32_t set_id) {
 
 int ish_gpu_records_info(ish_ctx *ctx, int32_t set_id, uint32_t *n, uint64_t *total_bytes) {
   if (!ctx) return ISH_EINVAL;
-  auto it = ctx->sets.find(set_id);
-  if (it == ctx->sets.end()) return fail(ctx, ISH_EINVAL, "unknown record set %d", set_id);
-  if (n) *n = it->second.n;
-  if (total_bytes) *total_bytes = it->second.total;
+  int urc = ISH_OK;
+  RecordSet *it_set = use_set(ctx, set_id, &urc);
+  if (!it_set) return urc;
+  if (n) *n = it_set->n;
+  if (total_bytes) *total_bytes = it_set->total;
   return ISH_OK;
 }
 
@@ -1157,15 +1258,16 @@ int ish_gpu_score_set(ish_ctx *ctx, int32_t query_id, int32_t set_id, int32_t *s
   if (!ctx) return ISH_EINVAL;
   auto qi = ctx->queries.find(query_id);
   if (qi == ctx->queries.end()) return fail(ctx, ISH_EINVAL, "unknown query %d", query_id);
-  auto si = ctx->sets.find(set_id);
-  if (si == ctx->sets.end()) return fail(ctx, ISH_EINVAL, "unknown record set %d", set_id);
+  int urc = ISH_OK;
+  RecordSet *si_set = use_set(ctx, set_id, &urc);
+  if (!si_set) return urc;
   cudaSetDevice(ctx->device);
-  int rc = run_scoring(ctx, qi->second, si->second);
+  int rc = run_scoring(ctx, qi->second, *si_set);
   if (rc) {
     cudaStreamSynchronize(ctx->stream);
     return rc;
   }
-  return fetch_outputs(ctx, si->second.n, score, query_end, target_end, hit, hit_idx, n_hits);
+  return fetch_outputs(ctx, si_set->n, score, query_end, target_end, hit, hit_idx, n_hits);
 }
 
 int ish_gpu_score(ish_ctx *ctx, int32_t query_id, const uint8_t *records, const uint64_t *offsets, uint32_t n,
@@ -1175,6 +1277,7 @@ int ish_gpu_score(ish_ctx *ctx, int32_t query_id, const uint8_t *records, const 
   auto qi = ctx->queries.find(query_id);
   if (qi == ctx->queries.end()) return fail(ctx, ISH_EINVAL, "unknown query %d", query_id);
   cudaSetDevice(ctx->device);
+  if (int rc0 = finish_pending_load(ctx)) return rc0;
   RecordSet rs;
   int rc = load_records(ctx, records, offsets, n, rs, nullptr);
   if (!rc) rc = run_scoring(ctx, qi->second, rs);

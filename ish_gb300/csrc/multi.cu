@@ -38,6 +38,12 @@ struct MultiPlan {
   DevBuf counters, score, qend, tend, hit, block_counts, hit_idx, nhits;
   std::vector<uint32_t> exact_q;  // positions of the queries the exact kernels score
   ExactRes exact;
+  // long records: the queries at positions win_q score the plan's window view
+  // (results per window in wscore.., window k of query w at [w * view.nw + k])
+  // and are folded into their outputs after the batched kernels
+  WindowView view;
+  std::vector<uint32_t> win_q;
+  DevBuf wscore, wqend, wtend, whit;
   std::vector<cudaStream_t> side;
   std::vector<cudaEvent_t> events;
   cudaGraph_t graph = nullptr;
@@ -57,7 +63,10 @@ struct MultiPlan {
       c.params.release();
       c.tiles.release();
     }
-    DevBuf *bufs[] = {&counters, &score, &qend, &tend, &hit, &block_counts, &hit_idx, &nhits};
+    view.release();
+    win_q.clear();
+    DevBuf *bufs[] = {&counters, &score, &qend, &tend, &hit, &block_counts, &hit_idx, &nhits, &wscore, &wqend,
+                      &wtend, &whit};
     for (DevBuf *b : bufs) b->release();
     exact.release();
   }
@@ -140,6 +149,42 @@ int build_plan(ish_ctx *ctx, const int32_t *qids, uint32_t nq, int32_t set_id, R
     m.layout = m.L->layout;
     members.push_back(m);
   }
+  // ---- windows: when the set's longest records would bound the pass, the
+  // members whose window fold is exact (free target start; no free query
+  // start, whose windows past row 0 would need a second profile) score a
+  // window view with the largest overlap any of them needs ----
+  std::vector<char> windowed(nq, 0);
+  if (ctx->windows_on && ctx->kernel == ISH_KERNEL_AUTO && nonempty > 0 && nonempty <= (1u << 22)) {
+    uint64_t O = 0, W = 0;
+    for (const Member &m : members) {
+      const Query &q = ctx->queries.at(qids[m.pos]);
+      if (windowable_whole(q)) O = std::max(O, window_overlap(q));
+    }
+    if (O) {
+      for (const Member &m : members) {
+        const Query &q = ctx->queries.at(qids[m.pos]);
+        if (windowable_whole(q) && window_overlap(q)) W = std::max(W, window_stride(ctx, rs, O, m.G, m.K, m.mode));
+      }
+    }
+    if (W) {
+      int rc = build_window_view(ctx, rs, nonempty, W, O, P.view, ctx->stream);
+      if (rc) return rc;
+      for (const Member &m : members) {
+        const Query &q = ctx->queries.at(qids[m.pos]);
+        if (windowable_whole(q) && window_overlap(q)) {
+          windowed[m.pos] = 1;
+          P.win_q.push_back(m.pos);
+        }
+      }
+      const size_t nwq = (size_t)P.win_q.size() * P.view.nw;
+      CU(P.wscore.ensure(nwq * 4 + 4));
+      CU(P.wqend.ensure(nwq * 4 + 4));
+      CU(P.wtend.ensure(nwq * 4 + 4));
+      CU(P.whit.ensure(nwq + 16));
+    }
+  }
+  const RecordSet view = P.view.nw ? window_set(rs, P.view) : RecordSet{};
+
   std::map<long, size_t> cls_of;
   for (const Member &m : members) {
     const long key = ((long)m.K << 8) | (m.mode << 4) | m.layout;
@@ -184,8 +229,17 @@ int build_plan(ish_ctx *ctx, const int32_t *qids, uint32_t nq, int32_t set_id, R
                  (want & W_QEND) ? P.qend.as<int32_t>() + (size_t)pos * n : nullptr,
                  (want & W_TEND) ? P.tend.as<int32_t>() + (size_t)pos * n : nullptr,
                  (want & (W_HIT | W_COMPACT)) ? P.hit.as<uint8_t>() + (size_t)pos * n : nullptr};
-      wave_params(q, *m.L, rs, out, ctx->error.as<int>(), &params[j]);
-      tiles.push_back(BatchTile{(uint32_t)j, 0, nonempty, 0});
+      if (windowed[pos]) {
+        const size_t w = std::find(P.win_q.begin(), P.win_q.end(), pos) - P.win_q.begin();
+        const size_t at = w * P.view.nw;
+        OutDev wout{P.wscore.as<int32_t>() + at, P.wqend.as<int32_t>() + at, P.wtend.as<int32_t>() + at,
+                    P.whit.as<uint8_t>() + at};
+        wave_params(q, *m.L, view, wout, ctx->error.as<int>(), &params[j]);
+        tiles.push_back(BatchTile{(uint32_t)j, 0, P.view.nw, 0});
+      } else {
+        wave_params(q, *m.L, rs, out, ctx->error.as<int>(), &params[j]);
+        tiles.push_back(BatchTile{(uint32_t)j, 0, nonempty, 0});
+      }
     }
     // the longest queries first: blocks that start on them finish with the rest
     std::stable_sort(tiles.begin(), tiles.end(), [&](const BatchTile &x, const BatchTile &y) {
@@ -244,6 +298,19 @@ int enqueue_plan(ish_ctx *ctx, MultiPlan &P, RecordSet &rs, cudaStream_t s) {
       CU(cudaEventRecord(P.events[i], cs));
       CU(cudaStreamWaitEvent(s, P.events[i], 0));
     }
+  }
+  // windowed queries: fold their window results into their outputs
+  for (size_t w = 0; w < P.win_q.size(); ++w) {
+    const uint32_t i = P.win_q[w];
+    const Query &q = ctx->queries.at(P.qids[i]);
+    OutDev out{(P.want & W_SCORE) ? P.score.as<int32_t>() + (size_t)i * n : nullptr,
+               (P.want & W_QEND) ? P.qend.as<int32_t>() + (size_t)i * n : nullptr,
+               (P.want & W_TEND) ? P.tend.as<int32_t>() + (size_t)i * n : nullptr,
+               (P.want & (W_HIT | W_COMPACT)) ? P.hit.as<uint8_t>() + (size_t)i * n : nullptr};
+    const size_t at = w * P.view.nw;
+    int rc = merge_windows(ctx, rs, n - rs.n_empty, P.view, q, P.wscore.as<const int32_t>() + at,
+                           P.wqend.as<const int32_t>() + at, P.wtend.as<const int32_t>() + at, out, s, &P.kernels);
+    if (rc) return rc;
   }
   // queries the lane-exact kernels score
   for (uint32_t i : P.exact_q) {
@@ -335,11 +402,12 @@ int ish_gpu_score_multi(ish_ctx *ctx, const int32_t *query_ids, uint32_t n_queri
                         uint64_t *hit_offsets) {
   if (!ctx) return ISH_EINVAL;
   if (n_queries && !query_ids) return fail(ctx, ISH_EINVAL, "query_ids is NULL");
-  auto si = ctx->sets.find(set_id);
-  if (si == ctx->sets.end()) return fail(ctx, ISH_EINVAL, "unknown record set %d", set_id);
+  int urc = ISH_OK;
+  RecordSet *si_set = use_set(ctx, set_id, &urc);
+  if (!si_set) return urc;
   for (uint32_t i = 0; i < n_queries; ++i)
     if (!ctx->queries.count(query_ids[i])) return fail(ctx, ISH_EINVAL, "unknown query %d", query_ids[i]);
-  RecordSet &rs = si->second;
+  RecordSet &rs = *si_set;
   const uint32_t n = rs.n;
   if (n_queries == 0 || n == 0) {
     if (hit_offsets)
@@ -417,9 +485,10 @@ int ish_gpu_autotune(ish_ctx *ctx, int32_t set_id, const int32_t *query_ids, uin
                      int32_t *cols) {
   if (!ctx) return ISH_EINVAL;
   if (n_queries && !query_ids) return fail(ctx, ISH_EINVAL, "query_ids is NULL");
-  auto si = ctx->sets.find(set_id);
-  if (si == ctx->sets.end()) return fail(ctx, ISH_EINVAL, "unknown record set %d", set_id);
-  RecordSet &rs = si->second;
+  int urc = ISH_OK;
+  RecordSet *si_set = use_set(ctx, set_id, &urc);
+  if (!si_set) return urc;
+  RecordSet &rs = *si_set;
   cudaSetDevice(ctx->device);
   const uint32_t nonempty = rs.n - rs.n_empty;
   CU(ctx->out_score.ensure((size_t)rs.n * 4 + 4));

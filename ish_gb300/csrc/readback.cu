@@ -49,9 +49,10 @@ using namespace ish::host;
 int ish_gpu_records_get(ish_ctx *ctx, int32_t set_id, uint32_t first, uint32_t count, uint8_t *codes,
                         uint64_t codes_cap, uint64_t *offsets) {
   if (!ctx) return ISH_EINVAL;
-  auto it = ctx->sets.find(set_id);
-  if (it == ctx->sets.end()) return fail(ctx, ISH_EINVAL, "unknown record set %d", set_id);
-  RecordSet &rs = it->second;
+  int urc = ISH_OK;
+  RecordSet *it_set = use_set(ctx, set_id, &urc);
+  if (!it_set) return urc;
+  RecordSet &rs = *it_set;
   if ((uint64_t)first + count > rs.n)
     return fail(ctx, ISH_EINVAL, "records [%u, %llu) outside the set's %u", first,
                 (unsigned long long)first + count, rs.n);

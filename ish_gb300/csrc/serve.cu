@@ -42,6 +42,13 @@ struct Bundle {
   }
 };
 
+// A window view of the served set, shared by the requests that score it and
+// released with the last of them.
+struct SharedView {
+  WindowView V;
+  ~SharedView() { V.release(); }
+};
+
 struct Request {
   uint64_t ticket = 0;
   Query q;  // private copy: parameters and sequence (its layouts belong to the scheduler)
@@ -49,8 +56,13 @@ struct Request {
   WaveLayout *L = nullptr;
   bool exact = false;  // scored by the lane-exact kernels (outside the wavefront kernels' regime)
   Bundle *b = nullptr;
+  // long records: the request scores the windows of `view` into wout, folded
+  // into its outputs after its last chunk
+  std::shared_ptr<SharedView> view;
+  DevBuf wscore, wqend, wtend, whit;
   WaveParams params{};
   uint32_t next_chunk = 0;
+  uint32_t nch = 0;  // chunks (steps) of this request
   Clock::time_point t_submit, t_done;
   int status = ISH_OK;
   std::string err;
@@ -80,6 +92,7 @@ struct Server {
   uint32_t max_active_seen = 0;
   // scheduler thread only
   std::vector<Request *> active;
+  std::shared_ptr<SharedView> view;  // the newest window view (overlap view->V.O)
   cudaStream_t s = nullptr;
   std::vector<cudaStream_t> side;
   std::vector<cudaEvent_t> join;
@@ -150,6 +163,11 @@ void make_chunks(Server &S, uint32_t n) {
 void finish(Server &S, Request *r) {
   r->t_done = Clock::now();
   release_query(r->q);
+  r->view.reset();
+  r->wscore.release();
+  r->wqend.release();
+  r->wtend.release();
+  r->whit.release();
   r->L = nullptr;
   if (r->b) {
     S.pool.push_back(r->b);
@@ -231,9 +249,61 @@ int admit(Server &S, Request *r, char *msg, size_t) {
   if (r->L) {
     OutDev out{r->b->score.as<int32_t>(), r->b->qend.as<int32_t>(), r->b->tend.as<int32_t>(),
                r->b->hit.as<uint8_t>()};
-    wave_params(r->q, *r->L, rs, out, S.error.as<int>(), &r->params);
+    // long records that would bound the request's steps: it scores a window
+    // view (free target start, no free query start), shared with the other
+    // requests whose overlap it covers; a request that needs a larger overlap
+    // gets a new view (the old one lives on with the requests using it)
+    const uint64_t O = S.ctx->windows_on && S.ctx->kernel == ISH_KERNEL_AUTO && windowable_whole(r->q)
+                           ? window_overlap(r->q) : 0;
+    const uint32_t nonempty = rs.n - rs.n_empty;
+    const int mode = r->q.algo == ISH_ALGO_LOCAL ? SW : SG;
+    const uint64_t W = (O && nonempty <= (1u << 22)) ? window_stride(S.ctx, rs, O, r->G, r->K, mode) : 0;
+    if (W) {
+      if (!S.view || S.view->V.O < O) {
+        auto v = std::make_shared<SharedView>();
+        const uint64_t Ov = S.view ? std::max<uint64_t>(O, S.view->V.O) : O;
+        const uint64_t Wv = std::max<uint64_t>(W, 8 * Ov);
+        int rc = build_window_view(S.ctx, rs, nonempty, (Wv + 15) & ~15ull, Ov, v->V, S.s);
+        if (rc) {
+          snprintf(msg, 256, "window view: %s", ish_gpu_last_error(S.ctx));
+          return rc;
+        }
+        S.view = v;
+      }
+      r->view = S.view;
+      const uint32_t nw = r->view->V.nw;
+      cudaError_t e = r->wscore.ensure((size_t)nw * 4);
+      if (e == cudaSuccess) e = r->wqend.ensure((size_t)nw * 4);
+      if (e == cudaSuccess) e = r->wtend.ensure((size_t)nw * 4);
+      if (e == cudaSuccess) e = r->whit.ensure((size_t)nw + 16);
+      if (e != cudaSuccess) {
+        (void)cudaGetLastError();
+        snprintf(msg, 256, "device memory for a request's windows: %s", cudaGetErrorString(e));
+        return ISH_ENOMEM;
+      }
+      OutDev wout{r->wscore.as<int32_t>(), r->wqend.as<int32_t>(), r->wtend.as<int32_t>(), r->whit.as<uint8_t>()};
+      wave_params(r->q, *r->L, window_set(rs, r->view->V), wout, S.error.as<int>(), &r->params);
+    } else {
+      wave_params(r->q, *r->L, rs, out, S.error.as<int>(), &r->params);
+    }
   }
-  r->next_chunk = (r->L || r->exact) ? 0 : (uint32_t)S.chunks.size();
+  // steps per request: the exact kernels take the set's contiguous chunks; a
+  // wavefront request takes as many interleaved chunks as keep its steps near
+  // ISH_OPT_SERVE_STEP_CELLS cells (short queries finish in one or two steps
+  // instead of paying a host round trip per chunk), at most the server's
+  // chunk count
+  const double step_cells = S.ctx->serve_step_cells;  // default 1.25e11: ~25 ms at 5 TCUPS
+  if (r->exact) {
+    r->nch = (uint32_t)S.chunks.size();
+  } else if (r->L) {
+    const double cells = (double)r->q.Q * (double)rs.total;
+    r->nch = step_cells > 0 ? (uint32_t)std::min<double>((double)S.chunks.size(),
+                                                         std::max(1.0, std::round(cells / step_cells)))
+                            : (uint32_t)S.chunks.size();
+  } else {
+    r->nch = 0;
+  }
+  r->next_chunk = 0;
   return ISH_OK;
 }
 
@@ -251,7 +321,7 @@ int step(Server &S, char *msg) {
   std::vector<Cls> cls;
   std::vector<std::vector<Request *>> members;
   for (Request *r : S.active) {
-    if (r->next_chunk >= S.chunks.size() || r->exact) continue;
+    if (r->next_chunk >= r->nch || r->exact) continue;
     size_t c = 0;
     for (; c < cls.size(); ++c)
       if (cls[c].K == r->K && cls[c].mode == r->mode && cls[c].layout == r->layout) break;
@@ -273,9 +343,9 @@ int step(Server &S, char *msg) {
       // (longest pairs first), so its kernels end as evenly as a pass over
       // the whole set (contiguous chunks of the longest-first order made the
       // steps of the long records end on a few long pairs)
-      const uint32_t nch = (uint32_t)S.chunks.size();
-      const uint32_t nonempty = rs.n - rs.n_empty;
-      S.h_tiles[k] = BatchTile{k - cls[c].first, 0, nonempty, nch > 1 ? (nch << 16) | r->next_chunk : 0u};
+      const uint32_t nch = r->nch;
+      const uint32_t entries = r->view ? r->view->V.nw : rs.n - rs.n_empty;  // windows or records
+      S.h_tiles[k] = BatchTile{k - cls[c].first, 0, entries, nch > 1 ? (nch << 16) | r->next_chunk : 0u};
       ++k;
     }
     cls[c].count = k - cls[c].first;
@@ -334,7 +404,7 @@ int step(Server &S, char *msg) {
   }
   // ---- requests on the exact kernels: their chunk, after the batched launch ----
   for (Request *r : S.active) {
-    if (!r->exact || r->next_chunk >= S.chunks.size()) continue;
+    if (!r->exact || r->next_chunk >= r->nch) continue;
     const auto &ch = S.chunks[r->next_chunk];
     OutDev out{r->b->score.as<int32_t>(), r->b->qend.as<int32_t>(), r->b->tend.as<int32_t>(), r->b->hit.as<uint8_t>()};
     uint32_t nl = 0;
@@ -349,10 +419,18 @@ int step(Server &S, char *msg) {
   const RecordsDev rec{rs.codes.as<const uint8_t>(), rs.off_s.as<const uint64_t>(), rs.len_s.as<const uint32_t>(),
                        rs.orig_s.as<const uint32_t>(), rs.n};
   for (Request *r : S.active) {
-    if (r->next_chunk < S.chunks.size()) ++r->next_chunk;
-    if (r->next_chunk < S.chunks.size()) continue;
+    if (r->next_chunk < r->nch) ++r->next_chunk;
+    if (r->next_chunk < r->nch) continue;
     Bundle &b = *r->b;
     OutDev out{b.score.as<int32_t>(), b.qend.as<int32_t>(), b.tend.as<int32_t>(), b.hit.as<uint8_t>()};
+    if (r->view) {
+      int rc = merge_windows(S.ctx, rs, rs.n - rs.n_empty, r->view->V, r->q, r->wscore.as<const int32_t>(),
+                             r->wqend.as<const int32_t>(), r->wtend.as<const int32_t>(), out, s, nullptr);
+      if (rc) {
+        snprintf(msg, 256, "window fold: %s", ish_gpu_last_error(S.ctx));
+        return rc;
+      }
+    }
     const uint32_t n_empty = (r->q.Q == 0) ? n : rs.n_empty;
     if (n_empty) {
       k_trivial<<<std::max<uint32_t>(1, std::min<uint32_t>(ceil_div(n_empty, 256), 1024)), 256, 0, s>>>(
@@ -526,15 +604,16 @@ extern "C" {
 int ish_gpu_serve_start(ish_ctx *ctx, int32_t set_id, uint32_t max_active, uint64_t mem_budget, uint32_t chunks) {
   if (!ctx) return ISH_EINVAL;
   if (ctx->server) return fail(ctx, ISH_EINVAL, "the serving loop is already running");
-  auto si = ctx->sets.find(set_id);
-  if (si == ctx->sets.end()) return fail(ctx, ISH_EINVAL, "unknown record set %d", set_id);
+  int urc = ISH_OK;
+  RecordSet *si_set = use_set(ctx, set_id, &urc);
+  if (!si_set) return urc;
   if (max_active == 0 || max_active > 4096) return fail(ctx, ISH_EINVAL, "max_active must be in 1..4096");
   if (chunks == 0 || chunks > 1024) return fail(ctx, ISH_EINVAL, "chunks must be in 1..1024");
   cudaSetDevice(ctx->device);
   Server *S = new Server();
   S->ctx = ctx;
   S->set_id = set_id;
-  S->rs = &si->second;
+  S->rs = si_set;
   S->max_active = max_active;
   const uint32_t n = S->rs->n;
   const uint32_t nb = std::max<uint32_t>(1, ceil_div(n, HIT_TILE));

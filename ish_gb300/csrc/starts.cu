@@ -101,13 +101,14 @@ extern "C" int ish_gpu_match_starts(ish_ctx *ctx, int32_t query_id, int32_t set_
   if (!ctx) return ISH_EINVAL;
   auto qi = ctx->queries.find(query_id);
   if (qi == ctx->queries.end()) return fail(ctx, ISH_EINVAL, "unknown query %d", query_id);
-  auto si = ctx->sets.find(set_id);
-  if (si == ctx->sets.end()) return fail(ctx, ISH_EINVAL, "unknown record set %d", set_id);
+  int urc = ISH_OK;
+  RecordSet *si_set = use_set(ctx, set_id, &urc);
+  if (!si_set) return urc;
   if (n_hits == 0) return ISH_OK;
   if (!hit_idx || !target_end || !start) return fail(ctx, ISH_EINVAL, "hit_idx, target_end and start are required");
   cudaSetDevice(ctx->device);
   Query &q = qi->second;
-  RecordSet &rs = si->second;
+  RecordSet &rs = *si_set;
   const uint32_t n = rs.n;
   for (uint32_t i = 0; i < n_hits; ++i)
     if (hit_idx[i] >= n) return fail(ctx, ISH_EINVAL, "hit index %u >= %u records", hit_idx[i], n);

@@ -23,6 +23,7 @@ OPT_WAVE_LEAN = 9
 OPT_WINDOWS = 10
 OPT_STEP_BUDGET = 11
 OPT_FAULT_ALLOC = 12
+OPT_SERVE_STEP_CELLS = 13
 PROF_AUTO, PROF_S16, PROF_PAIR, PROF_S32 = -1, 0, 1, 2
 
 # Entry points declared in include/ish_gpu.h (checked by the tests).
@@ -34,6 +35,7 @@ EXPORTS = (
     "ish_gpu_poll", "ish_gpu_serve_stop", "ish_gpu_serve_stats", "ish_gpu_match_starts",
     "ish_gpu_launch_count", "ish_gpu_records_load_raw", "ish_gpu_records_load_lines", "ish_gpu_last_windows",
     "ish_gpu_calibrate_lanes", "ish_gpu_records_load_fastx", "ish_gpu_records_get", "ish_gpu_last_load_ms",
+    "ish_gpu_records_load_async",
 )
 
 
@@ -84,6 +86,7 @@ def load(build_if_missing: bool = False):
     L.ish_gpu_free_query.argtypes = [vp, C.c_int32]
     L.ish_gpu_score.argtypes = [vp, C.c_int32, u8p, u64p, C.c_uint32, i32p, i32p, i32p, u8p, u32p, u32p]
     L.ish_gpu_records_load.argtypes = [vp, u8p, u64p, C.c_uint32, i32p]
+    L.ish_gpu_records_load_async.argtypes = [vp, u8p, u64p, C.c_uint32, i32p]
     L.ish_gpu_records_free.argtypes = [vp, C.c_int32]
     L.ish_gpu_records_info.argtypes = [vp, C.c_int32, u32p, u64p]
     L.ish_gpu_score_set.argtypes = [vp, C.c_int32, C.c_int32, i32p, i32p, i32p, u8p, u32p, u32p]
@@ -232,6 +235,19 @@ class Context:
         sid = C.c_int32()
         self._check(self._L.ish_gpu_records_load(self._h, _p(records, C.c_uint8), _p(offsets, C.c_uint64),
                                                  len(offsets) - 1, C.byref(sid)))
+        return sid.value
+
+    def records_load_async(self, records: np.ndarray, offsets: np.ndarray) -> int:
+        """Resident set whose upload and packing run on the load stream while
+        the caller goes on (e.g. scores the previous set); the arrays are kept
+        referenced here until the next load, since the copy may still read
+        them."""
+        records = np.ascontiguousarray(records, np.uint8)
+        offsets = np.ascontiguousarray(offsets, np.uint64)
+        sid = C.c_int32()
+        self._check(self._L.ish_gpu_records_load_async(self._h, _p(records, C.c_uint8), _p(offsets, C.c_uint64),
+                                                       len(offsets) - 1, C.byref(sid)))
+        self._inflight = (records, offsets)
         return sid.value
 
     def records_load_raw(self, raw: np.ndarray, offsets: np.ndarray, matrix_kind: int) -> int:

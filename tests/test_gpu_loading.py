@@ -156,3 +156,62 @@ def test_freed_set_buffers_are_reused_exactly(ctx):
         ctx.records_free(b)
     finally:
         ctx.free_query(qid)
+
+
+def test_async_load_equals_sync_and_overlaps_scoring(ctx):
+    # records_load_async: the set's upload and packing run on the load stream;
+    # scoring another set meanwhile, then using the new set, gives exactly
+    # what a synchronous load gives; a pending set may also be freed unused,
+    # replaced by another load, or left for close
+    rng = np.random.default_rng(61)
+    m = ScoringMatrix(O.BLOSUM62)
+    q = rng.integers(0, 20, 150, dtype=np.uint8)
+    qid = ctx.set_query(q, O.BLOSUM62, m.values, native.ALGO_SEMI_GLOBAL, 10, 1,
+                        native.FREE_TARGET_START | native.FREE_TARGET_END, int(m.values[q, q].sum()), 0.5)
+    batches = []
+    for b in range(4):
+        recs = [rng.integers(0, 20, int(rng.integers(0, 900)), dtype=np.uint8) for _ in range(3000 + 500 * b)]
+        for r in recs[::50]:
+            if len(r) >= len(q) + 3:
+                r[3:3 + len(q)] = q
+        batches.append(native.pack_records(recs))
+    want = []
+    for buf, off in batches:
+        sid = ctx.records_load(buf, off)
+        want.append(ctx.score_set(qid, sid))
+        ctx.records_free(sid)
+    # pipelined: load b + 1 asynchronously, then score b
+    sid = ctx.records_load_async(*batches[0])
+    for b in range(4):
+        nxt = ctx.records_load_async(*batches[b + 1]) if b + 1 < 4 else None
+        got = ctx.score_set(qid, sid)
+        for k in ("score", "qend", "tend", "hit", "hit_idx"):
+            assert np.array_equal(got[k], want[b][k]), (b, k)
+        assert ctx.records_info(sid)[0] == len(batches[b][1]) - 1
+        ctx.records_free(sid)
+        sid = nxt
+    # a pending set freed without use, then one replaced by a synchronous load
+    sid = ctx.records_load_async(*batches[1])
+    ctx.records_free(sid)
+    sid = ctx.records_load_async(*batches[2])
+    sid2 = ctx.records_load(*batches[3])
+    for s, b in ((sid, 2), (sid2, 3)):
+        got = ctx.score_set(qid, s)
+        assert np.array_equal(got["score"], want[b]["score"]) and np.array_equal(got["hit_idx"], want[b]["hit_idx"])
+        ctx.records_free(s)
+    # the one-shot call after an asynchronous load
+    sid = ctx.records_load_async(*batches[0])
+    one = ctx.score(qid, *batches[1])
+    assert np.array_equal(one["score"], want[1]["score"])
+    assert np.array_equal(ctx.score_set(qid, sid)["score"], want[0]["score"])
+    ctx.records_free(sid)
+    ctx.free_query(qid)
+
+
+def test_async_load_pending_at_close():
+    # a context closed with its asynchronous load still in flight
+    rng = np.random.default_rng(62)
+    buf, off = native.pack_records([rng.integers(0, 20, 500, dtype=np.uint8) for _ in range(2000)])
+    c = native.Context(0)
+    c.records_load_async(buf, off)
+    c.close()

@@ -230,3 +230,51 @@ def test_multi_with_exact_kernel_queries(ctx):
         ctx.records_free(sid)
         for qid in ids + ex:
             ctx.free_query(qid)
+
+
+def test_multi_windows_long_records(ctx):
+    # a few 40-60 kb records among short ones: the batched launch scores the
+    # long ones as overlapping windows for the queries whose fold is exact
+    # (free target start, no free query start) and whole for the others; all
+    # results equal the launch without windows, the single-query path and the
+    # oracle, and the windowed launch runs one fold kernel per windowed query
+    rng = np.random.default_rng(23)
+    kind, alphabet = O.ACTGN, 5
+    TS, TE, QS = native.FREE_TARGET_START, native.FREE_TARGET_END, native.FREE_QUERY_START
+    specs = [(100, native.ALGO_SEMI_GLOBAL, TS | TE), (60, native.ALGO_LOCAL, 0),
+             (150, native.ALGO_SEMI_GLOBAL, TS | TE | QS), (80, native.ALGO_SEMI_GLOBAL, TS | TE),
+             (120, native.ALGO_LOCAL, 0)]
+    qs, ids = make_queries(ctx, kind, specs, rng, alphabet, 3, 1)
+    recs = records(rng, alphabet, 300, 1, 400, plants=[q for q, *_ in qs], plant_frac=0.1)
+    for L in (40_000, 52_000, 60_000):
+        r = rng.integers(0, alphabet, L, dtype=np.uint8)
+        for q, *_ in qs:  # copies of the queries deep in the record, so hits span windows
+            pos = int(rng.integers(0, L - len(q)))
+            r[pos:pos + len(q)] = q
+        recs.insert(int(rng.integers(0, len(recs))), r)
+    buf, off = native.pack_records(recs)
+    sid = ctx.records_load(buf, off)
+    try:
+        l0 = ctx.launch_count()
+        res = ctx.score_multi(ids, sid)
+        l1 = ctx.launch_count()
+        ctx.set_option(native.OPT_WINDOWS, 0)
+        whole = ctx.score_multi(ids, sid)
+        l2 = ctx.launch_count()
+        ctx.set_option(native.OPT_WINDOWS, 1)
+        assert (l1 - l0) - (l2 - l1) == 4, ((l1 - l0), (l2 - l1))  # four windowed queries: one fold each
+        for k in ("score", "qend", "tend", "hit"):
+            assert np.array_equal(res[k], whole[k]), k
+        for i in range(len(ids)):
+            assert np.array_equal(res["hit_idx"][i], whole["hit_idx"][i])
+        check_against_single(ctx, ids, sid, res)
+        check_against_oracle(kind, qs, buf, off, res, 3, 1)
+        # a replay of the captured plan gives the same
+        again = ctx.score_multi(ids, sid)
+        for k in ("score", "qend", "tend", "hit"):
+            assert np.array_equal(res[k], again[k]), k
+    finally:
+        ctx.set_option(native.OPT_WINDOWS, 1)
+        ctx.records_free(sid)
+        for qid in ids:
+            ctx.free_query(qid)

@@ -20,6 +20,9 @@ pytestmark = pytest.mark.gpu
 def ctx():
     native.load(build_if_missing=True)
     c = native.Context(0)
+    # every query takes the server's full chunk count: these sets are small,
+    # and the adaptive step size would score most queries in one step
+    c.set_option(native.OPT_SERVE_STEP_CELLS, 0)
     yield c
     c.close()
 
@@ -204,4 +207,80 @@ def test_serving_exact_kernel_requests(ctx):
     finally:
         ctx.records_free(sid)
         for qid in ids + ex:
+            ctx.free_query(qid)
+
+
+def test_serving_windows_long_records(ctx):
+    # a served set with a few 40-60 kb records: requests whose window fold is
+    # exact score a shared window view (a later request with a larger overlap
+    # gets a new one); every result equals the query alone (single-query
+    # scoring windows the set itself) and the unwindowed loop
+    rng = np.random.default_rng(57)
+    m = ScoringMatrix(BLOSUM62)
+    specs = [(80, native.ALGO_SEMI_GLOBAL, 12), (60, native.ALGO_LOCAL, 0), (120, native.ALGO_SEMI_GLOBAL, 13),
+             (200, native.ALGO_LOCAL, 0), (150, native.ALGO_SEMI_GLOBAL, 12)]
+    seqs, ids = [], []
+    for L, algo, ends in specs:
+        q = rng.integers(0, 20, L, dtype=np.uint8)
+        ids.append(ctx.set_query(q, BLOSUM62, m.values, algo, 10, 1, ends, int(m.values[q, q].sum()), 0.4))
+        seqs.append(q)
+    buf, off = protein_set(rng, 1500, seqs, plant=0.05)
+    recs = [buf[int(off[i]):int(off[i + 1])] for i in range(len(off) - 1)]
+    for L in (40_000, 52_000, 60_000):
+        r = rng.integers(0, 20, L, dtype=np.uint8)
+        for q in seqs:
+            pos = int(rng.integers(0, L - len(q)))
+            r[pos:pos + len(q)] = q
+        recs.insert(int(rng.integers(0, len(recs))), r)
+    buf, off = native.pack_records(recs)
+    sid = ctx.records_load(buf, off)
+    try:
+        expect = [alone(ctx, qid, sid) for qid in ids]
+        for windows in (1, 0):
+            ctx.set_option(native.OPT_WINDOWS, windows)
+            ctx.serve_start(sid, max_active=8, mem_budget=0, chunks=4)
+            try:
+                tickets = [ctx.submit(qid) for qid in ids]
+                for i, t in enumerate(tickets):
+                    same(wait(ctx, t), expect[i], f"query {i} (windows {windows})")
+                # again, one at a time (each admitted alone)
+                for i, qid in enumerate(ids):
+                    same(wait(ctx, ctx.submit(qid)), expect[i], f"query {i} alone (windows {windows})")
+            finally:
+                ctx.serve_stop()
+    finally:
+        ctx.set_option(native.OPT_WINDOWS, 1)
+        ctx.records_free(sid)
+        for qid in ids:
+            ctx.free_query(qid)
+
+
+def test_serving_adaptive_steps(ctx):
+    # the default step size: queries whose work is small (here at most 8e9
+    # cells) take one step instead of the server's 8 chunks; results are
+    # unchanged
+    rng = np.random.default_rng(71)
+    seqs, ids = make_queries(ctx, rng, [30, 120, 400, 900])
+    buf, off = protein_set(rng, 20000, seqs)
+    sid = ctx.records_load(buf, off)
+    try:
+        expect = [alone(ctx, qid, sid) for qid in ids]
+        for cells in (1.25e11, 0):  # 0: every query takes all 8 chunks
+            ctx.set_option(native.OPT_SERVE_STEP_CELLS, int(cells))
+            ctx.serve_start(sid, max_active=8, chunks=8)
+            try:
+                tickets = [ctx.submit(qid) for qid in ids]
+                for i, t in enumerate(tickets):
+                    same(wait(ctx, t), expect[i], f"query {i} (step cells {cells:g})")
+                steps = ctx.serve_stats()["steps"]
+            finally:
+                ctx.serve_stop()
+            if cells:
+                assert steps <= 4, steps  # one step per query at most (shared when they overlap)
+            else:
+                assert steps >= 8, steps
+    finally:
+        ctx.set_option(native.OPT_SERVE_STEP_CELLS, 0)
+        ctx.records_free(sid)
+        for qid in ids:
             ctx.free_query(qid)
