@@ -155,6 +155,14 @@ def barrier(dist):
         dist.barrier()
 
 
+def _oracle_passes():
+    """How the CPU oracle runs the striped passes on this host: NEON vectors at
+    the reference's lane counts (aarch64) or lane loops."""
+    import oracle as O
+
+    return "NEON vectors, 8 x int16 / 16 x uint8 / 8 x uint16" if O.vectors() else "lane loops"
+
+
 def cpu_sample(wl, seconds):
     """(records, offsets, cells per pass, seconds per step) of a sample sized to ~`seconds`."""
     import oracle as O
@@ -416,7 +424,7 @@ def run_reference(args):
         "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms, 3),
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "int16",
         "data": "synthetic", "config": workload_config(args.records),
-        "cpu_baseline": {"value": round(gcups, 4), "unit": "GCUPS", "cores": threads, "kind": "port",
+        "cpu_baseline": {"value": round(gcups, 4), "unit": "GCUPS", "cores": threads, "kind": "port", "passes": _oracle_passes(),
                          "sample": sample},
         "e2e": {"value": round(gcups, 4), "unit": "GCUPS", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }))
@@ -613,7 +621,7 @@ def run_ours(args):
             om.batch(sub.records, sub.offsets, threads=threads, forward=False, matches=True)
         dt = time.perf_counter() - t
         cpu = {"value": round(2 * len(q) * int(sub.offsets[-1]) / dt / 1e9, 4), "unit": "GCUPS", "cores": threads,
-               "kind": "port",
+               "kind": "port", "passes": _oracle_passes(),
                "sample": f"{len(idx)} of {n} records, semi-global + local, {dt:.1f} s on {threads} threads"}
         # the last timed step's own outputs against the oracle on the same
         # records (outside the timed region)
@@ -726,7 +734,7 @@ def _cpu_sample(wl, queries, gap_open, gap_ext, thr, seconds, max_queries=8):
     sub, dt = timed(idx)
     cells = sum(len(q) for q, *_ in qs) * int(sub.offsets[-1])
     _cpu_sample.last = (idx, qsel, threads)
-    return {"value": round(cells / dt / 1e9, 4), "unit": "GCUPS", "cores": threads, "kind": "port",
+    return {"value": round(cells / dt / 1e9, 4), "unit": "GCUPS", "cores": threads, "kind": "port", "passes": _oracle_passes(),
             "sample": f"{len(qs)} of {len(queries)} queries x {k} of {wl.n} records, {dt:.1f} s on {threads} threads"}
 
 

@@ -259,8 +259,8 @@ struct LoadTimer {
 inline uint32_t ceil_div(uint64_t a, uint64_t b) { return (uint32_t)((a + b - 1) / b); }
 
 int frame_rows(int ext);
-int wave_lean(const ish_ctx *ctx, int K, int mode);
-int batch_lean(const ish_ctx *ctx, int K, int mode);
+int wave_lean(const ish_ctx *ctx, int K, int mode, int G);
+int batch_lean(const ish_ctx *ctx, int K, int mode, int G);
 uint64_t window_overlap(const Query &q);
 int launch_windows(ish_ctx *ctx, Query &q, RecordSet &rs, uint32_t nonempty, OutDev out, cudaStream_t s, bool *done);
 uint64_t window_stride(const ish_ctx *ctx, const RecordSet &rs, uint64_t O, int G, int K, int mode);

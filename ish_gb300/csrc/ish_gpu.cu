@@ -137,26 +137,40 @@ int matrix_alphabet_ok(uint32_t alphabet) { return alphabet >= 1 && alphabet <= 
 // G = 8, Q = 8K - 2): lean is ahead for semi-global at K = 34..40 (+0.5 to
 // +5.7 %) and local at 34..38 (+1.3 to +2.4 %), behind from there on (up to
 // -15 %).
-int wave_lean(const ish_ctx *ctx, int K, int mode) {
+int wave_lean(const ish_ctx *ctx, int K, int mode, int G) {
   if (!wave_has_lean(K)) return 0;
   if (ctx->force_lean >= 0) return ctx->force_lean;
-  // Measured per K (protein, 200k records, G = 8, Q = 8K - 2, the rows-per-step
-  // kernel): the 128 x 3 build beats 256 x 2 from K = 27 (semi-global) / 30
-  // (local) on, by up to 16 %; from K = 34 the 128 x 3 default build beats the
-  // 128 x 2 lean one by 3-19 % up to K = 44, and loses at 46-48.
-  if (K <= 32) return mode == SW ? K >= 30 : K >= 27;
-  return K >= 46;
+  // Measured per K (protein records, Q = G * K - 2).  G <= 8 (200k records):
+  // the 128 x 3 build beats 256 x 2 from K = 27 (semi-global) / 30 (local)
+  // on, by up to 16 %; from K = 34 the 128 x 3 default build beats the 128 x
+  // 2 lean one by 3-19 % up to K = 44, and loses at 46-48.  Wider groups
+  // (300k records): at G = 32 the 256 x 2 build wins up to K = 30 (by 7-20 %)
+  // and ties at K = 32; at G = 16 the lean build wins from K = 44
+  // (semi-global, +7 %) / 40 (local, +15 %; 2.6x at K = 48).
+  if (G <= 8) {
+    if (K <= 32) return mode == SW ? K >= 30 : K >= 27;
+    return K >= 46;
+  }
+  if (K <= 32) return mode == SG && K == 32 && G >= 32;
+  return mode == SW ? K >= 40 : K >= 44;
 }
 
 // The same choice for the batched kernel (parameters in shared memory, one
-// more live pointer), measured the same way through ish_gpu_score_multi: the
-// 128 x 3 build wins everywhere but local alignment at K = 36 (+2.0 %) and
-// K = 48 (+6.7 %); the lean build loses 12-17 % from K = 38 on.
-int batch_lean(const ish_ctx *ctx, int K, int mode) {
+// more live pointer), measured the same way through ish_gpu_score_multi.
+// G <= 8: the 128 x 3 build wins everywhere but local alignment at K = 36
+// (+2.0 %) and K = 48 (+6.7 %); the lean build loses 12-17 % from K = 38 on.
+// Wider groups: at G = 32 the lean build wins semi-global K = 32 (+10 %),
+// the default one K = 26-30; at G = 16 the lean build wins from K = 44
+// (semi-global) / 36 (local, 2.9x at K = 48).  G is the class's narrowest.
+int batch_lean(const ish_ctx *ctx, int K, int mode, int G) {
   if (!wave_has_lean(K)) return 0;
   if (ctx->force_lean >= 0) return ctx->force_lean;
-  if (K <= 32) return 0;
-  return mode == SW && (K == 36 || K == 48);
+  if (G <= 8) {
+    if (K <= 32) return 0;
+    return mode == SW && (K == 36 || K == 48);
+  }
+  if (K <= 32) return mode == SG && K == 32 && G >= 32;
+  return mode == SW ? K >= 36 : K >= 44;
 }
 
 int frame_rows(int ext) {
@@ -707,7 +721,7 @@ int launch_wave_range(ish_ctx *ctx, Query &q, RecordSet &rs, uint32_t first, uin
   int rc = build_wave_layout(ctx, q, G, K, layout, &L);
   if (rc) return rc;
   const int mode = q.algo == ISH_ALGO_LOCAL ? SW : SG;
-  const int lean = wave_lean(ctx, K, mode);
+  const int lean = wave_lean(ctx, K, mode, G);
   WaveFn fn = wave_fn(K, mode, L->layout, lean);
   if (!fn) return fail(ctx, ISH_EOVERFLOW, "no wavefront kernel for K=%d", K);
   const int threads = wave_threads_lean(K, mode, lean);

@@ -205,7 +205,7 @@ int build_plan(ish_ctx *ctx, const int32_t *qids, uint32_t nq, int32_t set_id, R
 
   // ---- per class: kernel, occupancy, parameters, tiles ----
   for (MultiClass &c : P.classes) {
-    const int lean = batch_lean(ctx, c.K, c.mode);
+    const int lean = batch_lean(ctx, c.K, c.mode, c.Gmin);
     c.fn = batch_fn(c.K, c.mode, c.layout, lean);
     if (!c.fn) return fail(ctx, ISH_EOVERFLOW, "no batch kernel for K=%d", c.K);
     c.threads = wave_threads_lean(c.K, c.mode, lean);

@@ -366,7 +366,7 @@ int step(Server &S, char *msg) {
     }
     for (size_t c = 0; c < cls.size(); ++c) {
       const Cls &C = cls[c];
-      const int lean = batch_lean(S.ctx, C.K, C.mode);
+      const int lean = batch_lean(S.ctx, C.K, C.mode, C.Gmin);
       BatchFn fn = batch_fn(C.K, C.mode, C.layout, lean);
       if (!fn) {
         snprintf(msg, 256, "no batch kernel for K=%d", C.K);

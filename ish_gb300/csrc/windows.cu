@@ -112,7 +112,7 @@ uint64_t window_overlap(const Query &q) {
 // when windows would not help: the longest records must exceed twice the
 // rows a group scores on average (they would bound the pass) and one window.
 uint64_t window_stride(const ish_ctx *ctx, const RecordSet &rs, uint64_t O, int G, int K, int mode) {
-  const int lean = wave_lean(ctx, K, mode);
+  const int lean = wave_lean(ctx, K, mode, G);
   // groups in flight and the rows each would score on average (two records
   // per pair share their rows)
   const uint64_t groups =

@@ -13,6 +13,7 @@ from __future__ import annotations
 import ctypes as C
 import os
 import subprocess
+import sys
 
 import numpy as np
 
@@ -34,10 +35,27 @@ def ends_from_str(s: str) -> int:
 
 
 def build(force: bool = False) -> str:
-    src = os.path.join(HERE, "ish_oracle.c")
-    if force or not os.path.exists(LIB_PATH) or os.path.getmtime(LIB_PATH) < os.path.getmtime(src):
-        subprocess.check_call(["make", "-s", "-C", HERE, "libish_oracle.so"])
+    srcs = [os.path.join(HERE, f) for f in ("ish_oracle.c", "ish_oracle_neon.c", "ish_oracle.h")]
+    if force or not os.path.exists(LIB_PATH) or os.path.getmtime(LIB_PATH) < max(map(os.path.getmtime, srcs)):
+        # -B: rebuild even when make's timestamps say otherwise (force, or a
+        # copy of the tree with reset times)
+        r = subprocess.run(["make", "-s", "-B", "-C", HERE, "libish_oracle.so"], capture_output=True, text=True)
+        if r.returncode != 0:
+            # the NEON passes did not compile: the lane loops alone
+            sys.stderr.write("oracle: vector passes not built (%s); lane loops only\n" % r.stderr.strip()[-400:])
+            subprocess.check_call(["make", "-s", "-B", "-C", HERE, "libish_oracle.so", "EXTRA=-DISH_O_NO_NEON"])
     return LIB_PATH
+
+
+def set_vectors(on: bool) -> None:
+    """On an aarch64 host, run the striped passes on NEON vectors (default)
+    or on the lane loops (for comparing the two)."""
+    lib().ish_o_set_vectors(1 if on else 0)
+
+
+def vectors() -> bool:
+    """Whether the striped passes run on NEON vectors."""
+    return bool(lib().ish_o_vectors())
 
 
 class End(C.Structure):
@@ -75,6 +93,8 @@ def lib():
         L.ish_o_matrix_minmax.argtypes = [i8p, C.c_int, i8p, i8p]
         L.ish_o_sw_bias.argtypes = [i8p, C.c_int]
         L.ish_o_sw_bias.restype = C.c_uint8
+        L.ish_o_set_vectors.argtypes = [C.c_int]
+        L.ish_o_vectors.restype = C.c_int
         L.ish_o_sg_aln_i16.argtypes = [u8p, C.c_int, C.c_int, C.c_int, C.c_int, i16p, C.c_int, C.c_int8, C.c_int8, C.c_int]
         L.ish_o_sg_aln_i16.restype = End
         L.ish_o_sg_aln_i8.argtypes = [u8p, C.c_int, C.c_int, C.c_int, C.c_int, i8p, C.c_int, C.c_int8, C.c_int8, C.c_int]

@@ -329,8 +329,15 @@ void ish_o_sw_profile_u16(const uint8_t *q, int Q, const int8_t *M, int size, in
 O_DEFINE_SG(o_sg_i16, int16_t, -32768, 32767)
 O_DEFINE_SG(o_sg_i8, int8_t, -128, 127)
 
+static int o_use_vectors = 1;
+void ish_o_set_vectors(int on) { o_use_vectors = on; }
+int ish_o_vectors(void) { return o_use_vectors && ish_o_neon_available(); }
+
 ish_o_end ish_o_sg_aln_i16(const uint8_t *rec, int T, int Q, int open, int ext, const int16_t *prof,
                            int W, int8_t max_s, int8_t min_s, int ends) {
+#if defined(__aarch64__) && !defined(ISH_O_NO_NEON)
+    if (W == 8 && o_use_vectors) return ish_o_neon_sg_i16(rec, T, Q, open, ext, prof, max_s, min_s, ends);
+#endif
     switch (W) {
     case 8: return o_sg_i16_impl(rec, T, Q, open, ext, prof, 8, max_s, min_s, ends);
     case 16: return o_sg_i16_impl(rec, T, Q, open, ext, prof, 16, max_s, min_s, ends);
@@ -475,12 +482,18 @@ O_DEFINE_SW(o_sw_u16, uint16_t, 65535)
 
 ish_o_end ish_o_sw_u8(const uint8_t *rec, int T, int reverse, int Q, uint8_t open, uint8_t ext,
                       const uint8_t *prof, int W, uint8_t terminate, uint8_t bias) {
+#if defined(__aarch64__) && !defined(ISH_O_NO_NEON)
+    if (W == 16 && o_use_vectors) return ish_o_neon_sw_u8(rec, T, reverse, Q, open, ext, prof, terminate, bias);
+#endif
     if (W == 16) return o_sw_u8_impl(rec, T, reverse, Q, open, ext, prof, 16, terminate, bias);
     return o_sw_u8_impl(rec, T, reverse, Q, open, ext, prof, W, terminate, bias);
 }
 
 ish_o_end ish_o_sw_u16(const uint8_t *rec, int T, int reverse, int Q, uint16_t open, uint16_t ext,
                        const uint16_t *prof, int W, uint16_t terminate, uint16_t bias) {
+#if defined(__aarch64__) && !defined(ISH_O_NO_NEON)
+    if (W == 8 && o_use_vectors) return ish_o_neon_sw_u16(rec, T, reverse, Q, open, ext, prof, terminate, bias);
+#endif
     if (W == 8) return o_sw_u16_impl(rec, T, reverse, Q, open, ext, prof, 8, terminate, bias);
     return o_sw_u16_impl(rec, T, reverse, Q, open, ext, prof, W, terminate, bias);
 }

@@ -143,6 +143,22 @@ ish_o_end ish_o_sg_model(const uint8_t *rec, int T, const uint8_t *q, int Q, con
 ish_o_end ish_o_sw_model(const uint8_t *rec, int T, const uint8_t *q, int Q, const int8_t *M,
                          int size, int open, int ext, int W);
 
+/* ---- vector passes (ish_oracle_neon.c) ----
+ * On an aarch64 host the striped passes at the reference's own lane counts
+ * (semi-global int16 x 8, local uint8 x 16 and uint16 x 8) run on NEON
+ * vectors, as the reference runs them there; ish_o_set_vectors(0) selects the
+ * lane loops instead (for comparing the two).  ish_o_vectors() reports
+ * whether the vector passes are in use. */
+ish_o_end ish_o_neon_sg_i16(const uint8_t *rec, int T, int Q, int open, int ext, const int16_t *prof,
+                            int8_t max_s, int8_t min_s, int ends);
+ish_o_end ish_o_neon_sw_u8(const uint8_t *rec, int T, int reverse, int Q, uint8_t open, uint8_t ext,
+                           const uint8_t *prof, uint8_t terminate, uint8_t bias);
+ish_o_end ish_o_neon_sw_u16(const uint8_t *rec, int T, int reverse, int Q, uint16_t open, uint16_t ext,
+                            const uint16_t *prof, uint16_t terminate, uint16_t bias);
+int ish_o_neon_available(void);
+void ish_o_set_vectors(int on);
+int ish_o_vectors(void);
+
 #ifdef __cplusplus
 }
 #endif
