@@ -303,6 +303,51 @@ def test_matchers_on_reference_searcher_fixtures(ctx):
             ctx.free_query(mt.query_id)
 
 
+def test_reference_searcher_fixtures_from_text_split_on_the_device(ctx):
+    """tests/test_searcher.mojo:77-200 end to end on the device: the fixture
+    file's text split into line or FASTA records by the library
+    (ish_gpu_records_load_lines / _fastx), scored, and the matched records
+    written back from the device's copy (ish_gpu_records_get, names from the
+    splitter's bounds) through the runners' output writer."""
+    import sys
+    sys.path.insert(0, os.path.dirname(os.path.abspath(__file__)))
+    from searcher_fixtures import cases
+
+    from ish_gb300 import output
+
+    for case in cases():
+        text = case["in_data"].encode()
+        for algo, ends in (("local", None), ("sg", "TTTT"), ("sg", "FFTT")):
+            if algo == "sg":
+                mt = StripedSemiGlobalMatcher(case["pattern"].encode(), 0.8, ends, case["matrix"], context=ctx)
+            else:
+                mt = StripedLocalMatcher(case["pattern"].encode(), 0.8, case["matrix"], context=ctx)
+            if case["record_type"] == "line":
+                sid, n = ctx.records_load_lines(text, mt.matrix.kind)
+                bounds = None
+            else:
+                sid, n, bounds = ctx.records_load_fastx(text, mt.matrix.kind)
+            try:
+                hits = ctx.score_set(mt.query_id, sid)["hit_idx"]
+                codes, off = ctx.records_get(sid)
+            finally:
+                ctx.records_free(sid)
+            matches = [(int(i), 0, 0) for i in hits]
+            parts = []
+            if case["record_type"] == "line":
+                output.write_line_matches(parts.append, codes, off, matches, mt.matrix.code_to_ascii)
+            else:
+                names = [text[int(b[0]):int(b[1])] for b in bounds]
+                output.write_fastx_matches(parts.append, names, codes, off, matches, mt.matrix.code_to_ascii)
+            got = b"".join(parts).decode("utf-8", errors="surrogateescape")
+            exp = case["expected"]
+            if case["record_type"] == "fastx":
+                assert got.upper() == exp.upper(), (case["line"], algo, ends)
+            else:
+                assert got == exp, (case["line"], algo, ends)
+            ctx.free_query(mt.query_id)
+
+
 @pytest.mark.parametrize("layout", [native.PROF_S16, native.PROF_PAIR, native.PROF_S32])
 @pytest.mark.parametrize("kind", [O.ACTGN, O.BLOSUM62])
 def test_every_profile_layout(ctx, layout, kind):
