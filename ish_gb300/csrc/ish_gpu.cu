@@ -437,9 +437,8 @@ int pack_set(ish_ctx *ctx, uint32_t n, uint64_t raw_bytes, const uint64_t *end, 
   uint32_t *max_code = ctx->max_code.as<uint32_t>();
   CU(cudaMemsetAsync(ctx->max_code.p, 0, 8, s));
   CU(cudaMemsetAsync(counts, 0, (size_t)NBUCKETS * 4, s));
-  const uint32_t nb = std::min<uint32_t>(ceil_div(n, 256), (uint32_t)ctx->num_sms * 16);
   CU(cudaEventRecord(ctx->load_ev[1], s));
-  k_lengths<<<nb, 256, 0, s>>>(ctx->off_in.as<uint64_t>(), end, n, ctx->len_tmp.as<uint32_t>(),
+  k_lengths<<<std::min<uint32_t>(ceil_div(n, 1024), (uint32_t)ctx->num_sms * 2), 1024, 0, s>>>(ctx->off_in.as<uint64_t>(), end, n, ctx->len_tmp.as<uint32_t>(),
                                 ctx->slot_tmp.as<uint64_t>(), counts, max_code + 1);
   ++ctx->launches;
   // exclusive scan of slot sizes -> packed offsets
@@ -466,7 +465,7 @@ int pack_set(ish_ctx *ctx, uint32_t n, uint64_t raw_bytes, const uint64_t *end, 
   CU(rs.len_s.ensure((size_t)n * 4));
   CU(rs.off_s.ensure((size_t)n * 8));
   CU(rs.orig_s.ensure((size_t)n * 4));
-  k_scatter<<<nb, 256, 0, s>>>(ctx->len_tmp.as<uint32_t>(), ctx->poff_tmp.as<uint64_t>(), n, cursor,
+  k_scatter<<<ceil_div(n, 1024), 1024, 0, s>>>(ctx->len_tmp.as<uint32_t>(), ctx->poff_tmp.as<uint64_t>(), n, cursor,
                                rs.len_s.as<uint32_t>(), rs.off_s.as<uint64_t>(), rs.orig_s.as<uint32_t>());
   ++ctx->launches;
   {
@@ -479,9 +478,13 @@ int pack_set(ish_ctx *ctx, uint32_t n, uint64_t raw_bytes, const uint64_t *end, 
     }
     CU(e);
   }
-  const uint32_t pb = std::min<uint32_t>(ceil_div((uint64_t)n * 32, 256), (uint32_t)ctx->num_sms * 32);
+  // lanes per record: the power of two nearest above the average 16-byte
+  // chunks per record, 4 to 32
+  uint32_t gw = 4;
+  while (gw < 32 && (uint64_t)gw * 16 * n < rs.total) gw <<= 1;
+  const uint32_t pb = std::min<uint32_t>(ceil_div((uint64_t)n * gw, 256), (uint32_t)ctx->num_sms * 8);
   k_pack<<<pb, 256, 0, s>>>(ctx->raw.as<uint8_t>(), raw_bytes, ctx->off_in.as<uint64_t>(), end,
-                            ctx->poff_tmp.as<uint64_t>(), n, enc, rs.codes.as<uint8_t>(), max_code);
+                            ctx->poff_tmp.as<uint64_t>(), n, enc, rs.codes.as<uint8_t>(), max_code, gw);
   ++ctx->launches;
   CU(cudaGetLastError());
   CU(cudaEventRecord(ctx->load_ev[2], s));

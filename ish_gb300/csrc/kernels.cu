@@ -27,19 +27,31 @@ __device__ __forceinline__ uint64_t rec_len(const uint64_t *off, const uint64_t 
   return (end ? end[i] : off[i + 1]) - off[i];
 }
 
-__global__ void k_lengths(const uint64_t *off, const uint64_t *end, uint32_t n, uint32_t *len, uint64_t *slot_bytes,
-                          uint32_t *hist, uint32_t *max_bucket) {
+// Lengths, 16-byte slot sizes and the length histogram.  The buckets below
+// SMEM_BUCKETS are counted in shared memory and flushed once per block (a
+// set's lengths crowd into a few hundred buckets, and one global atomic per
+// record on those few addresses would serialise); longer records go to the
+// global histogram directly.  Launched with 1024 threads.
+__global__ void __launch_bounds__(1024) k_lengths(const uint64_t *off, const uint64_t *end, uint32_t n, uint32_t *len,
+                                                  uint64_t *slot_bytes, uint32_t *hist, uint32_t *max_bucket) {
+  __shared__ uint32_t sh[SMEM_BUCKETS];
+  for (uint32_t k = threadIdx.x; k < SMEM_BUCKETS; k += blockDim.x) sh[k] = 0;
+  __syncthreads();
   uint32_t mb = 0;
   for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
     const uint64_t l = rec_len(off, end, i);
     len[i] = (uint32_t)l;
     slot_bytes[i] = (l + 15) & ~(uint64_t)15;
     const uint32_t b = len_bucket(l);
-    atomicAdd(&hist[b], 1u);
+    if (b < SMEM_BUCKETS) atomicAdd(&sh[b], 1u);
+    else atomicAdd(&hist[b], 1u);
     mb = max(mb, b);
   }
   for (int o = 16; o > 0; o >>= 1) mb = max(mb, __shfl_xor_sync(0xffffffffu, mb, o));
   if ((threadIdx.x & 31) == 0 && mb) atomicMax(max_bucket, mb);
+  __syncthreads();
+  for (uint32_t k = threadIdx.x; k < SMEM_BUCKETS; k += blockDim.x)
+    if (sh[k]) atomicAdd(&hist[k], sh[k]);
 }
 
 // Exclusive scan of the bucket histogram in DESCENDING bucket order, in two
@@ -105,41 +117,67 @@ __global__ void __launch_bounds__(1024) k_bucket_cursors(const uint32_t *hist, c
   cursor[bucket] = base + before_warp + incl - c;
 }
 
-__global__ void k_scatter(const uint32_t *len, const uint64_t *poff, uint32_t n, uint32_t *cursor,
-                          uint32_t *len_s, uint64_t *off_s, uint32_t *orig_s) {
-  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-    const uint32_t l = len[i];
-    const uint32_t pos = atomicAdd(&cursor[len_bucket(l)], 1u);
+// Sorted position of every record: record i goes to the next free place of
+// its bucket.  Each block takes 1024 records (one per thread, 1024 threads),
+// ranks them within their bucket in shared memory, reserves one range per
+// used bucket from the global cursor and writes; buckets from SMEM_BUCKETS on
+// (long records, few) take one global atomic per record.  The order within a
+// bucket is unspecified: the two lanes of a pair are scored independently.
+__global__ void __launch_bounds__(1024) k_scatter(const uint32_t *len, const uint64_t *poff, uint32_t n,
+                                                  uint32_t *cursor, uint32_t *len_s, uint64_t *off_s,
+                                                  uint32_t *orig_s) {
+  __shared__ uint32_t sh[SMEM_BUCKETS];  // counts, then the block's first position per bucket
+  for (uint32_t k = threadIdx.x; k < SMEM_BUCKETS; k += blockDim.x) sh[k] = 0;
+  __syncthreads();
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  uint32_t l = 0, b = 0, rank = 0;
+  if (i < n) {
+    l = len[i];
+    b = len_bucket(l);
+    if (b < SMEM_BUCKETS) rank = atomicAdd(&sh[b], 1u);
+  }
+  __syncthreads();
+  for (uint32_t k = threadIdx.x; k < SMEM_BUCKETS; k += blockDim.x) {
+    const uint32_t c = sh[k];
+    if (c) sh[k] = atomicAdd(&cursor[k], c);
+  }
+  __syncthreads();
+  if (i < n) {
+    const uint32_t pos = b < SMEM_BUCKETS ? sh[b] + rank : atomicAdd(&cursor[b], 1u);
     len_s[pos] = l;
     off_s[pos] = poff[i];
     orig_s[pos] = i;
   }
 }
 
-// One warp per record: the record is copied to dst[poff[i] ..) in 16-byte
-// chunks realigned with funnel shifts, optionally encoded through a 256-entry
+// A group of `gw` lanes per record (a power of two up to 32, chosen by the
+// host near the set's average 16-byte chunks per record, so that short lines
+// do not leave most of a warp idle): the record is copied to dst[poff[i] ..)
+// in 16-byte chunks realigned with funnel shifts, optionally encoded through a 256-entry
 // byte table (ish's convert_ascii_to_encoding, done per byte on the host by
 // the runners, ishlib/parallel_line_search_runner.mojo:90-94); the tail of the
 // 16-byte slot is zero-filled, and the largest code of the set is reduced into
 // *max_code, so a query's alphabet can be checked once per set.
 __global__ void k_pack(const uint8_t *src, uint64_t src_bytes, const uint64_t *off, const uint64_t *end,
-                       const uint64_t *poff, uint32_t n, const uint8_t *enc, uint8_t *dst, uint32_t *max_code) {
+                       const uint64_t *poff, uint32_t n, const uint8_t *enc, uint8_t *dst, uint32_t *max_code,
+                       uint32_t gw) {
   __shared__ uint8_t table[256];
   if (enc) {
     for (int i = threadIdx.x; i < 256; i += blockDim.x) table[i] = enc[i];
     __syncthreads();
   }
-  const uint32_t warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const uint32_t group = (blockIdx.x * blockDim.x + threadIdx.x) / gw;
   const uint32_t lane = threadIdx.x & 31;
-  const uint32_t nwarps = (gridDim.x * blockDim.x) >> 5;
+  const uint32_t glane = threadIdx.x & (gw - 1);
+  const uint32_t ngroups = (gridDim.x * blockDim.x) / gw;
   const uint32_t *src32 = reinterpret_cast<const uint32_t *>(src);
   const uint64_t nwords = (src_bytes + 3) >> 2;
   uint32_t mx = 0;
-  for (uint32_t r = warp; r < n; r += nwarps) {
+  for (uint32_t r = group; r < n; r += ngroups) {
     const uint64_t s0 = off[r], len = rec_len(off, end, r);
     uint4 *d = reinterpret_cast<uint4 *>(dst + poff[r]);
     const uint64_t nchunks = (len + 15) >> 4;
-    for (uint64_t c = lane; c < nchunks; c += 32) {
+    for (uint64_t c = glane; c < nchunks; c += gw) {
       const uint64_t b = s0 + c * 16;  // first source byte of the chunk
       const uint64_t w0 = b >> 2;
       const uint32_t sh = (uint32_t)(b & 3) * 8;
@@ -479,20 +517,30 @@ PlainFn plain_fn(int mode, int qmax) {
 // Hit compaction.  blockIdx.y selects one of several query-major flag arrays
 // of n entries (batched launches); counts and offsets are laid out [y][x], so
 // one exclusive scan over them concatenates the per-query hit lists.
-__global__ void k_count_hits(const uint8_t *hit, uint32_t n, uint32_t *block_counts) {
+// Hit compaction in tiles of HIT_TILE records per 1024-thread block: warp w
+// of a block covers HIT_TILE / 32 consecutive records of the tile, 32 per
+// ballot, so neither pass needs a block-wide barrier inside its loop.
+// blockIdx.y selects one of several hit arrays of n records laid end to end.
+constexpr uint32_t HIT_WARP = HIT_TILE / 32;
+
+__global__ void __launch_bounds__(1024) k_count_hits(const uint8_t *hit, uint32_t n, uint32_t *block_counts) {
   __shared__ uint32_t wsum[32];
   hit += (size_t)blockIdx.y * n;
   block_counts += (size_t)blockIdx.y * gridDim.x;
-  const uint32_t base = blockIdx.x * HIT_TILE;
+  const uint32_t lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  const uint64_t w0 = (uint64_t)blockIdx.x * HIT_TILE + wid * HIT_WARP;
   uint32_t c = 0;
-  for (uint32_t i = base + threadIdx.x; i < min(n, base + HIT_TILE); i += blockDim.x) c += hit[i] != 0;
-  for (int o = 16; o > 0; o >>= 1) c += __shfl_down_sync(0xffffffffu, c, o);
-  if ((threadIdx.x & 31) == 0) wsum[threadIdx.x >> 5] = c;
+#pragma unroll
+  for (uint32_t k = 0; k < HIT_WARP; k += 32) {
+    const uint64_t i = w0 + k + lane;
+    c += __popc(__ballot_sync(0xffffffffu, i < n && hit[i]));
+  }
+  if (lane == 0) wsum[wid] = c;
   __syncthreads();
-  if (threadIdx.x < 32) {
-    uint32_t v = threadIdx.x < (blockDim.x >> 5) ? wsum[threadIdx.x] : 0;
-    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
-    if (threadIdx.x == 0) block_counts[blockIdx.x] = v;
+  if (wid == 0) {
+    uint32_t v = wsum[lane];
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    if (lane == 0) block_counts[blockIdx.x] = v;
   }
 }
 
@@ -519,30 +567,36 @@ __global__ void k_scan_counts(uint32_t *counts, uint32_t nb, uint32_t *total) {
   if (threadIdx.x == 0) *total = carry;
 }
 
-__global__ void k_write_hits(const uint8_t *hit, uint32_t n, const uint32_t *block_offsets, uint32_t *idx) {
+__global__ void __launch_bounds__(1024) k_write_hits(const uint8_t *hit, uint32_t n, const uint32_t *block_offsets,
+                                                     uint32_t *idx) {
   __shared__ uint32_t wsum[32];
-  __shared__ uint32_t run;
   hit += (size_t)blockIdx.y * n;
   block_offsets += (size_t)blockIdx.y * gridDim.x;
-  const uint32_t base = blockIdx.x * HIT_TILE;
-  if (threadIdx.x == 0) run = block_offsets[blockIdx.x];
+  const uint32_t lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  const uint64_t w0 = (uint64_t)blockIdx.x * HIT_TILE + wid * HIT_WARP;
+  uint32_t c = 0;
+#pragma unroll
+  for (uint32_t k = 0; k < HIT_WARP; k += 32) {
+    const uint64_t i = w0 + k + lane;
+    c += __popc(__ballot_sync(0xffffffffu, i < n && hit[i]));
+  }
+  if (lane == 0) wsum[wid] = c;
   __syncthreads();
-  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
-  for (uint32_t b = base; b < min(n, base + HIT_TILE); b += blockDim.x) {
-    const uint32_t i = b + threadIdx.x;
-    const bool h = i < n && i < base + HIT_TILE && hit[i];
+  // hits of the tile's earlier warps (exclusive scan over the 32 warp counts)
+  uint32_t x = wsum[lane];
+  for (int o = 1; o < 32; o <<= 1) {
+    const uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
+    if (lane >= (uint32_t)o) x += y;
+  }
+  uint32_t run = block_offsets[blockIdx.x] + __shfl_sync(0xffffffffu, x, wid) - c;
+  if (!c) return;
+  const uint32_t below = (1u << lane) - 1u;
+  for (uint32_t k = 0; k < HIT_WARP; k += 32) {
+    const uint64_t i = w0 + k + lane;
+    const bool h = i < n && hit[i];
     const uint32_t m = __ballot_sync(0xffffffffu, h);
-    if (lane == 0) wsum[wid] = __popc(m);
-    __syncthreads();
-    uint32_t before = 0, total = 0;
-    for (int w = 0; w < nw; ++w) {
-      if (w < wid) before += wsum[w];
-      total += wsum[w];
-    }
-    if (h) idx[run + before + __popc(m & ((1u << lane) - 1u))] = i;
-    __syncthreads();
-    if (threadIdx.x == 0) run += total;
-    __syncthreads();
+    if (h) idx[run + __popc(m & below)] = (uint32_t)i;
+    run += __popc(m);
   }
 }
 

@@ -9,6 +9,7 @@ namespace ish {
 constexpr uint32_t NBUCKETS = 65536;     // length buckets of the record sort
 constexpr uint32_t SCAN_TILE = 4096;     // values per block of k_scan64_block (1024 threads)
 constexpr uint32_t HIT_TILE = 8192;      // records per block of the hit compaction
+constexpr uint32_t SMEM_BUCKETS = 4096;  // length buckets counted in shared memory by k_lengths / k_scatter
 
 constexpr uint32_t LINE_TILE = 65536;    // text bytes per block of the line splitter
 __global__ void k_lengths(const uint64_t *off, const uint64_t *end, uint32_t n, uint32_t *len, uint64_t *slot_bytes,
@@ -20,7 +21,8 @@ __global__ void k_bucket_cursors(const uint32_t *hist, const uint32_t *max_bucke
 __global__ void k_scatter(const uint32_t *len, const uint64_t *poff, uint32_t n, uint32_t *cursor, uint32_t *len_s,
                           uint64_t *off_s, uint32_t *orig_s);
 __global__ void k_pack(const uint8_t *src, uint64_t src_bytes, const uint64_t *off, const uint64_t *end,
-                       const uint64_t *poff, uint32_t n, const uint8_t *enc, uint8_t *dst, uint32_t *max_code);
+                       const uint64_t *poff, uint32_t n, const uint8_t *enc, uint8_t *dst, uint32_t *max_code,
+                       uint32_t gw);
 __global__ void k_count_newlines(const uint8_t *text, uint64_t bytes, uint32_t *block_counts);
 __global__ void k_write_newlines(const uint8_t *text, uint64_t bytes, const uint32_t *block_offsets, uint64_t *pos);
 __global__ void k_line_bounds(const uint8_t *text, uint64_t bytes, const uint64_t *nl, uint32_t n_nl, uint32_t n_lines,
