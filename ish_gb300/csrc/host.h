@@ -189,6 +189,13 @@ struct ish_ctx {
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
   cudaEvent_t load_ev[3] = {nullptr, nullptr, nullptr};  // last load: start, packing start, end
   double last_load_ms[3] = {0, 0, 0};                    // upload (+ splitting), packing, host wall
+  // a load's records' bytes travel on copy_stream, after its offsets
+  // (off_ev), while the packing kernels that need only the offsets run;
+  // raw_ev marks the end of that upload
+  cudaStream_t copy_stream = nullptr;
+  cudaEvent_t raw_ev = nullptr;
+  cudaEvent_t off_ev = nullptr;  // the offsets are on the device
+  bool raw_overlapped = false;  // the last load used copy_stream
   std::string err;
   int kernel = ISH_KERNEL_AUTO;
   int sg_lanes = 8, sw_u8_lanes = 16, sw_u16_lanes = 8;
@@ -206,7 +213,8 @@ struct ish_ctx {
   std::vector<ish::host::RecordSet> spare_sets;
   int32_t next_set = 1;
   // scratch
-  ish::host::DevBuf raw, off_in, len_tmp, slot_tmp, poff_tmp, hist, scan_tmp, max_code;
+  ish::host::DevBuf raw, off_in, len_tmp, poff_tmp, hist, scan_tmp, summary;
+  bool pack_dirty = true;  // the packing accumulators need clearing before the next load
   ish::host::DevBuf counter, error, out_score, out_qend, out_tend, out_hit, hit_idx, block_counts, nhits;
   ish::host::DevBuf plain_scratch;
   ish::host::DevBuf enc_tables, nl_pos, line_end;  // encoding tables; line splitting scratch
@@ -293,7 +301,11 @@ int load_records(ish_ctx *ctx, const uint8_t *records, const uint64_t *offsets, 
 // stream).  defer: the host-side summary of the set (histogram, largest code)
 // is read back when the set is first used (finish_pending_load), not now.
 int pack_set(ish_ctx *ctx, uint32_t n, uint64_t raw_bytes, const uint64_t *end, const uint8_t *enc, RecordSet &rs,
-             cudaStream_t s = nullptr, bool defer = false);
+             cudaStream_t s = nullptr, bool defer = false, bool raw_pending = false);
+// Device phases of the last load (ish_gpu_last_load_ms).
+void load_phase_times(ish_ctx *ctx);
+// A set's host-side summary from {largest code, largest bucket, counts}.
+void set_summary(RecordSet &rs, const uint32_t *h);
 // Completes an asynchronous load in flight (ish_gpu_records_load_async), if any.
 int finish_pending_load(ish_ctx *ctx);
 // The set, with its asynchronous load completed; nullptr (and the error) if

@@ -422,43 +422,46 @@ int device_encoding(ish_ctx *ctx, int kind, const uint8_t **out) {
 // raw[off_in[i] .. end[i]) with `end` on the device, or raw[off_in[i] ..
 // off_in[i + 1]) without; `enc` (device, may be null) encodes bytes on the way
 // (see k_lengths .. k_pack in kernels.cu).  rs.total must hold the residue count.
+// Device phases of the last load for ish_gpu_last_load_ms: upload (with the
+// splitting of a text load) and packing.  When the records' bytes travelled on
+// the copy stream, the packing kernels that need only the offsets ran during
+// the upload, and packing counts from the end of the upload.
+void load_phase_times(ish_ctx *ctx) {
+  float a = 0.f, b = 0.f;
+  cudaEvent_t mid = ctx->raw_overlapped ? ctx->raw_ev : ctx->load_ev[1];
+  if (cudaEventElapsedTime(&a, ctx->load_ev[0], mid) == cudaSuccess) ctx->last_load_ms[0] = a;
+  if (cudaEventElapsedTime(&b, mid, ctx->load_ev[2]) == cudaSuccess) ctx->last_load_ms[1] = b;
+  (void)cudaGetLastError();
+}
+
 int pack_set(ish_ctx *ctx, uint32_t n, uint64_t raw_bytes, const uint64_t *end, const uint8_t *enc, RecordSet &rs,
-             cudaStream_t s, bool defer) {
+             cudaStream_t s, bool defer, bool raw_pending) {
   if (!s) s = ctx->stream;
   rs.n = n;
-  CU(ctx->len_tmp.ensure((size_t)n * 4));
-  CU(ctx->slot_tmp.ensure((size_t)n * 8));
-  CU(ctx->poff_tmp.ensure((size_t)n * 8));
-  // counts [NBUCKETS], descending cursors [NBUCKETS], per-block sums
-  CU(ctx->hist.ensure((size_t)NBUCKETS * 4 * 2 + BUCKET_BLOCKS * 4));
-  uint32_t *counts = ctx->hist.as<uint32_t>(), *cursor = counts + NBUCKETS, *bsums = cursor + NBUCKETS;
-  // max_code[0]: largest record code, [1]: largest length bucket
-  CU(ctx->max_code.ensure(16));
-  uint32_t *max_code = ctx->max_code.as<uint32_t>();
-  CU(cudaMemsetAsync(ctx->max_code.p, 0, 8, s));
-  CU(cudaMemsetAsync(counts, 0, (size_t)NBUCKETS * 4, s));
-  CU(cudaEventRecord(ctx->load_ev[1], s));
-  k_lengths<<<std::min<uint32_t>(ceil_div(n, 1024), (uint32_t)ctx->num_sms * 2), 1024, 0, s>>>(ctx->off_in.as<uint64_t>(), end, n, ctx->len_tmp.as<uint32_t>(),
-                                ctx->slot_tmp.as<uint64_t>(), counts, max_code + 1);
-  ++ctx->launches;
-  // exclusive scan of slot sizes -> packed offsets
   const uint32_t tiles = ceil_div(n, SCAN_TILE);
   if (tiles > SCAN_TILE) return fail(ctx, ISH_EINVAL, "too many records in one set (%u)", n);
-  CU(ctx->scan_tmp.ensure((size_t)(tiles + 1) * 8 * 2));
-  uint64_t *bsum = ctx->scan_tmp.as<uint64_t>();
-  uint64_t *boff = bsum + tiles + 1;
-  k_scan64_block<<<tiles, 1024, 0, s>>>(ctx->slot_tmp.as<uint64_t>(), ctx->poff_tmp.as<uint64_t>(), n, bsum);
-  ++ctx->launches;
-  if (tiles > 1) {
-    k_scan64_block<<<1, 1024, 0, s>>>(bsum, boff, tiles, nullptr);
-    ++ctx->launches;
-    k_scan64_add<<<tiles, 1024, 0, s>>>(ctx->poff_tmp.as<uint64_t>(), n, boff);
+  CU(ctx->len_tmp.ensure((size_t)n * 4));
+  CU(ctx->poff_tmp.ensure((size_t)n * 8));
+  CU(ctx->scan_tmp.ensure((size_t)tiles * 8));
+  // counts [NBUCKETS], descending cursors [NBUCKETS], the largest bucket
+  CU(ctx->hist.ensure((size_t)NBUCKETS * 4 * 2 + 16));
+  uint32_t *counts = ctx->hist.as<uint32_t>(), *cursor = counts + NBUCKETS, *max_bucket = cursor + NBUCKETS;
+  // what the host reads back: largest code, largest bucket, counts
+  CU(ctx->summary.ensure((size_t)(2 + NBUCKETS) * 4));
+  uint32_t *summary = ctx->summary.as<uint32_t>();
+  CU(cudaEventRecord(ctx->load_ev[1], s));
+  if (ctx->pack_dirty) {  // first load, or the last one stopped before k_scatter cleared the accumulators
+    k_zero2<<<64, 1024, 0, s>>>(counts, NBUCKETS, max_bucket, 1);
     ++ctx->launches;
   }
-  // descending bucket cursors (the counts stay for the host copy below)
-  k_bucket_sums<<<BUCKET_BLOCKS, 1024, 0, s>>>(counts, max_code + 1, bsums);
+  ctx->pack_dirty = true;
+  uint64_t *tile_sum = ctx->scan_tmp.as<uint64_t>();
+  k_lengths<<<tiles, 1024, 0, s>>>(ctx->off_in.as<uint64_t>(), end, n, ctx->len_tmp.as<uint32_t>(), tile_sum, counts,
+                                   max_bucket, summary);
   ++ctx->launches;
-  k_bucket_cursors<<<BUCKET_BLOCKS, 1024, 0, s>>>(counts, max_code + 1, bsums, cursor);
+  k_scan_slots<<<tiles, 1024, 0, s>>>(ctx->len_tmp.as<uint32_t>(), n, tile_sum, ctx->poff_tmp.as<uint64_t>());
+  ++ctx->launches;
+  k_bucket_cursors<<<BUCKET_BLOCKS, 1024, 0, s>>>(counts, max_bucket, cursor, summary);
   ++ctx->launches;
   const uint64_t packed = rs.total + 16ull * n + 16;
   take_spare_set(ctx, rs, packed);
@@ -466,8 +469,11 @@ int pack_set(ish_ctx *ctx, uint32_t n, uint64_t raw_bytes, const uint64_t *end, 
   CU(rs.off_s.ensure((size_t)n * 8));
   CU(rs.orig_s.ensure((size_t)n * 4));
   k_scatter<<<ceil_div(n, 1024), 1024, 0, s>>>(ctx->len_tmp.as<uint32_t>(), ctx->poff_tmp.as<uint64_t>(), n, cursor,
-                               rs.len_s.as<uint32_t>(), rs.off_s.as<uint64_t>(), rs.orig_s.as<uint32_t>());
+                                               rs.len_s.as<uint32_t>(), rs.off_s.as<uint64_t>(),
+                                               rs.orig_s.as<uint32_t>(), counts, max_bucket, summary);
   ++ctx->launches;
+  CU(cudaGetLastError());
+  ctx->pack_dirty = false;
   {
     cudaError_t e = rs.codes.ensure(packed);
     if (e == cudaErrorMemoryAllocation && !ctx->spare_sets.empty()) {  // give the cached buffers back first
@@ -482,43 +488,48 @@ int pack_set(ish_ctx *ctx, uint32_t n, uint64_t raw_bytes, const uint64_t *end, 
   // chunks per record, 4 to 32
   uint32_t gw = 4;
   while (gw < 32 && (uint64_t)gw * 16 * n < rs.total) gw <<= 1;
-  const uint32_t pb = std::min<uint32_t>(ceil_div((uint64_t)n * gw, 256), (uint32_t)ctx->num_sms * 8);
+  ctx->raw_overlapped = raw_pending;
+  if (raw_pending) CU(cudaStreamWaitEvent(s, ctx->raw_ev, 0));  // the records' bytes are on the device
+  const uint32_t pb = std::min<uint32_t>(ceil_div((uint64_t)n * gw, 256), (uint32_t)ctx->num_sms * 3);
   k_pack<<<pb, 256, 0, s>>>(ctx->raw.as<uint8_t>(), raw_bytes, ctx->off_in.as<uint64_t>(), end,
-                            ctx->poff_tmp.as<uint64_t>(), n, enc, rs.codes.as<uint8_t>(), max_code, gw);
+                            ctx->poff_tmp.as<uint64_t>(), n, enc, rs.codes.as<uint8_t>(), summary, gw);
   ++ctx->launches;
   CU(cudaGetLastError());
   CU(cudaEventRecord(ctx->load_ev[2], s));
   if (defer) {
     // the summary the host needs, read back when the set is first used
-    CU(cudaMemcpyAsync(ctx->h_summary, max_code, 8, cudaMemcpyDeviceToHost, s));
-    CU(cudaMemcpyAsync(ctx->h_summary + 2, counts, (size_t)NBUCKETS * 4, cudaMemcpyDeviceToHost, s));
+    CU(cudaMemcpyAsync(ctx->h_summary, summary, (size_t)(2 + NBUCKETS) * 4, cudaMemcpyDeviceToHost, s));
     CU(cudaEventRecord(ctx->load_done, s));
     rs.pending = true;
     return ISH_OK;
   }
-  // host copy of the histogram: the buckets of lengths up to HIST_HEAD in the
-  // same round trip as the largest code and bucket, the rest (long records
-  // only) after it
+  // host copy of the summary: the largest code and bucket and the counts of
+  // the buckets of lengths below HIST_HEAD in one round trip, the rest (long
+  // records only) after it
   constexpr uint32_t HIST_HEAD = 8192;
-  uint32_t mc[2] = {0, 0};
-  rs.hist.assign(NBUCKETS, 0);
-  CU(cudaMemcpyAsync(mc, ctx->max_code.p, 8, cudaMemcpyDeviceToHost, s));
-  CU(cudaMemcpyAsync(rs.hist.data(), counts, (size_t)HIST_HEAD * 4, cudaMemcpyDeviceToHost, s));
+  uint32_t *h = ctx->h_summary;
+  CU(cudaMemcpyAsync(h, summary, (size_t)(2 + HIST_HEAD) * 4, cudaMemcpyDeviceToHost, s));
   CU(cudaStreamSynchronize(s));
-  rs.max_code = mc[0];
-  const uint32_t maxb = std::min<uint32_t>(mc[1], NBUCKETS - 1);
+  const uint32_t maxb = std::min<uint32_t>(h[1], NBUCKETS - 1);
   if (maxb >= HIST_HEAD) {
-    CU(cudaMemcpyAsync(rs.hist.data() + HIST_HEAD, counts + HIST_HEAD, (size_t)(maxb + 1 - HIST_HEAD) * 4,
+    CU(cudaMemcpyAsync(h + 2 + HIST_HEAD, summary + 2 + HIST_HEAD, (size_t)(maxb + 1 - HIST_HEAD) * 4,
                        cudaMemcpyDeviceToHost, s));
     CU(cudaStreamSynchronize(s));
   }
+  set_summary(rs, h);
+  load_phase_times(ctx);
+  return ISH_OK;
+}
+
+// A set's host-side summary from the device's {largest code, largest bucket,
+// counts}; counts above the largest bucket are not read (they are zero).
+void set_summary(RecordSet &rs, const uint32_t *h) {
+  rs.max_code = h[0];
+  const uint32_t maxb = std::min<uint32_t>(h[1], NBUCKETS - 1);
+  rs.hist.assign(NBUCKETS, 0);
+  std::copy(h + 2, h + 2 + maxb + 1, rs.hist.begin());
   rs.n_empty = rs.hist[0];
   rs.max_len = maxb < 32768 ? maxb : (uint32_t)(32768 + ((uint64_t)(maxb - 32768) << 5) + 31);
-  float a = 0.f, b = 0.f;
-  if (cudaEventElapsedTime(&a, ctx->load_ev[0], ctx->load_ev[1]) == cudaSuccess) ctx->last_load_ms[0] = a;
-  if (cudaEventElapsedTime(&b, ctx->load_ev[1], ctx->load_ev[2]) == cudaSuccess) ctx->last_load_ms[1] = b;
-  (void)cudaGetLastError();
-  return ISH_OK;
 }
 
 // Upload and pack a record set given as concatenated records + n+1 offsets.
@@ -536,20 +547,36 @@ int load_records(ish_ctx *ctx, const uint8_t *records, const uint64_t *offsets, 
   if (bytes && !records) return fail(ctx, ISH_EINVAL, "records is NULL");
   rs.total = bytes;
   cudaStream_t s = stream ? stream : ctx->stream;
-  // raw bytes (+16 slack for the realigning pack loads)
+  // The offsets go first on s; the records' bytes (+16 slack for the
+  // realigning pack loads) follow on the copy stream once the offsets are in
+  // (everything before this load on s, which includes the previous pack's
+  // reads of the same buffer, is before that point too), while s computes
+  // lengths, packed offsets and sorted positions.
   CU(ctx->raw.ensure(bytes + 32));
-  CU(cudaEventRecord(ctx->load_ev[0], s));
-  if (bytes) CU(cudaMemcpyAsync(ctx->raw.p, records + base, bytes, cudaMemcpyHostToDevice, s));
   CU(ctx->off_in.ensure((size_t)(n + 1) * 8));
-  if (base == 0) {
-    CU(cudaMemcpyAsync(ctx->off_in.p, offsets, (size_t)(n + 1) * 8, cudaMemcpyHostToDevice, s));
-  } else {
-    std::vector<uint64_t> rebased(offsets, offsets + n + 1);
+  CU(cudaEventRecord(ctx->load_ev[0], s));
+  std::vector<uint64_t> rebased;
+  if (base) {
+    rebased.assign(offsets, offsets + n + 1);
     for (auto &v : rebased) v -= base;
-    CU(cudaMemcpyAsync(ctx->off_in.p, rebased.data(), (size_t)(n + 1) * 8, cudaMemcpyHostToDevice, s));
-    CU(cudaStreamSynchronize(s));
   }
-  return pack_set(ctx, n, bytes, nullptr, enc, rs, s, defer);
+  CU(cudaMemcpyAsync(ctx->off_in.p, base ? rebased.data() : offsets, (size_t)(n + 1) * 8, cudaMemcpyHostToDevice, s));
+  CU(cudaEventRecord(ctx->off_ev, s));
+  {
+    cudaStream_t c = ctx->copy_stream;
+    cudaError_t oe = cudaStreamWaitEvent(c, ctx->off_ev, 0);
+    if (oe == cudaSuccess && bytes) oe = cudaMemcpyAsync(ctx->raw.p, records + base, bytes, cudaMemcpyHostToDevice, c);
+    if (oe == cudaSuccess) oe = cudaEventRecord(ctx->raw_ev, c);
+    if (oe != cudaSuccess) {
+      cudaStreamSynchronize(c);  // the caller's buffers are free again on return
+      cudaStreamSynchronize(s);
+      CU(oe);
+    }
+  }
+  if (base) CU(cudaEventSynchronize(ctx->off_ev));  // the rebased offsets are a temporary
+  const int rc = pack_set(ctx, n, bytes, nullptr, enc, rs, s, defer, bytes != 0);
+  if (rc && bytes) cudaStreamSynchronize(ctx->copy_stream);
+  return rc;
 }
 
 // Completes the asynchronous load in flight: waits for its stream's work and
@@ -570,16 +597,8 @@ int finish_pending_load(ish_ctx *ctx) {
     return fail(ctx, ISH_EDEVICE, "asynchronous load of record set %d failed: %s (the set is gone)", id,
                 cudaGetErrorString(e));
   }
-  const uint32_t *h = ctx->h_summary;
-  rs.max_code = h[0];
-  const uint32_t maxb = std::min<uint32_t>(h[1], NBUCKETS - 1);
-  rs.hist.assign(h + 2, h + 2 + NBUCKETS);
-  rs.n_empty = rs.hist[0];
-  rs.max_len = maxb < 32768 ? maxb : (uint32_t)(32768 + ((uint64_t)(maxb - 32768) << 5) + 31);
-  float a = 0.f, b = 0.f;
-  if (cudaEventElapsedTime(&a, ctx->load_ev[0], ctx->load_ev[1]) == cudaSuccess) ctx->last_load_ms[0] = a;
-  if (cudaEventElapsedTime(&b, ctx->load_ev[1], ctx->load_ev[2]) == cudaSuccess) ctx->last_load_ms[1] = b;
-  (void)cudaGetLastError();
+  set_summary(rs, ctx->h_summary);
+  load_phase_times(ctx);
   return ISH_OK;
 }
 
@@ -995,6 +1014,11 @@ int ish_gpu_open(int device, ish_ctx **out) {
     if ((e = cudaEventCreate(&ev)) != cudaSuccess) return bail(e, "cudaEventCreate");
   if ((e = cudaStreamCreateWithFlags(&ctx->load_stream, cudaStreamNonBlocking)) != cudaSuccess)
     return bail(e, "cudaStreamCreate");
+  if ((e = cudaStreamCreateWithFlags(&ctx->copy_stream, cudaStreamNonBlocking)) != cudaSuccess)
+    return bail(e, "cudaStreamCreate");
+  if ((e = cudaEventCreate(&ctx->raw_ev)) != cudaSuccess) return bail(e, "cudaEventCreate");
+  if ((e = cudaEventCreateWithFlags(&ctx->off_ev, cudaEventDisableTiming)) != cudaSuccess)
+    return bail(e, "cudaEventCreate");
   if ((e = cudaEventCreateWithFlags(&ctx->load_done, cudaEventDisableTiming)) != cudaSuccess)
     return bail(e, "cudaEventCreate");
   if ((e = cudaHostAlloc((void **)&ctx->h_summary, (size_t)(2 + NBUCKETS) * 4, cudaHostAllocDefault)) != cudaSuccess)
@@ -1013,7 +1037,7 @@ void ish_gpu_close(ish_ctx *ctx) {
   for (auto &kv : ctx->queries) release_query(kv.second);
   for (auto &kv : ctx->sets) release_set(kv.second);
   for (RecordSet &sp : ctx->spare_sets) release_set(sp);
-  DevBuf *bufs[] = {&ctx->raw, &ctx->off_in, &ctx->len_tmp, &ctx->slot_tmp, &ctx->poff_tmp, &ctx->hist, &ctx->max_code,
+  DevBuf *bufs[] = {&ctx->raw, &ctx->off_in, &ctx->len_tmp, &ctx->poff_tmp, &ctx->hist, &ctx->summary,
                     &ctx->scan_tmp, &ctx->counter, &ctx->error, &ctx->out_score, &ctx->out_qend, &ctx->out_tend,
                     &ctx->out_hit, &ctx->hit_idx, &ctx->block_counts, &ctx->nhits, &ctx->plain_scratch,
                     &ctx->enc_tables, &ctx->nl_pos, &ctx->line_end};
@@ -1025,6 +1049,9 @@ void ish_gpu_close(ish_ctx *ctx) {
   cudaEventDestroy(ctx->ev1);
   cudaEventDestroy(ctx->load_done);
   cudaStreamDestroy(ctx->load_stream);
+  if (ctx->raw_ev) cudaEventDestroy(ctx->raw_ev);
+  if (ctx->off_ev) cudaEventDestroy(ctx->off_ev);
+  if (ctx->copy_stream) cudaStreamDestroy(ctx->copy_stream);
   cudaFreeHost(ctx->h_summary);
   for (cudaEvent_t ev : ctx->load_ev) cudaEventDestroy(ev);
   cudaStreamDestroy(ctx->stream);

@@ -27,82 +27,162 @@ __device__ __forceinline__ uint64_t rec_len(const uint64_t *off, const uint64_t 
   return (end ? end[i] : off[i + 1]) - off[i];
 }
 
-// Lengths, 16-byte slot sizes and the length histogram.  The buckets below
-// SMEM_BUCKETS are counted in shared memory and flushed once per block (a
-// set's lengths crowd into a few hundred buckets, and one global atomic per
-// record on those few addresses would serialise); longer records go to the
-// global histogram directly.  Launched with 1024 threads.
-__global__ void __launch_bounds__(1024) k_lengths(const uint64_t *off, const uint64_t *end, uint32_t n, uint32_t *len,
-                                                  uint64_t *slot_bytes, uint32_t *hist, uint32_t *max_bucket) {
-  __shared__ uint32_t sh[SMEM_BUCKETS];
-  for (uint32_t k = threadIdx.x; k < SMEM_BUCKETS; k += blockDim.x) sh[k] = 0;
-  __syncthreads();
-  uint32_t mb = 0;
-  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-    const uint64_t l = rec_len(off, end, i);
-    len[i] = (uint32_t)l;
-    slot_bytes[i] = (l + 15) & ~(uint64_t)15;
-    const uint32_t b = len_bucket(l);
-    if (b < SMEM_BUCKETS) atomicAdd(&sh[b], 1u);
-    else atomicAdd(&hist[b], 1u);
-    mb = max(mb, b);
+// The packing kernels below run in this order on one stream: k_lengths,
+// k_scan_slots, k_bucket_cursors, k_scatter, k_pack.  The accumulators they
+// share between loads -- the length histogram `hist` and the largest length
+// bucket `max_bucket` -- are zero when a load starts and are zeroed again by
+// k_scatter, their last reader, so a load needs no separate clearing pass;
+// what the host reads back goes to `summary` = {largest code, largest
+// bucket, per-bucket record counts}.  (The host clears the accumulators with
+// k_zero2 after a load that stopped half way.)
+__global__ void k_zero2(uint32_t *a, uint32_t na, uint32_t *b, uint32_t nb) {
+  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < na + nb; i += gridDim.x * blockDim.x) {
+    if (i < na) a[i] = 0;
+    else b[i - na] = 0;
   }
-  for (int o = 16; o > 0; o >>= 1) mb = max(mb, __shfl_xor_sync(0xffffffffu, mb, o));
-  if ((threadIdx.x & 31) == 0 && mb) atomicMax(max_bucket, mb);
+}
+
+// Per record: its length; per tile of SCAN_TILE records (one 1024-thread
+// block, four consecutive records per thread): the sum of the 16-byte slot
+// sizes; and the length histogram.  The buckets below SMEM_BUCKETS are counted
+// in shared memory and flushed once per block (a set's lengths crowd into a few
+// hundred buckets, and one global atomic per record on those few addresses
+// would serialise); longer records go to the global histogram directly.
+__global__ void __launch_bounds__(1024) k_lengths(const uint64_t *off, const uint64_t *end, uint32_t n, uint32_t *len,
+                                                  uint64_t *tile_sum, uint32_t *hist, uint32_t *max_bucket,
+                                                  uint32_t *summary) {
+  __shared__ uint32_t sh[SMEM_BUCKETS];
+  __shared__ uint64_t wsum[32];
+  for (uint32_t k = threadIdx.x; k < SMEM_BUCKETS; k += blockDim.x) sh[k] = 0;
+  if (blockIdx.x == 0 && threadIdx.x == 0) summary[0] = 0;  // largest code, raised by k_pack
   __syncthreads();
+  constexpr int PER = SCAN_TILE / 1024;
+  uint32_t mb = 0;
+  uint64_t slots = 0;
+#pragma unroll
+  for (int k = 0; k < PER; ++k) {
+    const uint32_t i = blockIdx.x * SCAN_TILE + threadIdx.x * PER + k;
+    if (i < n) {
+      const uint64_t l = rec_len(off, end, i);
+      len[i] = (uint32_t)l;
+      slots += (l + 15) & ~(uint64_t)15;
+      const uint32_t b = len_bucket(l);
+      if (b < SMEM_BUCKETS) atomicAdd(&sh[b], 1u);
+      else atomicAdd(&hist[b], 1u);
+      mb = max(mb, b);
+    }
+  }
+  const uint32_t lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  for (int o = 16; o > 0; o >>= 1) {
+    mb = max(mb, __shfl_xor_sync(0xffffffffu, mb, o));
+    slots += __shfl_xor_sync(0xffffffffu, slots, o);
+  }
+  if (lane == 0) {
+    if (mb) atomicMax(max_bucket, mb);
+    wsum[wid] = slots;
+  }
+  __syncthreads();
+  if (wid == 0) {
+    uint64_t t = wsum[lane];
+    for (int o = 16; o > 0; o >>= 1) t += __shfl_xor_sync(0xffffffffu, t, o);
+    if (lane == 0) tile_sum[blockIdx.x] = t;
+  }
   for (uint32_t k = threadIdx.x; k < SMEM_BUCKETS; k += blockDim.x)
     if (sh[k]) atomicAdd(&hist[k], sh[k]);
 }
 
-// Exclusive scan of the bucket histogram in DESCENDING bucket order, in two
-// passes of BUCKET_BLOCKS blocks: block b covers the descending positions
-// [b*1024, b*1024 + 1024), i.e. buckets NBUCKETS-1-(b*1024+t), so every load
-// is coalesced.  Blocks whose buckets all lie above the set's largest bucket
-// hold no records and skip their loads.
-__device__ __forceinline__ bool bucket_block_empty(uint32_t b, const uint32_t *max_bucket) {
-  return NBUCKETS - 1024 * (b + 1) > *max_bucket;  // the block's smallest bucket is above the largest used
-}
-
-__global__ void __launch_bounds__(1024) k_bucket_sums(const uint32_t *hist, const uint32_t *max_bucket,
-                                                      uint32_t *sums) {
-  __shared__ uint32_t warp_sum[32];
-  const uint32_t b = blockIdx.x;
-  if (bucket_block_empty(b, max_bucket)) {
-    if (threadIdx.x == 0) sums[b] = 0;
-    return;
-  }
-  uint32_t v = hist[NBUCKETS - 1 - (b * 1024 + threadIdx.x)];
-  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-  if ((threadIdx.x & 31) == 0) warp_sum[threadIdx.x >> 5] = v;
+// Packed offset of every record: the exclusive scan of the 16-byte slot sizes
+// in record order.  Block b scans tile b and adds the slots of the tiles
+// before it (at most SCAN_TILE tile sums, summed by the block itself), so one
+// pass does what a scan of tile sums and an add pass would.
+__global__ void __launch_bounds__(1024) k_scan_slots(const uint32_t *len, uint32_t n, const uint64_t *tile_sum,
+                                                     uint64_t *poff) {
+  __shared__ uint64_t warp_sums[32];
+  __shared__ uint64_t before;
+  const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
+  // slots of the earlier tiles
+  uint64_t e = 0;
+  for (uint32_t t = tid; t < blockIdx.x; t += blockDim.x) e += tile_sum[t];
+  for (int o = 16; o > 0; o >>= 1) e += __shfl_xor_sync(0xffffffffu, e, o);
+  if (lane == 0) warp_sums[wid] = e;
   __syncthreads();
-  if (threadIdx.x < 32) {
-    uint32_t w = warp_sum[threadIdx.x];
+  if (wid == 0) {
+    uint64_t w = warp_sums[lane];
     for (int o = 16; o > 0; o >>= 1) w += __shfl_xor_sync(0xffffffffu, w, o);
-    if (threadIdx.x == 0) sums[b] = w;
+    if (lane == 0) before = w;
+  }
+  __syncthreads();
+  constexpr int PER = SCAN_TILE / 1024;
+  const uint32_t base = blockIdx.x * SCAN_TILE + tid * PER;
+  uint64_t v[PER], sum = 0;
+#pragma unroll
+  for (int k = 0; k < PER; ++k) {
+    v[k] = base + k < n ? ((uint64_t)len[base + k] + 15) & ~(uint64_t)15 : 0;
+    sum += v[k];
+  }
+  uint64_t x = sum;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const uint64_t y = __shfl_up_sync(0xffffffffu, x, o);
+    if (lane >= o) x += y;
+  }
+  if (lane == 31) warp_sums[wid] = x;  // the earlier reads of warp_sums ended at the barrier above
+  __syncthreads();
+  if (wid == 0) {
+    uint64_t w = warp_sums[lane];
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const uint64_t y = __shfl_up_sync(0xffffffffu, w, o);
+      if (lane >= o) w += y;
+    }
+    warp_sums[lane] = w;
+  }
+  __syncthreads();
+  uint64_t run = before + x - sum + (wid > 0 ? warp_sums[wid - 1] : 0);
+#pragma unroll
+  for (int k = 0; k < PER; ++k) {
+    if (base + k < n) poff[base + k] = run;
+    run += v[k];
   }
 }
 
+// First sorted position of every length bucket, buckets in DESCENDING order
+// (longest records first): block b covers the descending positions
+// [b*1024, b*1024 + 1024), i.e. buckets NBUCKETS-1-(b*1024+t), so its loads
+// are coalesced, and adds the records of the positions before it that can
+// hold any (buckets up to the set's largest).  Blocks whose buckets all lie
+// above the largest hold no records and stop at once.  The counts and the
+// largest bucket are copied to `summary` for the host.
 __global__ void __launch_bounds__(1024) k_bucket_cursors(const uint32_t *hist, const uint32_t *max_bucket,
-                                                         const uint32_t *sums, uint32_t *cursor) {
+                                                         uint32_t *cursor, uint32_t *summary) {
   __shared__ uint32_t warp_incl[32];
   __shared__ uint32_t base;
-  const uint32_t b = blockIdx.x;
-  if (bucket_block_empty(b, max_bucket)) return;  // no record lands in these buckets
-  const uint32_t tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-  if (warp == 0) {  // records in the blocks before this one (BUCKET_BLOCKS <= 64)
-    uint32_t s = 0;
-    for (uint32_t k = lane; k < b; k += 32) s += sums[k];
-    for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
-    if (lane == 0) base = s;
+  const uint32_t b = blockIdx.x, tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const uint32_t maxb = *max_bucket;
+  if (b == 0 && tid == 0) summary[1] = maxb;
+  if (NBUCKETS - 1024 * (b + 1) > maxb) return;  // the block's smallest bucket is above the largest used
+  // records at the descending positions [lo, b*1024): buckets maxb down to the block's first
+  const uint32_t lo = NBUCKETS - 1 - maxb;
+  uint32_t e = 0;
+  for (uint32_t p = lo + tid; p < b * 1024; p += 1024) e += hist[NBUCKETS - 1 - p];
+  for (int o = 16; o > 0; o >>= 1) e += __shfl_xor_sync(0xffffffffu, e, o);
+  if (lane == 0) warp_incl[warp] = e;
+  __syncthreads();
+  if (warp == 0) {
+    uint32_t w = warp_incl[lane];
+    for (int o = 16; o > 0; o >>= 1) w += __shfl_xor_sync(0xffffffffu, w, o);
+    if (lane == 0) base = w;
   }
+  __syncthreads();
   const uint32_t bucket = NBUCKETS - 1 - (b * 1024 + tid);
   const uint32_t c = hist[bucket];
+  summary[2 + bucket] = c;
   uint32_t incl = c;
   for (int o = 1; o < 32; o <<= 1) {
     const uint32_t x = __shfl_up_sync(0xffffffffu, incl, o);
     if (lane >= (uint32_t)o) incl += x;
   }
-  if (lane == 31) warp_incl[warp] = incl;
+  if (lane == 31) warp_incl[warp] = incl;  // the reads of warp_incl above ended at the barrier
   __syncthreads();
   if (warp == 0) {
     uint32_t w = warp_incl[lane];
@@ -123,11 +203,17 @@ __global__ void __launch_bounds__(1024) k_bucket_cursors(const uint32_t *hist, c
 // used bucket from the global cursor and writes; buckets from SMEM_BUCKETS on
 // (long records, few) take one global atomic per record.  The order within a
 // bucket is unspecified: the two lanes of a pair are scored independently.
+// The kernel also zeroes the histogram (buckets up to the largest, the only
+// ones that can be non-zero) and the largest bucket for the next load.
 __global__ void __launch_bounds__(1024) k_scatter(const uint32_t *len, const uint64_t *poff, uint32_t n,
                                                   uint32_t *cursor, uint32_t *len_s, uint64_t *off_s,
-                                                  uint32_t *orig_s) {
+                                                  uint32_t *orig_s, uint32_t *hist, uint32_t *max_bucket,
+                                                  const uint32_t *summary) {
   __shared__ uint32_t sh[SMEM_BUCKETS];  // counts, then the block's first position per bucket
   for (uint32_t k = threadIdx.x; k < SMEM_BUCKETS; k += blockDim.x) sh[k] = 0;
+  const uint32_t maxb = summary[1];
+  for (uint32_t k = blockIdx.x * blockDim.x + threadIdx.x; k <= maxb; k += gridDim.x * blockDim.x) hist[k] = 0;
+  if (blockIdx.x == 0 && threadIdx.x == 0) *max_bucket = 0;
   __syncthreads();
   const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
   uint32_t l = 0, b = 0, rank = 0;
@@ -158,7 +244,7 @@ __global__ void __launch_bounds__(1024) k_scatter(const uint32_t *len, const uin
 // the runners, ishlib/parallel_line_search_runner.mojo:90-94); the tail of the
 // 16-byte slot is zero-filled, and the largest code of the set is reduced into
 // *max_code, so a query's alphabet can be checked once per set.
-__global__ void k_pack(const uint8_t *src, uint64_t src_bytes, const uint64_t *off, const uint64_t *end,
+__global__ void __launch_bounds__(256, 3) k_pack(const uint8_t *src, uint64_t src_bytes, const uint64_t *off, const uint64_t *end,
                        const uint64_t *poff, uint32_t n, const uint8_t *enc, uint8_t *dst, uint32_t *max_code,
                        uint32_t gw) {
   __shared__ uint8_t table[256];
@@ -173,40 +259,70 @@ __global__ void k_pack(const uint8_t *src, uint64_t src_bytes, const uint64_t *o
   const uint32_t *src32 = reinterpret_cast<const uint32_t *>(src);
   const uint64_t nwords = (src_bytes + 3) >> 2;
   uint32_t mx = 0;
-  for (uint32_t r = group; r < n; r += ngroups) {
-    const uint64_t s0 = off[r], len = rec_len(off, end, r);
-    uint4 *d = reinterpret_cast<uint4 *>(dst + poff[r]);
-    const uint64_t nchunks = (len + 15) >> 4;
-    for (uint64_t c = glane; c < nchunks; c += gw) {
-      const uint64_t b = s0 + c * 16;  // first source byte of the chunk
-      const uint64_t w0 = b >> 2;
-      const uint32_t sh = (uint32_t)(b & 3) * 8;
-      uint32_t w[5];
+  // one 16-byte chunk: realign, encode, zero the bytes past the record end,
+  // store, and fold into the largest code
+  auto emit = [&](uint4 *d, uint64_t c, uint64_t len, uint64_t b, const uint32_t (&w)[5]) {
+    const uint32_t sh = (uint32_t)(b & 3) * 8;
+    uint32_t o[4];
 #pragma unroll
-      for (int k = 0; k < 5; ++k) w[k] = (w0 + k < nwords) ? __ldg(src32 + w0 + k) : 0u;
-      uint32_t o[4];
+    for (int k = 0; k < 4; ++k) o[k] = __funnelshift_r(w[k], w[k + 1], sh);
+    if (enc) {
 #pragma unroll
-      for (int k = 0; k < 4; ++k) o[k] = __funnelshift_r(w[k], w[k + 1], sh);
-      if (enc) {
-#pragma unroll
-        for (int k = 0; k < 4; ++k) {
-          const uint32_t x = o[k];
-          o[k] = (uint32_t)table[x & 0xffu] | ((uint32_t)table[(x >> 8) & 0xffu] << 8) |
-                 ((uint32_t)table[(x >> 16) & 0xffu] << 16) | ((uint32_t)table[x >> 24] << 24);
-        }
+      for (int k = 0; k < 4; ++k) {
+        const uint32_t x = o[k];
+        o[k] = (uint32_t)table[x & 0xffu] | ((uint32_t)table[(x >> 8) & 0xffu] << 8) |
+               ((uint32_t)table[(x >> 16) & 0xffu] << 16) | ((uint32_t)table[x >> 24] << 24);
       }
-      // zero bytes past the record end
-      const uint64_t rem = len - c * 16;
-      if (rem < 16) {
+    }
+    const uint64_t rem = len - c * 16;
+    if (rem < 16) {
 #pragma unroll
-        for (int k = 0; k < 4; ++k) {
-          const int64_t keep = (int64_t)rem - 4 * k;
-          if (keep <= 0) o[k] = 0;
-          else if (keep < 4) o[k] &= (1u << (8 * keep)) - 1u;
-        }
+      for (int k = 0; k < 4; ++k) {
+        const int64_t keep = (int64_t)rem - 4 * k;
+        if (keep <= 0) o[k] = 0;
+        else if (keep < 4) o[k] &= (1u << (8 * keep)) - 1u;
       }
-      d[c] = make_uint4(o[0], o[1], o[2], o[3]);
-      mx = __vmaxu4(mx, __vmaxu4(__vmaxu4(o[0], o[1]), __vmaxu4(o[2], o[3])));
+    }
+    d[c] = make_uint4(o[0], o[1], o[2], o[3]);
+    mx = __vmaxu4(mx, __vmaxu4(__vmaxu4(o[0], o[1]), __vmaxu4(o[2], o[3])));
+  };
+  auto load = [&](uint64_t b, uint32_t (&w)[5]) {
+    const uint64_t w0 = b >> 2;
+#pragma unroll
+    for (int k = 0; k < 5; ++k) w[k] = (w0 + k < nwords) ? __ldg(src32 + w0 + k) : 0u;
+  };
+  // PACK_U records per group at a time: their offsets, then the first chunk
+  // of each, are loaded before any is used, so that a group has several
+  // records' loads in flight (short records are latency-bound)
+  constexpr int PACK_U = 4;
+  for (uint64_t r0 = group; r0 < n; r0 += (uint64_t)PACK_U * ngroups) {
+    uint64_t s0[PACK_U], len[PACK_U], po[PACK_U];
+#pragma unroll
+    for (int u = 0; u < PACK_U; ++u) {
+      const uint64_t r = r0 + (uint64_t)u * ngroups;
+      s0[u] = len[u] = po[u] = 0;
+      if (r < n) {
+        s0[u] = off[r];
+        len[u] = rec_len(off, end, (uint32_t)r);
+        po[u] = poff[r];
+      }
+    }
+    uint32_t w[PACK_U][5];
+#pragma unroll
+    for (int u = 0; u < PACK_U; ++u) {
+      if ((uint64_t)glane * 16 < len[u]) load(s0[u] + (uint64_t)glane * 16, w[u]);
+    }
+#pragma unroll
+    for (int u = 0; u < PACK_U; ++u) {
+      uint4 *d = reinterpret_cast<uint4 *>(dst + po[u]);
+      const uint64_t nchunks = (len[u] + 15) >> 4;
+      if (glane < nchunks) emit(d, glane, len[u], s0[u] + (uint64_t)glane * 16, w[u]);
+      for (uint64_t c = glane + gw; c < nchunks; c += gw) {
+        const uint64_t b = s0[u] + c * 16;  // first source byte of the chunk
+        uint32_t wc[5];
+        load(b, wc);
+        emit(d, c, len[u], b, wc);
+      }
     }
   }
   uint32_t m = max(max(mx & 0xffu, (mx >> 8) & 0xffu), max((mx >> 16) & 0xffu, mx >> 24));

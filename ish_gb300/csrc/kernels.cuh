@@ -12,14 +12,16 @@ constexpr uint32_t HIT_TILE = 8192;      // records per block of the hit compact
 constexpr uint32_t SMEM_BUCKETS = 4096;  // length buckets counted in shared memory by k_lengths / k_scatter
 
 constexpr uint32_t LINE_TILE = 65536;    // text bytes per block of the line splitter
-__global__ void k_lengths(const uint64_t *off, const uint64_t *end, uint32_t n, uint32_t *len, uint64_t *slot_bytes,
-                          uint32_t *hist, uint32_t *max_bucket);
-constexpr uint32_t BUCKET_BLOCKS = NBUCKETS / 1024;  // blocks of the two-pass bucket scan
-__global__ void k_bucket_sums(const uint32_t *hist, const uint32_t *max_bucket, uint32_t *sums);
-__global__ void k_bucket_cursors(const uint32_t *hist, const uint32_t *max_bucket, const uint32_t *sums,
-                                 uint32_t *cursor);
+__global__ void k_zero2(uint32_t *a, uint32_t na, uint32_t *b, uint32_t nb);
+__global__ void k_lengths(const uint64_t *off, const uint64_t *end, uint32_t n, uint32_t *len, uint64_t *tile_sum,
+                          uint32_t *hist, uint32_t *max_bucket, uint32_t *summary);
+__global__ void k_scan_slots(const uint32_t *len, uint32_t n, const uint64_t *tile_sum, uint64_t *poff);
+constexpr uint32_t BUCKET_BLOCKS = NBUCKETS / 1024;  // blocks of the bucket cursor kernel
+__global__ void k_bucket_cursors(const uint32_t *hist, const uint32_t *max_bucket, uint32_t *cursor,
+                                 uint32_t *summary);
 __global__ void k_scatter(const uint32_t *len, const uint64_t *poff, uint32_t n, uint32_t *cursor, uint32_t *len_s,
-                          uint64_t *off_s, uint32_t *orig_s);
+                          uint64_t *off_s, uint32_t *orig_s, uint32_t *hist, uint32_t *max_bucket,
+                          const uint32_t *summary);
 __global__ void k_pack(const uint8_t *src, uint64_t src_bytes, const uint64_t *off, const uint64_t *end,
                        const uint64_t *poff, uint32_t n, const uint8_t *enc, uint8_t *dst, uint32_t *max_code,
                        uint32_t gw);
