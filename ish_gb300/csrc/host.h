@@ -135,12 +135,16 @@ struct RecordSet {
   uint64_t total = 0;
   uint32_t max_len = 0;
   DevBuf codes, off_s, len_s, orig_s;
-  std::vector<uint32_t> hist;  // length-bucket histogram (host copy)
+  std::vector<uint32_t> hist;  // length-bucket histogram (host copy) up to the largest bucket used
   uint32_t n_empty = 0;
   uint32_t max_code = 0;       // largest record code in the set
   DevBuf inv;                  // sorted entry of each original record (built on first use)
   WindowView windows;          // built on first windowed pass
 };
+
+// The largest length bucket a set's histogram holds (the buckets above it
+// have no records).
+inline uint32_t top_bucket(const RecordSet &rs) { return rs.hist.empty() ? 0u : (uint32_t)rs.hist.size() - 1; }
 
 struct Regime {
   bool fast = false;
@@ -185,6 +189,7 @@ struct ish_ctx {
   cudaStream_t load_stream = nullptr;  // asynchronous record loads (ish_gpu_records_load_async)
   cudaEvent_t load_done = nullptr;     // end of the asynchronous load in flight
   uint32_t *h_summary = nullptr;       // pinned: its largest code, largest bucket, then the histogram
+  uint64_t *h_small = nullptr;         // pinned: small results read back by a call (error flags, counts)
   int32_t pending_set = 0;             // the set whose asynchronous load is in flight (0: none)
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
   cudaEvent_t load_ev[3] = {nullptr, nullptr, nullptr};  // last load: start, packing start, end

@@ -526,8 +526,7 @@ int pack_set(ish_ctx *ctx, uint32_t n, uint64_t raw_bytes, const uint64_t *end, 
 void set_summary(RecordSet &rs, const uint32_t *h) {
   rs.max_code = h[0];
   const uint32_t maxb = std::min<uint32_t>(h[1], NBUCKETS - 1);
-  rs.hist.assign(NBUCKETS, 0);
-  std::copy(h + 2, h + 2 + maxb + 1, rs.hist.begin());
+  rs.hist.assign(h + 2, h + 2 + maxb + 1);
   rs.n_empty = rs.hist[0];
   rs.max_len = maxb < 32768 ? maxb : (uint32_t)(32768 + ((uint64_t)(maxb - 32768) << 5) + 31);
 }
@@ -637,11 +636,11 @@ int load_lines(ish_ctx *ctx, const uint8_t *text, uint64_t bytes, RecordSet &rs,
   ++ctx->launches;
   k_scan_counts<<<1, 1024, 0, s>>>(ctx->block_counts.as<uint32_t>(), tiles, ctx->nhits.as<uint32_t>());
   ++ctx->launches;
-  uint32_t n_nl = 0;
-  uint8_t last = 0;
-  CU(cudaMemcpyAsync(&n_nl, ctx->nhits.p, 4, cudaMemcpyDeviceToHost, s));
+  uint32_t *hs = reinterpret_cast<uint32_t *>(ctx->h_small);
+  CU(cudaMemcpyAsync(hs, ctx->nhits.p, 4, cudaMemcpyDeviceToHost, s));
   CU(cudaStreamSynchronize(s));
-  last = text[bytes - 1];
+  const uint32_t n_nl = hs[0];
+  const uint8_t last = text[bytes - 1];
   const uint64_t lines = (uint64_t)n_nl + (last != '\n' ? 1 : 0);
   if (lines >= 0xffffffffull) return fail(ctx, ISH_EINVAL, "too many lines (%llu)", (unsigned long long)lines);
   const uint32_t n = (uint32_t)lines;
@@ -658,10 +657,9 @@ int load_lines(ish_ctx *ctx, const uint8_t *text, uint64_t bytes, RecordSet &rs,
   ++ctx->launches;
   CU(cudaGetLastError());
   // residues: the text minus the newlines and the dropped carriage returns
-  unsigned long long total = 0;
-  CU(cudaMemcpyAsync(&total, ctx->nhits.p, 8, cudaMemcpyDeviceToHost, s));
+  CU(cudaMemcpyAsync(ctx->h_small, ctx->nhits.p, 8, cudaMemcpyDeviceToHost, s));
   CU(cudaStreamSynchronize(s));
-  rs.total = total;
+  rs.total = ctx->h_small[0];
   *n_out = n;
   return pack_set(ctx, n, bytes, ctx->line_end.as<uint64_t>(), enc, rs);
 }
@@ -670,7 +668,7 @@ int load_lines(ish_ctx *ctx, const uint8_t *text, uint64_t bytes, RecordSet &rs,
 // may exceed `len`.
 uint32_t count_longer(const RecordSet &rs, uint64_t len) {
   uint64_t cnt = 0;
-  for (uint32_t b = NBUCKETS - 1; b > 0; --b) {
+  for (uint32_t b = top_bucket(rs); b > 0; --b) {
     const uint64_t lo = b < 32768 ? b : 32768 + ((uint64_t)(b - 32768) << 5);
     const uint64_t hi = b < 32768 ? b : lo + 31;
     if (hi <= len) break;
@@ -953,16 +951,20 @@ int fetch_outputs(ish_ctx *ctx, uint32_t n, int32_t *score, int32_t *qend, int32
   if (n && qend) CU(cudaMemcpyAsync(qend, ctx->out_qend.p, (size_t)n * 4, cudaMemcpyDeviceToHost, s));
   if (n && tend) CU(cudaMemcpyAsync(tend, ctx->out_tend.p, (size_t)n * 4, cudaMemcpyDeviceToHost, s));
   if (n && hit) CU(cudaMemcpyAsync(hit, ctx->out_hit.p, (size_t)n, cudaMemcpyDeviceToHost, s));
-  int herr = 0;
-  uint32_t total = 0;
-  CU(cudaMemcpyAsync(&herr, ctx->error.p, 4, cudaMemcpyDeviceToHost, s));
-  if (compact) CU(cudaMemcpyAsync(&total, ctx->nhits.p, 4, cudaMemcpyDeviceToHost, s));
+  // error flags and hit count into pinned staging, so that every copy of the
+  // call stays asynchronous until the one synchronisation below
+  uint32_t *hs = reinterpret_cast<uint32_t *>(ctx->h_small);
+  hs[1] = 0;
+  CU(cudaMemcpyAsync(hs, ctx->error.p, 4, cudaMemcpyDeviceToHost, s));
+  if (compact) CU(cudaMemcpyAsync(hs + 1, ctx->nhits.p, 4, cudaMemcpyDeviceToHost, s));
   // the first hit indices travel with the count (hit_idx holds n entries, so
   // the prefix fits whatever the count); the rest, if any, after it
   constexpr uint32_t HIT_PREFIX = 4096;
   const uint32_t prefix = std::min<uint32_t>(n, HIT_PREFIX);
   if (hit_idx && compact) CU(cudaMemcpyAsync(hit_idx, ctx->hit_idx.p, (size_t)prefix * 4, cudaMemcpyDeviceToHost, s));
   CU(cudaStreamSynchronize(s));
+  const int herr = (int)hs[0];
+  const uint32_t total = hs[1];
   if (hit_idx && total > prefix) {
     CU(cudaMemcpyAsync(hit_idx + prefix, ctx->hit_idx.as<uint32_t>() + prefix, (size_t)(total - prefix) * 4,
                        cudaMemcpyDeviceToHost, s));
@@ -1023,6 +1025,8 @@ int ish_gpu_open(int device, ish_ctx **out) {
     return bail(e, "cudaEventCreate");
   if ((e = cudaHostAlloc((void **)&ctx->h_summary, (size_t)(2 + NBUCKETS) * 4, cudaHostAllocDefault)) != cudaSuccess)
     return bail(e, "cudaHostAlloc");
+  if ((e = cudaHostAlloc((void **)&ctx->h_small, 64 * 8, cudaHostAllocDefault)) != cudaSuccess)
+    return bail(e, "cudaHostAlloc");
   *out = ctx;
   return ISH_OK;
 }
@@ -1053,6 +1057,7 @@ void ish_gpu_close(ish_ctx *ctx) {
   if (ctx->off_ev) cudaEventDestroy(ctx->off_ev);
   if (ctx->copy_stream) cudaStreamDestroy(ctx->copy_stream);
   cudaFreeHost(ctx->h_summary);
+  if (ctx->h_small) cudaFreeHost(ctx->h_small);
   for (cudaEvent_t ev : ctx->load_ev) cudaEventDestroy(ev);
   cudaStreamDestroy(ctx->stream);
   delete ctx;

@@ -450,16 +450,18 @@ int ish_gpu_score_multi(ish_ctx *ctx, const int32_t *query_ids, uint32_t n_queri
   if (query_end) CU(cudaMemcpyAsync(query_end, P->qend.p, total * 4, cudaMemcpyDeviceToHost, s));
   if (target_end) CU(cudaMemcpyAsync(target_end, P->tend.p, total * 4, cudaMemcpyDeviceToHost, s));
   if (hit) CU(cudaMemcpyAsync(hit, P->hit.p, total, cudaMemcpyDeviceToHost, s));
-  int herr = 0;
-  uint32_t nh = 0;
   std::vector<uint32_t> offs;
-  CU(cudaMemcpyAsync(&herr, ctx->error.p, 4, cudaMemcpyDeviceToHost, s));
+  uint32_t *hs = reinterpret_cast<uint32_t *>(ctx->h_small);  // pinned: error flags, hit count
+  hs[1] = 0;
+  CU(cudaMemcpyAsync(hs, ctx->error.p, 4, cudaMemcpyDeviceToHost, s));
   if (want & W_COMPACT) {
     offs.resize((size_t)P->nb * n_queries);
     CU(cudaMemcpyAsync(offs.data(), P->block_counts.p, offs.size() * 4, cudaMemcpyDeviceToHost, s));
-    CU(cudaMemcpyAsync(&nh, P->nhits.p, 4, cudaMemcpyDeviceToHost, s));
+    CU(cudaMemcpyAsync(hs + 1, P->nhits.p, 4, cudaMemcpyDeviceToHost, s));
   }
   CU(cudaStreamSynchronize(s));
+  const int herr = (int)hs[0];
+  const uint32_t nh = hs[1];
   float ms = 0.f;
   if (cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1) == cudaSuccess) ctx->last_ms = ms;
   if (herr & 2) return fail(ctx, ISH_ETIMEDOUT, "batch kernel exceeded its step budget (internal error)");
@@ -546,7 +548,7 @@ int ish_gpu_autotune(ish_ctx *ctx, int32_t set_id, const int32_t *query_ids, uin
       {
         uint64_t pos = 0;
         double res = 0;
-        for (uint32_t b = NBUCKETS - 1; b >= 1 && count == 0; --b) {
+        for (uint32_t b = top_bucket(rs); b >= 1 && count == 0; --b) {
           const uint64_t c = rs.hist[b];
           if (pos + c > first) {
             const uint64_t from = std::max<uint64_t>(first, pos);

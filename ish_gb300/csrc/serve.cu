@@ -117,11 +117,11 @@ inline uint64_t bucket_len(uint32_t b) { return b < 32768 ? b : 32768 + ((uint64
 void make_chunks(Server &S, uint32_t n) {
   const RecordSet &rs = *S.rs;
   double total = 0;
-  for (uint32_t b = 1; b < NBUCKETS; ++b) total += (double)rs.hist[b] * (double)bucket_len(b);
+  for (uint32_t b = 1; b <= top_bucket(rs); ++b) total += (double)rs.hist[b] * (double)bucket_len(b);
   const double per = total / std::max<uint32_t>(n, 1);
   uint32_t pos = 0, first = 0;
   double acc = 0;
-  for (uint32_t b = NBUCKETS - 1; b >= 1; --b) {
+  for (uint32_t b = top_bucket(rs); b >= 1; --b) {
     uint64_t c = rs.hist[b];
     const double L = (double)bucket_len(b);
     while (c) {
@@ -147,7 +147,7 @@ void make_chunks(Server &S, uint32_t n) {
   // residues per chunk (for the cell count)
   uint32_t ci = 0;
   uint64_t at = 0;
-  for (uint32_t b = NBUCKETS - 1; b >= 1 && ci < S.chunks.size(); --b) {
+  for (uint32_t b = top_bucket(rs); b >= 1 && ci < S.chunks.size(); --b) {
     uint64_t c = rs.hist[b];
     while (c && ci < S.chunks.size()) {
       const uint64_t end = (uint64_t)S.chunks[ci].first + S.chunks[ci].second;
