@@ -314,7 +314,8 @@ def serving_leg(local, gb, count, rates=None):
     m = ScoringMatrix(wl.kind)
     out = {"workload": f"{gb:g} GB resident blosum62 set ({wl.n} records, lognormal median 350), Poisson arrivals, "
                        f"{count} queries per rate, Q ~ U[20,2000], striped-local / semi-global FFTT mix, gap 10/1, "
-                       "threshold 0.8", "records": wl.n, "residues": residues}
+                       "threshold 0.8; capacity = the same queries scored one launch each",
+           "records": wl.n, "residues": residues}
 
     deadline = time.perf_counter() + 900.0  # the whole leg; a stuck query fails it instead of hanging the run
 
@@ -337,20 +338,22 @@ def serving_leg(local, gb, count, rates=None):
 
     with native.Context(local) as ctx:
         sid = ctx.records_load(wl.records, wl.offsets)
-        # capacity from a few queries alone: their device time per query
-        probe = workloads.serving_queries(seed=9, count=12, rate=1.0)
-        pids = make(ctx, probe)
+        # the stream's queries (the same queries at every rate: the rate only
+        # scales their arrival times), each scored alone first: the device
+        # rate and capacity every rate below is offered against
+        stream = workloads.serving_queries(seed=5, count=count, rate=1.0)
+        pids = make(ctx, stream)
         alone_ms = 0.0
         alone = []
         for qid in pids:
             r = ctx.score_set(qid, sid, want=("hit_idx",))
             alone_ms += ctx.last_kernel_ms()
             alone.append(r["hit_idx"])
-        pcells = sum(len(q) for _, _, q in probe) * residues
+        pcells = sum(len(q) for _, _, q in stream) * residues
         single = pcells / (alone_ms * 1e-3) / 1e9
-        capacity = len(probe) / (alone_ms * 1e-3)
+        capacity = len(stream) / (alone_ms * 1e-3)
         # the same queries through the serving loop, submitted at once: the
-        # results must equal each query alone
+        # device rate at saturation, and every result against the query alone
         ctx.serve_start(sid, max_active=64, chunks=8)
         tickets = [ctx.submit(q) for q in pids]
         same = True
@@ -390,7 +393,7 @@ def serving_leg(local, gb, count, rates=None):
         ctx.records_free(sid)
     out.update({"single_query_launches_gcups": round(single, 1), "capacity_per_s": round(capacity, 3),
                 "saturated_device_gcups": round(sat, 1), "saturated_over_single": round(sat / single, 3),
-                "results_equal_alone": bool(same), "rates": per_rate})
+                "results_equal_alone": bool(same), "results_compared": len(alone), "rates": per_rate})
     return out
 
 

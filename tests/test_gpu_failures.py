@@ -180,3 +180,35 @@ def test_injected_allocation_failure(ctx):
     assert e.value.code == native.ENOMEM
     ctx.set_option(native.OPT_FAULT_ALLOC, -1)
     same(ctx.score_set(qid, sid), o, "resident set after the second fault")
+
+
+def test_allocation_failure_at_every_step_of_a_load(ctx):
+    """A load that fails at any one of its device allocations -- before the
+    packing kernels start, or after the first of them have run and touched the
+    shared length histogram -- leaves the context able to load and score: the
+    next load's results equal the oracle's.  Each attempt is larger than the
+    one before, so its buffers grow and allocate; the countdown picks which
+    allocation fails, and the synchronous and the asynchronous load alternate."""
+    rng = np.random.default_rng(23)
+    q = rng.integers(0, 20, 120, dtype=np.uint8)
+    qid = set_query(ctx, q, native.ALGO_SEMI_GLOBAL)
+    good_buf, good_off = protein(rng, 300, q)
+    o = oracle(good_buf, good_off, q, native.ALGO_SEMI_GLOBAL)
+    size, failures = 600, 0
+    for k in range(8):
+        size = int(size * 1.5)
+        buf, off = protein(rng, size, q)
+        load = ctx.records_load if k % 2 == 0 else ctx.records_load_async
+        ctx.set_option(native.OPT_FAULT_ALLOC, k)
+        try:
+            sid = load(buf, off)
+            ctx.records_info(sid)  # an asynchronous load completes here
+            ctx.records_free(sid)
+        except native.IshGpuError as e:
+            assert e.code == native.ENOMEM, str(e)
+            failures += 1
+        ctx.set_option(native.OPT_FAULT_ALLOC, -1)
+        sid = ctx.records_load(good_buf, good_off)
+        same(ctx.score_set(qid, sid), o, f"load after a fault at allocation {k}")
+        ctx.records_free(sid)
+    assert failures >= 3
