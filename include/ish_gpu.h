@@ -339,9 +339,13 @@ ISH_API int ish_gpu_last_kernel_ms(ish_ctx *ctx, double *ms);
 /* Phases of the last record load (ish_gpu_records_load*): upload_ms, device
  * time from the start of the host-to-device copy to the start of packing
  * (for text loads this includes the splitting kernels); pack_ms, device time
- * of the sort and pack kernels; wall_ms, host time of the whole call.  Any
- * pointer may be NULL.  No counterpart in the reference: measurement support
- * for the engine. */
+ * of the sort and pack kernels; wall_ms, host time of the whole call.  When
+ * the records' bytes are uploaded on the copy stream (concatenated records:
+ * ish_gpu_records_load, _async, _raw and ish_gpu_score), the sort kernels run
+ * during that upload, upload_ms ends with the upload and pack_ms is the time
+ * after it, so the two add up to the load's device time.  Any pointer may be
+ * NULL.  No counterpart in the reference: measurement support for the
+ * engine. */
 ISH_API int ish_gpu_last_load_ms(ish_ctx *ctx, double *upload_ms, double *pack_ms, double *wall_ms);
 
 /* Throughput of the packed 16-bit DPX add-max instruction on this device,

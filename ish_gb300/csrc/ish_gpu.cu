@@ -443,7 +443,8 @@ int pack_set(ish_ctx *ctx, uint32_t n, uint64_t raw_bytes, const uint64_t *end, 
   CU(ctx->len_tmp.ensure((size_t)n * 4));
   CU(ctx->poff_tmp.ensure((size_t)n * 8));
   CU(ctx->scan_tmp.ensure((size_t)tiles * 8));
-  // counts [NBUCKETS], descending cursors [NBUCKETS], the largest bucket
+  // counts [NBUCKETS], descending cursors [NBUCKETS], the largest bucket and
+  // the pack's long-record counter
   CU(ctx->hist.ensure((size_t)NBUCKETS * 4 * 2 + 16));
   uint32_t *counts = ctx->hist.as<uint32_t>(), *cursor = counts + NBUCKETS, *max_bucket = cursor + NBUCKETS;
   // what the host reads back: largest code, largest bucket, counts
@@ -451,7 +452,7 @@ int pack_set(ish_ctx *ctx, uint32_t n, uint64_t raw_bytes, const uint64_t *end, 
   uint32_t *summary = ctx->summary.as<uint32_t>();
   CU(cudaEventRecord(ctx->load_ev[1], s));
   if (ctx->pack_dirty) {  // first load, or the last one stopped before k_scatter cleared the accumulators
-    k_zero2<<<64, 1024, 0, s>>>(counts, NBUCKETS, max_bucket, 1);
+    k_zero2<<<64, 1024, 0, s>>>(counts, NBUCKETS, max_bucket, 2);
     ++ctx->launches;
   }
   ctx->pack_dirty = true;
@@ -490,9 +491,12 @@ int pack_set(ish_ctx *ctx, uint32_t n, uint64_t raw_bytes, const uint64_t *end, 
   while (gw < 32 && (uint64_t)gw * 16 * n < rs.total) gw <<= 1;
   ctx->raw_overlapped = raw_pending;
   if (raw_pending) CU(cudaStreamWaitEvent(s, ctx->raw_ev, 0));  // the records' bytes are on the device
-  const uint32_t pb = std::min<uint32_t>(ceil_div((uint64_t)n * gw, 256), (uint32_t)ctx->num_sms * 3);
+  // one group per record, or a block per 64 KB for sets of long records
+  const uint32_t pb = (uint32_t)std::min<uint64_t>(
+      std::max<uint64_t>(ceil_div((uint64_t)n * gw, 256), (rs.total >> 16) + 1), (uint64_t)ctx->num_sms * 3);
   k_pack<<<pb, 256, 0, s>>>(ctx->raw.as<uint8_t>(), raw_bytes, ctx->off_in.as<uint64_t>(), end,
-                            ctx->poff_tmp.as<uint64_t>(), n, enc, rs.codes.as<uint8_t>(), summary, gw);
+                            ctx->poff_tmp.as<uint64_t>(), n, rs.len_s.as<uint32_t>(), rs.orig_s.as<uint32_t>(),
+                            max_bucket + 1, enc, rs.codes.as<uint8_t>(), summary, gw);
   ++ctx->launches;
   CU(cudaGetLastError());
   CU(cudaEventRecord(ctx->load_ev[2], s));

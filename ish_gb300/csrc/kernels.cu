@@ -204,7 +204,8 @@ __global__ void __launch_bounds__(1024) k_bucket_cursors(const uint32_t *hist, c
 // (long records, few) take one global atomic per record.  The order within a
 // bucket is unspecified: the two lanes of a pair are scored independently.
 // The kernel also zeroes the histogram (buckets up to the largest, the only
-// ones that can be non-zero) and the largest bucket for the next load.
+// ones that can be non-zero) and the largest bucket for the next load, and
+// the long-record counter that k_pack takes next (max_bucket[1]).
 __global__ void __launch_bounds__(1024) k_scatter(const uint32_t *len, const uint64_t *poff, uint32_t n,
                                                   uint32_t *cursor, uint32_t *len_s, uint64_t *off_s,
                                                   uint32_t *orig_s, uint32_t *hist, uint32_t *max_bucket,
@@ -213,7 +214,10 @@ __global__ void __launch_bounds__(1024) k_scatter(const uint32_t *len, const uin
   for (uint32_t k = threadIdx.x; k < SMEM_BUCKETS; k += blockDim.x) sh[k] = 0;
   const uint32_t maxb = summary[1];
   for (uint32_t k = blockIdx.x * blockDim.x + threadIdx.x; k <= maxb; k += gridDim.x * blockDim.x) hist[k] = 0;
-  if (blockIdx.x == 0 && threadIdx.x == 0) *max_bucket = 0;
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    max_bucket[0] = 0;  // for the next load
+    max_bucket[1] = 0;  // k_pack's long-record counter, for this load
+  }
   __syncthreads();
   const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
   uint32_t l = 0, b = 0, rank = 0;
@@ -236,18 +240,28 @@ __global__ void __launch_bounds__(1024) k_scatter(const uint32_t *len, const uin
   }
 }
 
-// A group of `gw` lanes per record (a power of two up to 32, chosen by the
-// host near the set's average 16-byte chunks per record, so that short lines
-// do not leave most of a warp idle): the record is copied to dst[poff[i] ..)
-// in 16-byte chunks realigned with funnel shifts, optionally encoded through a 256-entry
-// byte table (ish's convert_ascii_to_encoding, done per byte on the host by
-// the runners, ishlib/parallel_line_search_runner.mojo:90-94); the tail of the
-// 16-byte slot is zero-filled, and the largest code of the set is reduced into
-// *max_code, so a query's alphabet can be checked once per set.
-__global__ void __launch_bounds__(256, 3) k_pack(const uint8_t *src, uint64_t src_bytes, const uint64_t *off, const uint64_t *end,
-                       const uint64_t *poff, uint32_t n, const uint8_t *enc, uint8_t *dst, uint32_t *max_code,
-                       uint32_t gw) {
+// Copies every record to dst[poff[i] ..) in 16-byte chunks realigned with
+// funnel shifts, optionally encoded through a 256-entry byte table (ish's
+// convert_ascii_to_encoding, done per byte on the host by the runners,
+// ishlib/parallel_line_search_runner.mojo:90-94); the tail of the 16-byte slot
+// is zero-filled, and the largest code of the set is reduced into *max_code,
+// so a query's alphabet can be checked once per set.  Records of PACK_LONG
+// bytes or more are copied first, each by a whole block, longest first (the
+// prefix of the sorted order, taken through *long_counter, which k_scatter
+// zeroed): one warp cannot keep enough loads in flight to copy a megabase
+// record quickly.  The other records go to groups of `gw` lanes (a power of
+// two up to 32, chosen by the host near the set's average 16-byte chunks per
+// record, so that short lines do not leave most of a warp idle), PACK_U
+// records per group at a time.
+constexpr uint64_t PACK_LONG = 16384;
+
+__global__ void __launch_bounds__(256, 3) k_pack(const uint8_t *src, uint64_t src_bytes, const uint64_t *off,
+                                                 const uint64_t *end, const uint64_t *poff, uint32_t n,
+                                                 const uint32_t *len_s, const uint32_t *orig_s,
+                                                 uint32_t *long_counter, const uint8_t *enc, uint8_t *dst,
+                                                 uint32_t *max_code, uint32_t gw) {
   __shared__ uint8_t table[256];
+  __shared__ uint32_t s_item;
   if (enc) {
     for (int i = threadIdx.x; i < 256; i += blockDim.x) table[i] = enc[i];
     __syncthreads();
@@ -291,20 +305,48 @@ __global__ void __launch_bounds__(256, 3) k_pack(const uint8_t *src, uint64_t sr
 #pragma unroll
     for (int k = 0; k < 5; ++k) w[k] = (w0 + k < nwords) ? __ldg(src32 + w0 + k) : 0u;
   };
-  // PACK_U records per group at a time: their offsets, then the first chunk
-  // of each, are loaded before any is used, so that a group has several
-  // records' loads in flight (short records are latency-bound)
-  constexpr int PACK_U = 4;
+  constexpr int PACK_U = 4, PACK_V = 2;
+  // chunks [c0, nchunks) of a record, `step` lanes apart, PACK_V per lane in flight
+  auto copy_from = [&](uint4 *d, uint64_t s0, uint64_t len, uint64_t c0, uint64_t step) {
+    const uint64_t nchunks = (len + 15) >> 4;
+    for (; c0 < nchunks; c0 += (uint64_t)PACK_V * step) {
+      uint32_t wc[PACK_V][5];
+#pragma unroll
+      for (int v = 0; v < PACK_V; ++v) {
+        const uint64_t c = c0 + (uint64_t)v * step;
+        if (c < nchunks) load(s0 + c * 16, wc[v]);
+      }
+#pragma unroll
+      for (int v = 0; v < PACK_V; ++v) {
+        const uint64_t c = c0 + (uint64_t)v * step;
+        if (c < nchunks) emit(d, c, len, s0 + c * 16, wc[v]);
+      }
+    }
+  };
+  // long records: a whole block each, longest first
+  for (;;) {
+    if (threadIdx.x == 0) s_item = atomicAdd(long_counter, 1u);
+    __syncthreads();
+    const uint32_t i = s_item;
+    __syncthreads();  // every thread has read s_item before it is taken again
+    if (i >= n || len_s[i] < PACK_LONG) break;
+    const uint32_t r = orig_s[i];
+    copy_from(reinterpret_cast<uint4 *>(dst + poff[r]), off[r], len_s[i], threadIdx.x, blockDim.x);
+  }
+  // the other records: PACK_U per group at a time, their offsets and then the
+  // first chunk of each loaded before any is used, so that a group has
+  // several records' loads in flight (short records are latency-bound)
   for (uint64_t r0 = group; r0 < n; r0 += (uint64_t)PACK_U * ngroups) {
     uint64_t s0[PACK_U], len[PACK_U], po[PACK_U];
 #pragma unroll
     for (int u = 0; u < PACK_U; ++u) {
       const uint64_t r = r0 + (uint64_t)u * ngroups;
       s0[u] = len[u] = po[u] = 0;
-      if (r < n) {
+      if (r < n) {  // three independent loads; a long record (done above) gets no work
         s0[u] = off[r];
-        len[u] = rec_len(off, end, (uint32_t)r);
         po[u] = poff[r];
+        const uint64_t l = rec_len(off, end, (uint32_t)r);
+        len[u] = l < PACK_LONG ? l : 0;
       }
     }
     uint32_t w[PACK_U][5];
@@ -315,14 +357,8 @@ __global__ void __launch_bounds__(256, 3) k_pack(const uint8_t *src, uint64_t sr
 #pragma unroll
     for (int u = 0; u < PACK_U; ++u) {
       uint4 *d = reinterpret_cast<uint4 *>(dst + po[u]);
-      const uint64_t nchunks = (len[u] + 15) >> 4;
-      if (glane < nchunks) emit(d, glane, len[u], s0[u] + (uint64_t)glane * 16, w[u]);
-      for (uint64_t c = glane + gw; c < nchunks; c += gw) {
-        const uint64_t b = s0[u] + c * 16;  // first source byte of the chunk
-        uint32_t wc[5];
-        load(b, wc);
-        emit(d, c, len[u], b, wc);
-      }
+      if ((uint64_t)glane * 16 < len[u]) emit(d, glane, len[u], s0[u] + (uint64_t)glane * 16, w[u]);
+      copy_from(d, s0[u], len[u], glane + gw, gw);
     }
   }
   uint32_t m = max(max(mx & 0xffu, (mx >> 8) & 0xffu), max((mx >> 16) & 0xffu, mx >> 24));

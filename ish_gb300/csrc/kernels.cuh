@@ -23,8 +23,8 @@ __global__ void k_scatter(const uint32_t *len, const uint64_t *poff, uint32_t n,
                           uint64_t *off_s, uint32_t *orig_s, uint32_t *hist, uint32_t *max_bucket,
                           const uint32_t *summary);
 __global__ void k_pack(const uint8_t *src, uint64_t src_bytes, const uint64_t *off, const uint64_t *end,
-                       const uint64_t *poff, uint32_t n, const uint8_t *enc, uint8_t *dst, uint32_t *max_code,
-                       uint32_t gw);
+                       const uint64_t *poff, uint32_t n, const uint32_t *len_s, const uint32_t *orig_s,
+                       uint32_t *long_counter, const uint8_t *enc, uint8_t *dst, uint32_t *max_code, uint32_t gw);
 __global__ void k_count_newlines(const uint8_t *text, uint64_t bytes, uint32_t *block_counts);
 __global__ void k_write_newlines(const uint8_t *text, uint64_t bytes, const uint32_t *block_offsets, uint64_t *pos);
 __global__ void k_line_bounds(const uint8_t *text, uint64_t bytes, const uint64_t *nl, uint32_t n_nl, uint32_t n_lines,
