@@ -118,30 +118,32 @@ __device__ uint32_t block_excl_maps(uint32_t m, uint32_t *total) {
 // First '>' or '@' of every line (the header a SEEK line starts), by
 // atomicMin; hc is preset to all ones.  block_offsets: newlines before each
 // LINE_TILE-byte tile (exclusive scan of k_count_newlines).
-__global__ void k_fx_header_chars(const uint8_t *text, uint64_t bytes, const uint32_t *block_offsets,
-                                  unsigned long long *hc) {
+__global__ void __launch_bounds__(1024) k_fx_header_chars(const uint8_t *text, uint64_t bytes,
+                                                          const uint32_t *block_offsets, unsigned long long *hc) {
   __shared__ uint32_t wsum[32];
-  __shared__ uint32_t run;
-  const uint64_t base = (uint64_t)blockIdx.x * LINE_TILE;
-  if (threadIdx.x == 0) run = block_offsets[blockIdx.x];
-  __syncthreads();
-  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
-  for (uint64_t b = base; b < bytes && b < base + LINE_TILE; b += blockDim.x) {
-    const uint64_t i = b + threadIdx.x;
-    const bool in = i < bytes && i < base + LINE_TILE;
-    const uint8_t ch = in ? text[i] : 0;
-    const uint32_t m = __ballot_sync(0xffffffffu, ch == '\n');
-    if (lane == 0) wsum[wid] = __popc(m);
-    __syncthreads();
-    uint32_t before = 0, total = 0;
-    for (int w = 0; w < nw; ++w) {
-      if (w < wid) before += wsum[w];
-      total += wsum[w];
+  const uint32_t lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  const uint64_t w0 = (uint64_t)blockIdx.x * LINE_TILE + (uint64_t)wid * LINE_WARP;
+  uint32_t run = warp_newline_base(text, bytes, block_offsets, w0, lane, wid, wsum);
+  for (uint32_t k = 0; k < LINE_WARP; k += 128) {
+    const uint64_t i = w0 + k + 4 * lane;
+    uint32_t nl = 0, h = 0;
+    if (i < bytes) {
+      nl = byte_bits(text, bytes, i, '\n');
+      h = byte_bits(text, bytes, i, '>') | byte_bits(text, bytes, i, '@');
     }
-    if (ch == '>' || ch == '@') atomicMin(hc + run + before + __popc(m & ((1u << lane) - 1u)), (unsigned long long)i);
-    __syncthreads();
-    if (threadIdx.x == 0) run += total;
-    __syncthreads();
+    const uint32_t cnt = __popc(nl);
+    uint32_t incl = cnt;
+    for (int o = 1; o < 32; o <<= 1) {
+      const uint32_t y = __shfl_up_sync(0xffffffffu, incl, o);
+      if (lane >= (uint32_t)o) incl += y;
+    }
+    const uint32_t before = run + incl - cnt;  // newlines before this lane's 4 bytes
+    while (h) {
+      const uint32_t bit = (uint32_t)(__ffs(h) - 1);
+      atomicMin(hc + before + __popc(nl & ((1u << bit) - 1u)), (unsigned long long)(i + bit));
+      h &= h - 1;
+    }
+    run += __shfl_sync(0xffffffffu, incl, 31);
   }
 }
 

@@ -373,45 +373,42 @@ __global__ void __launch_bounds__(256, 3) k_pack(const uint8_t *src, uint64_t sr
 // longer than one byte, a final line without '\n' is a record, and a final
 // '\n' does not start another one.
 // ---------------------------------------------------------------------------
-__global__ void k_count_newlines(const uint8_t *text, uint64_t bytes, uint32_t *block_counts) {
+__global__ void __launch_bounds__(1024) k_count_newlines(const uint8_t *text, uint64_t bytes, uint32_t *block_counts) {
   __shared__ uint32_t wsum[32];
-  const uint64_t base = (uint64_t)blockIdx.x * LINE_TILE;
-  uint32_t c = 0;
-  for (uint64_t i = base + threadIdx.x; i < bytes && i < base + LINE_TILE; i += blockDim.x) c += text[i] == '\n';
-  for (int o = 16; o > 0; o >>= 1) c += __shfl_down_sync(0xffffffffu, c, o);
-  if ((threadIdx.x & 31) == 0) wsum[threadIdx.x >> 5] = c;
+  const uint32_t lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  const uint32_t c = warp_newlines(text, bytes, (uint64_t)blockIdx.x * LINE_TILE + (uint64_t)wid * LINE_WARP, lane);
+  if (lane == 0) wsum[wid] = c;
   __syncthreads();
-  if (threadIdx.x < 32) {
-    uint32_t v = threadIdx.x < (blockDim.x >> 5) ? wsum[threadIdx.x] : 0;
-    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
-    if (threadIdx.x == 0) block_counts[blockIdx.x] = v;
+  if (wid == 0) {
+    uint32_t v = wsum[lane];
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    if (lane == 0) block_counts[blockIdx.x] = v;
   }
 }
 
 // Positions of the newlines, in order (block_offsets: exclusive scan of the
 // per-block counts).
-__global__ void k_write_newlines(const uint8_t *text, uint64_t bytes, const uint32_t *block_offsets, uint64_t *pos) {
+__global__ void __launch_bounds__(1024) k_write_newlines(const uint8_t *text, uint64_t bytes,
+                                                         const uint32_t *block_offsets, uint64_t *pos) {
   __shared__ uint32_t wsum[32];
-  __shared__ uint32_t run;
-  const uint64_t base = (uint64_t)blockIdx.x * LINE_TILE;
-  if (threadIdx.x == 0) run = block_offsets[blockIdx.x];
-  __syncthreads();
-  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
-  for (uint64_t b = base; b < bytes && b < base + LINE_TILE; b += blockDim.x) {
-    const uint64_t i = b + threadIdx.x;
-    const bool h = i < bytes && i < base + LINE_TILE && text[i] == '\n';
-    const uint32_t m = __ballot_sync(0xffffffffu, h);
-    if (lane == 0) wsum[wid] = __popc(m);
-    __syncthreads();
-    uint32_t before = 0, total = 0;
-    for (int w = 0; w < nw; ++w) {
-      if (w < wid) before += wsum[w];
-      total += wsum[w];
+  const uint32_t lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  const uint64_t w0 = (uint64_t)blockIdx.x * LINE_TILE + (uint64_t)wid * LINE_WARP;
+  uint32_t run = warp_newline_base(text, bytes, block_offsets, w0, lane, wid, wsum);
+  for (uint32_t k = 0; k < LINE_WARP; k += 128) {
+    const uint64_t i = w0 + k + 4 * lane;
+    uint32_t m = i < bytes ? byte_bits(text, bytes, i, '\n') : 0u;
+    const uint32_t cnt = __popc(m);
+    uint32_t incl = cnt;
+    for (int o = 1; o < 32; o <<= 1) {
+      const uint32_t y = __shfl_up_sync(0xffffffffu, incl, o);
+      if (lane >= (uint32_t)o) incl += y;
     }
-    if (h) pos[run + before + __popc(m & ((1u << lane) - 1u))] = i;
-    __syncthreads();
-    if (threadIdx.x == 0) run += total;
-    __syncthreads();
+    uint32_t p = run + incl - cnt;
+    while (m) {
+      pos[p++] = i + (uint32_t)(__ffs(m) - 1);
+      m &= m - 1;
+    }
+    run += __shfl_sync(0xffffffffu, incl, 31);
   }
 }
 

@@ -115,4 +115,51 @@ WaveFn wave_fn(int K, int mode, int layout, int lean = 0);
 typedef void (*BatchFn)(const BatchParams);
 BatchFn batch_fn(int K, int mode, int layout, int lean = 0);  // batch_kernel<K, mode, layout, lean> or nullptr
 
+// The splitting kernels take the text in tiles of LINE_TILE bytes per
+// 1024-thread block; warp w of a block covers LINE_WARP consecutive bytes of
+// its tile, 128 per step and 4 per lane, so no block-wide barrier runs inside
+// a loop.  The text lies in a buffer with at least 3 bytes of slack past its
+// end (every 4-byte word that starts inside it can be loaded) and starts
+// 4-byte aligned.
+constexpr uint32_t LINE_WARP = LINE_TILE / 32;
+
+// Bit k set where byte k of the 4 at text[i] (i < bytes, i % 4 == 0) is c and
+// lies inside the text.
+__device__ __forceinline__ uint32_t byte_bits(const uint8_t *text, uint64_t bytes, uint64_t i, uint32_t c) {
+  const uint32_t w = *reinterpret_cast<const uint32_t *>(text + i);
+  uint32_t m = 0;
+#pragma unroll
+  for (int k = 0; k < 4; ++k) m |= (uint32_t)(((w >> (8 * k)) & 0xffu) == c) << k;
+  const uint64_t left = bytes - i;
+  return left >= 4 ? m : m & ((1u << left) - 1u);
+}
+
+// Newlines of the warp's segment starting at byte w0 (every lane gets the count).
+__device__ __forceinline__ uint32_t warp_newlines(const uint8_t *text, uint64_t bytes, uint64_t w0, uint32_t lane) {
+  uint32_t c = 0;
+#pragma unroll 4
+  for (uint32_t k = 0; k < LINE_WARP; k += 128) {
+    const uint64_t i = w0 + k + 4 * lane;
+    if (i < bytes) c += __popc(byte_bits(text, bytes, i, '\n'));
+  }
+  for (int o = 16; o > 0; o >>= 1) c += __shfl_xor_sync(0xffffffffu, c, o);
+  return c;
+}
+
+// Newlines before each warp's segment: block_offsets (exclusive scan of the
+// per-tile counts) plus the tile's earlier warps.
+__device__ __forceinline__ uint32_t warp_newline_base(const uint8_t *text, uint64_t bytes,
+                                                      const uint32_t *block_offsets, uint64_t w0, uint32_t lane,
+                                                      uint32_t wid, uint32_t *wsum) {
+  const uint32_t c = warp_newlines(text, bytes, w0, lane);
+  if (lane == 0) wsum[wid] = c;
+  __syncthreads();
+  uint32_t x = wsum[lane];
+  for (int o = 1; o < 32; o <<= 1) {
+    const uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
+    if (lane >= (uint32_t)o) x += y;
+  }
+  return block_offsets[blockIdx.x] + __shfl_sync(0xffffffffu, x, wid) - c;
+}
+
 }  // namespace ish
