@@ -163,3 +163,34 @@ def test_records_get_ranges(ctx):
     with pytest.raises(native.IshGpuError):
         ctx.records_get(sid, 250, 60)
     ctx.records_free(sid)
+
+
+def test_packing_round_trip_short_and_long_records(ctx):
+    """Every record, as packed on the device, read back byte for byte: short
+    records (copied by lane groups sized to the set's average length), records
+    of 16 KB and more (copied by whole blocks, longest first) and empty ones,
+    at odd offsets in the caller's buffer (the pack realigns every record),
+    with and without the device-side encoding of raw text."""
+    rng = np.random.default_rng(41)
+    lens = ([int(x) for x in rng.integers(0, 200, 3000)] + [0, 1, 15, 16, 17, 16383, 16384, 16385]
+            + [int(x) for x in rng.integers(16384, 300_000, 12)])
+    rng.shuffle(lens)
+    recs = [rng.integers(0, 20, L, dtype=np.uint8) for L in lens]
+    buf, off = native.pack_records(recs)
+    # a caller's buffer whose records start 3 bytes into it
+    shifted = np.concatenate([np.full(3, 99, np.uint8), buf])
+    for b, o in ((buf, off), (shifted, off + np.uint64(3))):
+        sid = ctx.records_load(b, o)
+        codes, got = ctx.records_get(sid)
+        ctx.records_free(sid)
+        for i, r in enumerate(recs):
+            assert np.array_equal(codes[int(got[i]):int(got[i + 1])], r), (i, len(r))
+    # raw residues encoded on the device (blosum62 letters -> codes)
+    letters = ScoringMatrix(O.BLOSUM62).code_to_ascii
+    raw = [letters[r] for r in recs]
+    rbuf, roff = native.pack_records(raw)
+    sid = ctx.records_load_raw(rbuf, roff, O.BLOSUM62)
+    codes, got = ctx.records_get(sid)
+    ctx.records_free(sid)
+    for i, r in enumerate(recs):
+        assert np.array_equal(codes[int(got[i]):int(got[i + 1])], r), ("raw", i, len(r))
