@@ -418,10 +418,6 @@ int device_encoding(ish_ctx *ctx, int kind, const uint8_t **out) {
   return ISH_OK;
 }
 
-// Sort and pack n records held in ctx->raw (raw_bytes bytes): record i is
-// raw[off_in[i] .. end[i]) with `end` on the device, or raw[off_in[i] ..
-// off_in[i + 1]) without; `enc` (device, may be null) encodes bytes on the way
-// (see k_lengths .. k_pack in kernels.cu).  rs.total must hold the residue count.
 // Device phases of the last load for ish_gpu_last_load_ms: upload (with the
 // splitting of a text load) and packing.  When the records' bytes travelled on
 // the copy stream, the packing kernels that need only the offsets ran during
@@ -434,6 +430,14 @@ void load_phase_times(ish_ctx *ctx) {
   (void)cudaGetLastError();
 }
 
+// Sort and pack n records held in ctx->raw (raw_bytes bytes): record i is
+// raw[off_in[i] .. end[i]) with `end` on the device, or raw[off_in[i] ..
+// off_in[i + 1]) without; `enc` (device, may be null) encodes bytes on the way
+// (see k_lengths .. k_pack in kernels.cu).  rs.total must hold the residue
+// count.  The kernels run on s; with raw_pending the records' bytes are still
+// on their way on the copy stream and only k_pack waits for them (raw_ev).
+// With defer the host summary is copied into pinned staging and read when the
+// set is first used (finish_pending_load).
 int pack_set(ish_ctx *ctx, uint32_t n, uint64_t raw_bytes, const uint64_t *end, const uint8_t *enc, RecordSet &rs,
              cudaStream_t s, bool defer, bool raw_pending) {
   if (!s) s = ctx->stream;
